@@ -1,0 +1,403 @@
+"""TEST INFRASTRUCTURE -- the oracle (checker) for the band-projection path.
+
+Python driver over ``oracle/liboracle.so`` (the C restatement in oracle.c)
+that reproduces the reference's Python-level flow:
+
+* species setup per element, in POTCAR order (wavefunction.py:386-415,
+  pawpyc.pyx:352-412, projector.c:20-171);
+* sphere tables for all sites and FFT + gather for every band
+  (projector.c:193-209, 560-602; utils.c:590-696);
+* ``make_site_lists`` (projector.py:115-160, with its ``sites[i]`` quirk);
+* ``overlap_setup_real`` (projector.c:604-725): smooth-(phi-phit) tables of the
+  other structure's sites, their projections, the N_RS pair matrices
+  ``conj(reciprocal_offsite_wave_overlap)`` (radial.c:116-196);
+* ``pseudoprojection`` (pseudoprojector.c:63-90) and ``compensation_terms``
+  (projector.c:850-963) for every defect band, as full matrices.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+bench.py use this module; the product path never imports it.  The
+compensation sums are evaluated with numpy in double precision.
+"""
+
+import ctypes as C
+import math
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from pawpyseed_gb300 import vaspio  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.oracle_species_setup.argtypes = [C.c_int, _ip, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
+                                           _dp, C.c_double] + [_dp] * 11
+        L.oracle_site_table.restype = C.c_int
+        L.oracle_site_table.argtypes = [_dp, _ip, _dp, C.c_double, C.c_int, C.c_int, _dp, C.c_int,
+                                        _ip, _dp, _dp, C.c_int, _ip, _dp, _dp]
+        L.oracle_project_bands.argtypes = [C.c_int, _fp, C.c_long, _ip, C.c_int, _ip, _dp, _dp,
+                                           C.c_int, _ip, _lp, _lp, _ip, _ip, C.c_int, _ip, _dp, _dp, _dp]
+        L.oracle_offsite.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, C.c_int,
+                                     C.c_int, C.c_int, C.c_int, C.c_int, _dp,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_pseudo_k.argtypes = [C.c_int, C.c_int, C.c_int, _fp, C.c_long, _fp, C.c_long,
+                                      C.c_int, _dp]
+        L.oracle_fft3d.argtypes = [_dp, _ip, _fp, C.c_int, _ip, C.c_double]
+        L.oracle_spline_coeff.argtypes = [_dp, _dp, C.c_int, _dp, _dp, _dp]
+        L.oracle_legendre.restype = C.c_double
+        L.oracle_legendre.argtypes = [C.c_int, C.c_int, C.c_double]
+        L.oracle_ylm.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_sbt_forward.argtypes = [C.c_double, C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+# --------------------------------------------------------------------------
+# Gaunt-type factors (regenerated from the Wigner 3j symbols, gaunt.py:11-31)
+# --------------------------------------------------------------------------
+
+
+def wigner3j(j1, j2, j3, m1, m2, m3):
+    """Racah's closed form of the Wigner 3j symbol for integer arguments."""
+    if m1 + m2 + m3 != 0 or abs(m1) > j1 or abs(m2) > j2 or abs(m3) > j3:
+        return 0.0
+    if j3 < abs(j1 - j2) or j3 > j1 + j2:
+        return 0.0
+    f = math.factorial
+    tri = f(j1 + j2 - j3) * f(j1 - j2 + j3) * f(-j1 + j2 + j3) / f(j1 + j2 + j3 + 1)
+    pre = math.sqrt(tri * f(j1 + m1) * f(j1 - m1) * f(j2 + m2) * f(j2 - m2) * f(j3 + m3) * f(j3 - m3))
+    s = 0.0
+    kmin = max(0, j2 - j3 - m1, j1 - j3 + m2)
+    kmax = min(j1 + j2 - j3, j1 - m1, j2 + m2)
+    for k in range(kmin, kmax + 1):
+        s += (-1) ** k / (f(k) * f(j3 - j2 + k + m1) * f(j3 - j1 + k - m2) * f(j1 + j2 - j3 - k)
+                          * f(j1 - k - m1) * f(j2 - k + m2))
+    return (-1) ** (j1 - j2 - m3) * pre * s
+
+
+def sbtfacs():
+    """SBTFACS[l1][l2][(L-|l1-l2|)/2][l1+m1][m2], flat float64 [4*4*4*7*4]."""
+    t = np.zeros((4, 4, 4, 7, 4))
+    for l1 in range(4):
+        for l2 in range(l1 + 1):
+            for l3 in range(abs(l1 - l2), l1 + l2 + 1, 2):
+                for m1 in range(-l1, l1 + 1):
+                    for m2 in range(0, l2 + 1):
+                        v = wigner3j(l1, l2, l3, 0, 0, 0) * wigner3j(l1, l2, l3, -m1, m2, m1 - m2)
+                        v *= math.sqrt((2 * l1 + 1) * (2 * l2 + 1) * (2 * l3 + 1) / 4 / math.pi)
+                        t[l1, l2, (l3 - abs(l1 - l2)) // 2, l1 + m1, m2] = v
+    return np.ascontiguousarray(t.reshape(-1))
+
+
+# --------------------------------------------------------------------------
+# species and sites
+# --------------------------------------------------------------------------
+
+
+class OSpecies:
+    def __init__(self, pp, grid_encut):
+        L = lib()
+        self.ls = np.array(pp.ls, dtype=np.int32)
+        self.nproj = len(pp.ls)
+        self.ndata = int(pp.ndata)
+        self.ngrid = len(pp.grid)
+        self.rmax = float(pp.rmax)
+        self.total = int(sum(2 * l + 1 for l in pp.ls))
+        wg = np.ascontiguousarray(pp.grid, dtype=np.float64)
+        proj = np.ascontiguousarray(np.concatenate([p[: self.ndata] for p in pp.realprojs]))
+        ae = np.ascontiguousarray(np.concatenate(pp.aewaves))
+        ps = np.ascontiguousarray(np.concatenate(pp.pswaves))
+        nd, ng, npj = self.ndata, self.ngrid, self.nproj
+        self.wave_grid = wg
+        self.proj = proj
+        self.proj_grid = np.zeros(nd)
+        self.proj_spl = np.zeros(npj * 3 * nd)
+        self.smooth_grid = np.zeros(nd)
+        self.sdw = np.zeros(npj * nd)
+        self.sdw_spl = np.zeros(npj * 3 * nd)
+        self.kgrid = np.zeros(ng)
+        self.kwave = np.zeros(npj * ng)
+        self.kwave_spl = np.zeros(npj * 3 * ng)
+        self.aeov = np.zeros(npj * npj)
+        self.psov = np.zeros(npj * npj)
+        self.diov = np.zeros(npj * npj)
+        L.oracle_species_setup(npj, self.ls, nd, ng, self.rmax, wg, proj, ae, ps, grid_encut,
+                               self.proj_grid, self.proj_spl, self.smooth_grid, self.sdw,
+                               self.sdw_spl, self.kgrid, self.kwave, self.kwave_spl,
+                               self.aeov, self.psov, self.diov)
+        self.wave_rmax = float(wg[-1])
+        # (n, l, m) of each lm channel, in the order of setup_site (utils.c:622-635)
+        self.nlm = [(n, int(l), m) for n, l in enumerate(pp.ls) for m in range(-int(l), int(l) + 1)]
+        D = (self.aeov - self.psov).reshape(npj, npj)
+        T = self.total
+        self.Dfull = np.zeros((T, T))
+        for i, (ni, li, mi) in enumerate(self.nlm):
+            for j, (nj, lj, mj) in enumerate(self.nlm):
+                if li == lj and mi == mj:
+                    self.Dfull[i, j] = D[ni, nj]
+
+
+class SiteTables:
+    """Concatenated sphere tables of a list of sites (setup_site, utils.c:590-696)."""
+
+    def __init__(self, lattice, fftg, site_nums, labels, coords, species, smooth):
+        L = lib()
+        lat = np.ascontiguousarray(lattice, dtype=np.float64).reshape(-1)
+        fg = np.ascontiguousarray(fftg, dtype=np.int32)
+        idx, pth, val, npts, total = [], [], [], [], []
+        for s, p in enumerate(site_nums):
+            sp = species[labels[p]]
+            r0_size = species[labels[s]].ndata  # pps[labels[s]] as utils.c:651-652
+            rmax = sp.wave_rmax if smooth else sp.rmax
+            grid = sp.smooth_grid if smooth else sp.proj_grid
+            f = sp.sdw if smooth else sp.proj
+            spl = sp.sdw_spl if smooth else sp.proj_spl
+            box = [int(np.linalg.norm(np.cross(lat.reshape(3, 3)[(a + 1) % 3], lat.reshape(3, 3)[(a + 2) % 3]))
+                       * rmax / abs(np.linalg.det(lat.reshape(3, 3))) * fftg[a]) + 1 for a in range(3)]
+            cap = int(np.prod([2 * b + 1 for b in box]))
+            ind = np.zeros(cap, np.int32)
+            pa = np.zeros(3 * cap)
+            va = np.zeros(2 * cap * sp.total)
+            n = L.oracle_site_table(lat, fg, np.ascontiguousarray(coords[p], dtype=np.float64), rmax,
+                                    sp.ndata, r0_size, grid, sp.nproj, sp.ls, f, spl, cap, ind, pa, va)
+            if n < 0:
+                raise RuntimeError("sphere table overflow")
+            idx.append(ind[:n])
+            pth.append(pa[: 3 * n])
+            val.append(va[: 2 * n * sp.total])
+            npts.append(n)
+            total.append(sp.total)
+        self.npts = np.array(npts, np.int32)
+        self.total = np.array(total, np.int32)
+        self.toff = np.concatenate([[0], np.cumsum(self.npts)[:-1]]).astype(np.int64)
+        self.voff = np.concatenate([[0], np.cumsum(self.npts * self.total)[:-1]]).astype(np.int64)
+        self.ooff = np.concatenate([[0], np.cumsum(self.total)[:-1]]).astype(np.int32)
+        self.ntot = int(self.total.sum())
+        self.indices = np.ascontiguousarray(np.concatenate(idx) if idx else np.zeros(0, np.int32))
+        self.paths = np.ascontiguousarray(np.concatenate(pth) if pth else np.zeros(0))
+        self.values = np.ascontiguousarray(np.concatenate(val) if val else np.zeros(0))
+        self.nsites = len(site_nums)
+
+    def project(self, cs, gs, fftg, lattice, kcart):
+        """<T|psi> for all bands cs[nb, W] -> complex128 [nb, ntot]."""
+        L = lib()
+        nb, nw = cs.shape
+        out = np.zeros(2 * nb * self.ntot)
+        if self.nsites == 0 or nb == 0:
+            return np.zeros((nb, self.ntot), np.complex128)
+        cf = np.ascontiguousarray(cs.view(np.float32).reshape(-1))
+        L.oracle_project_bands(nb, cf, nw, np.ascontiguousarray(gs.reshape(-1), dtype=np.int32), nw,
+                               np.ascontiguousarray(fftg, dtype=np.int32),
+                               np.ascontiguousarray(lattice, dtype=np.float64).reshape(-1),
+                               np.ascontiguousarray(kcart, dtype=np.float64), self.nsites, self.npts,
+                               self.toff, self.voff, self.total, self.ooff, self.ntot, self.indices,
+                               self.paths, self.values, out)
+        return (out[0::2] + 1j * out[1::2]).reshape(nb, self.ntot)
+
+
+class OracleWavefunction:
+    """One structure: WAVECAR data, species tables and <p|psi> for every band."""
+
+    def __init__(self, path=None, data=None, struct=None, cr=None, dim=None):
+        if path is not None:
+            struct = vaspio.read_poscar(os.path.join(path, "CONTCAR"))
+            cr = vaspio.CoreRegion(os.path.join(path, "POTCAR"))
+            vr = vaspio.Vasprun(os.path.join(path, "vasprun.xml"))
+            dim = [vr.parameters[n] for n in ("NGX", "NGY", "NGZ")]
+            data = vaspio.read_wavecar_numpy(os.path.join(path, "WAVECAR"))
+        self.struct, self.cr = struct, cr
+        self.dim = np.array(dim, np.int32)
+        self.data = data
+        self.nband, self.nwk, self.nspin = data["nband"], data["nwk"], data["nspin"]
+        self.nk = self.nwk * self.nspin
+        self.lattice = np.asarray(data["lattice"], dtype=np.float64)
+        self.kpts = np.asarray(data["kpts"], dtype=np.float64)
+        labels = {e: n for n, e in enumerate(cr.pps)}
+        self.nums = np.array([labels[s] for s in struct.species], np.int32)
+        self.coords = np.ascontiguousarray(struct.frac_coords, dtype=np.float64)
+        self.occs = np.asarray(data["occs"])
+
+    def kcart(self, kidx):
+        return self.kpts[kidx % self.nwk] @ vaspio.reciprocal_lattice(self.lattice)
+
+    def setup_projectors(self):
+        grid_encut = float(np.max((np.pi * self.dim / self.struct.abc) ** 2 / 0.262))
+        self.grid_encut = grid_encut
+        self.species = [OSpecies(self.cr.pps[e], grid_encut) for e in self.cr.pps]
+        self.tables = SiteTables(self.lattice, self.dim, list(range(len(self.struct))), self.nums,
+                                 self.coords, self.species, smooth=False)
+        self.site_off = self.tables.ooff
+        self.P = [self.tables.project(self.data["coeffs"][k], self.data["gs"][k], self.dim,
+                                      self.lattice, self.kcart(k)) for k in range(self.nk)]
+
+    def site_block(self, P, s):
+        o = self.site_off[s]
+        return P[:, o: o + self.tables.total[s]]
+
+
+def site_lists(basis_struct, wf_struct, basis_cr, wf_cr):
+    """Restatement of Projector.make_site_lists (projector.py:115-160), quirk included."""
+    ref, cur = basis_struct, wf_struct
+    M_R, M_S = [], []
+    for i in range(len(ref)):
+        for j in range(len(cur)):
+            if ref.distance(i, cur, j) <= 0.02 and ref.species[i] == cur.species[j]:
+                M_R.append(i)
+                M_S.append(j)
+    N_R = [i for i in range(len(ref)) if i not in M_R]
+    N_S = [j for j in range(len(cur)) if j not in M_S]
+    N_RS = []
+    for i in N_R:
+        for j in N_S:
+            rmax1 = basis_cr.pps[ref.species[i]].rmax
+            rmax2 = wf_cr.pps[cur.species[i]].rmax
+            if ref.distance(i, cur, j) < rmax1 + rmax2:
+                N_RS.append((i, j))
+    return M_R, M_S, N_R, N_S, N_RS
+
+
+def min_cart_path(coord, center, lattice):
+    """utils.c:51-73 (first strict minimum over the 27 images, i outer)."""
+    best, path = np.inf, None
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for k in (-1, 0, 1):
+                v = (np.asarray(coord) + [i, j, k] - np.asarray(center)) @ lattice
+                d = math.sqrt(float(v @ v))
+                if d < best:
+                    best, path = d, v
+    return path, best
+
+
+class OracleProjector:
+    """aug_real projection of wf (S) onto basis (R), full matrices in FP64."""
+
+    def __init__(self, wf, basis, lists=None):
+        self.wf, self.basis = wf, basis
+        L = lib()
+        for w in (basis, wf):
+            if not hasattr(w, "P"):
+                w.setup_projectors()
+        if lists is None:
+            lists = site_lists(basis.struct, wf.struct, basis.cr, wf.cr)
+        self.M_R, self.M_S, self.N_R, self.N_S, N_RS = lists
+        self.N_RS_R = [a for a, _ in N_RS]
+        self.N_RS_S = [b for _, b in N_RS]
+        nk = basis.nk
+        # <(phi-phit)_R|psi_S> on N_R sites of R in S's grid (projector.c:625-646)
+        self.WP_S = [np.zeros((wf.nband, 0), np.complex128)] * nk
+        self.WP_R = [np.zeros((basis.nband, 0), np.complex128)] * nk
+        if self.N_R:
+            tab = SiteTables(wf.lattice, wf.dim, self.N_R, basis.nums, basis.coords, basis.species, True)
+            self.tab_NR = tab
+            self.WP_S = [tab.project(wf.data["coeffs"][k], wf.data["gs"][k], wf.dim, wf.lattice,
+                                     wf.kcart(k)) for k in range(nk)]
+        if self.N_S:
+            tab = SiteTables(basis.lattice, basis.dim, self.N_S, wf.nums, wf.coords, wf.species, True)
+            self.tab_NS = tab
+            self.WP_R = [tab.project(basis.data["coeffs"][k], basis.data["gs"][k], basis.dim,
+                                     basis.lattice, basis.kcart(k)) for k in range(nk)]
+        # N_RS pair matrices (projector.c:682-719)
+        facs = sbtfacs()
+        self.Q, self.dcoords = [], []
+        for s1, s2 in zip(self.N_RS_R, self.N_RS_S):
+            sp1 = basis.species[basis.nums[s1]]
+            sp2 = wf.species[wf.nums[s2]]
+            dc, _ = min_cart_path(wf.coords[s2], basis.coords[s1], basis.lattice)
+            dc = np.ascontiguousarray(dc, dtype=np.float64)
+            Q = np.zeros((sp1.total, sp2.total), np.complex128)
+            ng1, ng2 = sp1.ngrid, sp2.ngrid
+            for tj, (n1, l1, m1) in enumerate(sp1.nlm):
+                f1 = np.ascontiguousarray(sp1.kwave[n1 * ng1:(n1 + 1) * ng1])
+                s1p = np.ascontiguousarray(sp1.kwave_spl[n1 * 3 * ng1:(n1 + 1) * 3 * ng1])
+                for tk, (n2, l2, m2) in enumerate(sp2.nlm):
+                    f2 = np.ascontiguousarray(sp2.kwave[n2 * ng2:(n2 + 1) * ng2])
+                    s2p = np.ascontiguousarray(sp2.kwave_spl[n2 * 3 * ng2:(n2 + 1) * 3 * ng2])
+                    re, im = C.c_double(), C.c_double()
+                    L.oracle_offsite(dc, sp1.kgrid, f1, s1p, ng1, sp2.kgrid, f2, s2p, ng2,
+                                     l1, m1, l2, m2, facs, C.byref(re), C.byref(im))
+                    Q[tj, tk] = complex(re.value, -im.value)  # conj, projector.c:706
+            self.Q.append(Q)
+            self.dcoords.append(dc)
+
+    def _kR(self, k, flip):
+        b = self.basis
+        if b.nspin == 2 and flip:
+            return k + b.nwk if k < b.nwk else k - b.nwk
+        return k
+
+    def pseudo_full(self, flip_spin=False, fp32=False):
+        """S[k][bS, bR] = <C_R,bR,kR|C_S,bS,k> (complex128 [nk, nbS, nbR])."""
+        L = lib()
+        b, w = self.basis, self.wf
+        out = np.zeros((b.nk, w.nband, b.nband), np.complex128)
+        for k in range(b.nk):
+            kR = self._kR(k, flip_spin)
+            CR = np.ascontiguousarray(b.data["coeffs"][kR].view(np.float32).reshape(-1))
+            CS = np.ascontiguousarray(w.data["coeffs"][k].view(np.float32).reshape(-1))
+            nw = b.data["coeffs"][k].shape[1]
+            tmp = np.zeros(2 * w.nband * b.nband)
+            L.oracle_pseudo_k(b.nband, w.nband, nw, CR, b.data["coeffs"][kR].shape[1], CS,
+                              w.data["coeffs"][k].shape[1], int(fp32), tmp)
+            out[k] = (tmp[0::2] + 1j * tmp[1::2]).reshape(w.nband, b.nband)
+        return out
+
+    def comp_full(self, flip_spin=False):
+        """The PAW terms O_M + O_R + O_S + O_N (projector.c:850-963), [nk, nbS, nbR]."""
+        b, w = self.basis, self.wf
+        out = np.zeros((b.nk, w.nband, b.nband), np.complex128)
+        for k in range(b.nk):
+            kR = self._kR(k, flip_spin)
+            PR, PS = b.P[kR], w.P[k]
+            acc = np.zeros((b.nband, w.nband), np.complex128)
+            for s1, s2 in zip(self.M_R, self.M_S):
+                sp = b.species[b.nums[s1]]
+                acc += b.site_block(PR, s1).conj() @ sp.Dfull @ w.site_block(PS, s2).T
+            for si, s in enumerate(self.N_R):
+                pr = b.site_block(PR, s)
+                o = self.tab_NR.ooff[si]
+                ws = self.WP_S[k][:, o:o + self.tab_NR.total[si]]
+                acc += pr.conj() @ ws.T
+            for si, s in enumerate(self.N_S):
+                ps = w.site_block(PS, s)
+                o = self.tab_NS.ooff[si]
+                wr = self.WP_R[kR][:, o:o + self.tab_NS.total[si]]
+                acc += wr.conj() @ ps.T
+            kv = b.kpts[kR % b.nwk]
+            for Q, dc, s1, s2 in zip(self.Q, self.dcoords, self.N_RS_R, self.N_RS_S):
+                ph = np.exp(2j * np.pi * float(kv @ dc))
+                acc += (b.site_block(PR, s1).conj() @ Q @ w.site_block(PS, s2).T) * ph
+            out[k] = acc.T
+        return out
+
+    def full(self, flip_spin=False, fp32=False):
+        return self.pseudo_full(flip_spin, fp32) + self.comp_full(flip_spin)
+
+    @staticmethod
+    def band_vector(full, band):
+        """single_band_projection layout: res[bR*nk + k] from a [nk, nbS, nbR] matrix."""
+        return np.ascontiguousarray(full[:, band, :].T.reshape(-1))
