@@ -1,0 +1,295 @@
+/* pawpy_gpu.h -- C ABI of the GB300 band-projection library (libpawpy_gpu.so).
+ *
+ * Drop-in for the hot path of pawpyseed's C core: the structs below have the
+ * binary layout of pawpyseed/core/utils.h:30-166 (the Cython layer reads
+ * pswf_t members directly, e.g. pawpyc.pyx:537), and the seven entry points
+ * in section 2 keep the exact names and signatures that pawpyc_extern.pxd
+ * declares, so the Cython extension links against this library unchanged.
+ * Section 3 adds batched entry points, status reporting and host helpers;
+ * they use a pawpy_gpu_ prefix so that they never collide with reference
+ * symbols.
+ *
+ * Every computation runs on one CUDA device (the current device when the
+ * library first touches a wavefunction); there is no CPU fallback. No entry
+ * point aborts the process: on failure a call leaves its outputs unspecified
+ * and records a status that pawpy_gpu_last_error() returns (0 = success).
+ */
+#ifndef PAWPY_GPU_H
+#define PAWPY_GPU_H
+
+#ifdef __cplusplus
+#include <complex>
+typedef std::complex<double> pawpy_c128;
+typedef std::complex<float> pawpy_c64;
+extern "C" {
+#else
+#include <complex.h>
+typedef double complex pawpy_c128;
+typedef float complex pawpy_c64;
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* 1. Structs (layout of pawpyseed/core/utils.h:30-166)                    */
+/* ---------------------------------------------------------------------- */
+
+typedef struct funcset {
+  int l;
+  double *proj;
+  double **proj_spline;
+  double *aewave;
+  double **aewave_spline;
+  double *pswave;
+  double **pswave_spline;
+  double *diffwave;
+  double **diffwave_spline;
+  double *kwave;
+  double **kwave_spline;
+  double *smooth_diffwave;
+  double **smooth_diffwave_spline;
+  double *dense_kwave;
+  double **dense_kwave_spline;
+} funcset_t;
+
+typedef struct ppot {
+  int num_projs;
+  int total_projs;
+  int lmax;
+  funcset_t *funcs;
+  double rmax;
+  double wave_rmax;
+  double *pspw_overlap_matrix;
+  double *aepw_overlap_matrix;
+  double *diff_overlap_matrix;
+  int proj_gridsize;
+  int wave_gridsize;
+  int num_cart_gridpts;
+  double *wave_grid;
+  double *kwave_grid;
+  double *proj_grid;
+  double *smooth_grid;
+  double *dense_kgrid;
+} ppot_t;
+
+typedef struct projection {
+  int num_projs;
+  int total_projs;
+  int *ns;
+  int *ls;
+  int *ms;
+  pawpy_c128 *overlaps;
+} projection_t;
+
+typedef struct band {
+  int n;
+  int num_waves;
+  double occ;
+  double N;
+  double energy;
+  pawpy_c64 *Cs;
+  pawpy_c128 *CRs;
+  pawpy_c64 *CAs;
+  projection_t *projections;
+  projection_t *up_projections;
+  projection_t *down_projections;
+  projection_t *wave_projections;
+} band_t;
+
+typedef struct rayleigh_set {
+  int l;
+  pawpy_c128 *terms;
+} rayleigh_set_t;
+
+typedef struct kpoint {
+  short int up;
+  int num_waves;
+  int *Gs;
+  double *k;
+  double weight;
+  int num_bands;
+  band_t **bands;
+  rayleigh_set_t **expansion;
+} kpoint_t;
+
+typedef struct pswf {
+  double encut;
+  int num_elems;
+  int *num_projs;
+  int num_sites;
+  ppot_t *pps;
+  int *G_bounds;
+  kpoint_t **kpts;
+  int nspin;
+  int nband;
+  int nwk;
+  double *lattice;
+  double *reclattice;
+  int *fftg;
+  int is_ncl;
+  int wp_num;
+  int num_aug_overlap_sites;
+  double *dcoords;
+  pawpy_c128 **overlaps;
+} pswf_t;
+
+typedef struct real_proj {
+  int l;
+  int m;
+  int func_num;
+  pawpy_c128 *values;
+} real_proj_t;
+
+typedef struct real_proj_site {
+  int index;
+  int elem;
+  int num_projs;
+  int total_projs;
+  int num_indices;
+  int gridsize;
+  double rmax;
+  double *coord;
+  int *indices;
+  double *paths;
+  real_proj_t *projs;
+} real_proj_site_t;
+
+/* ---------------------------------------------------------------------- */
+/* 2. Drop-in entry points (names and signatures of pawpyc_extern.pxd)     */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces pseudoprojection (pseudoprojector.c:63-90; declared
+ * pawpyc_extern.pxd, called pawpyc.pyx:324). projections[b*NK + k] =
+ * <C_ref,b,k'|C_proj,BAND_NUM,k> for every basis band b and k = 0..NK-1
+ * (NK = nwk*nspin; k' = k with the spins swapped when flip_spin and nspin==2).
+ * Overwrites projections. Computed on the device as part of the full
+ * basis x defect overlap matrix, which is cached per (wf_ref, wf_proj, flip)
+ * so that a loop over BAND_NUM costs one matrix product. */
+void pseudoprojection(pawpy_c128 *projections, pswf_t *wf_ref, pswf_t *wf_proj,
+                      int BAND_NUM, int flip_spin);
+
+/* Replaces get_projector_list (projector.c:20-171 with
+ * make_pwave_overlap_matrices projector.c:507-558 and the spherical Bessel
+ * transforms of sbt.c; called pawpyc.pyx:392-395). labels holds 4 ints per
+ * element: [label, nproj, ndata, ngrid]. Returns a malloc'd ppot_t[num_els]
+ * whose members are laid out and owned as the reference's (freed by
+ * free_pswf once setup_projections has attached it). The radial work runs on
+ * the device in double precision. */
+ppot_t *get_projector_list(int num_els, int *labels, int *ls, double *wave_grids,
+                           double *projectors, double *aewaves, double *pswaves,
+                           double *rmaxs, double grid_encut);
+
+/* Replaces setup_projections (projector.c:560-602; called pawpyc.pyx:406-410).
+ * Attaches pps to wf (takes ownership), builds the augmentation-sphere tables
+ * of every site on the device, and computes <p_i|psi> for every band and
+ * k-point (batched scatter + 3D FFT + sphere gather). Unless disabled with
+ * pawpy_gpu_set_host_projections(0), also fills band->projections as malloc'd
+ * projection_t arrays, as the reference does. */
+void setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num_sites,
+                       int *fftg, int *labels, double *coords);
+
+/* Replaces onto_projector (projector.c:333-357): <p_i|psi> of one band from
+ * host sphere tables; fills kpt->bands[band_num]->projections. */
+void onto_projector(kpoint_t *kpt, int band_num, real_proj_site_t *sites,
+                    int num_sites, int *G_bounds, double *lattice,
+                    double *reclattice, int num_cart_gridpts, int *fftg);
+
+/* Replaces overlap_setup_real (projector.c:604-725; called pawpyc.pyx:680-683).
+ * <(phi-phit)|psi> on the other structure's sites (smoothed partial waves,
+ * N_R for wf_S bands and N_S for wf_R bands) and the N_RS pair matrices
+ * conj(<(phi-phit)_R|(phi-phit)_S>) with the minimum-image displacements.
+ * Empty site lists may be NULL. Sets wf_S->overlaps/dcoords/
+ * num_aug_overlap_sites and wp_num as the reference does; wave_projections
+ * are filled on the host unless host projections are disabled. */
+void overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, int *labels_R, int *labels_S,
+                        double *coords_R, double *coords_S, int *N_R, int *N_S,
+                        int *N_RS_R, int *N_RS_S, int num_N_R, int num_N_S,
+                        int num_N_RS);
+
+/* Replaces compensation_terms (projector.c:850-963; called pawpyc.pyx:698-702;
+ * argument order wf_S = defect, wf_R = basis). Adds O_M + O_R + O_S + O_N of
+ * defect band BAND_NUM into overlap[b*NK + k], computed on the device in
+ * double precision from the device copies of the projector coefficients. */
+void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S,
+                        pswf_t *wf_R, int num_M, int num_N_R, int num_N_S,
+                        int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S,
+                        int *N_RS_R, int *N_RS_S, int *proj_labels,
+                        double *proj_coords, int *ref_labels, double *ref_coords,
+                        int *fft_grid, int flip_spin);
+
+/* Replaces fft3d (linalg.c:14-45; called from C only). x[i*N2*N3 + j*N3 + k] =
+ * V^-1/2 sum_w Cs[w] exp(2 pi i (g1 i/N1 + g2 j/N2 + g3 k/N3)). The transform
+ * runs on the device in single precision (|error| well below the 1e-5 that
+ * the reference's fft_check allows, tests.c:61). */
+void fft3d(pawpy_c128 *x, int *G_bounds, double *lattice, double *kpt, int *Gs,
+           pawpy_c64 *Cs, int num_waves, int *fftg);
+
+/* ---------------------------------------------------------------------- */
+/* 3. Library extensions (no counterpart in the reference)                 */
+/* ---------------------------------------------------------------------- */
+
+enum pawpy_gpu_precision {
+  PAWPY_GPU_FP32 = 0,   /* complex FP32 overlap GEMM on the CUDA cores */
+  PAWPY_GPU_BF16X3 = 1, /* split-BF16 (3 terms) on the tensor cores, FP32 accumulate */
+  PAWPY_GPU_TF32 = 2    /* TF32 tensor cores, FP32 accumulate (reported variant) */
+};
+
+/* Status of the last entry point called on this thread: 0 on success. */
+int pawpy_gpu_last_error(void);
+/* Human-readable message for the last failure on this thread ("" if none). */
+const char *pawpy_gpu_error_string(void);
+/* Clears the recorded status. */
+void pawpy_gpu_clear_error(void);
+
+/* Overlap precision for the device overlap matrices (default FP32). */
+void pawpy_gpu_set_precision(int precision);
+int pawpy_gpu_get_precision(void);
+/* Whether setup_projections / overlap_setup_real also fill the host
+ * projection_t arrays (default 1, as the reference). */
+void pawpy_gpu_set_host_projections(int on);
+
+/* Full PAW overlap matrix of every defect band against every basis band:
+ * out[bS*(NB_R*NK) + bR*NK + k] = single_band_projection(bS)[bR*NK + k],
+ * i.e. pseudo overlap plus O_M + O_R + O_S + O_N, computed as one augmented
+ * overlap contraction per k-point. Needs setup_projections on both and
+ * overlap_setup_real with the same site lists. Returns 0 on success. */
+int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M,
+                          int num_N_R, int num_N_S, int num_N_RS, int *M_R,
+                          int *M_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S,
+                          int flip_spin);
+
+/* WAVECAR reader producing a pswf_t with the reference's layout and VASP plane-
+ * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf. */
+pswf_t *pawpy_gpu_read_wavefunctions(const char *filename, const double *kpt_weights);
+/* Builds a pswf_t from in-memory arrays: Gs[iwk] int32[3*nplane[iwk]] and
+ * Cs[iwk] complex64[nband*nplane[iwk]] for iwk = spin*nwk + k. Copies them. */
+pswf_t *pawpy_gpu_wavefunction_from_arrays(int nspin, int nwk, int nband, double encut,
+                                           const double *lattice, const double *kpts,
+                                           const double *weights, const int *nplane,
+                                           const int *const *Gs, const pawpy_c64 *const *Cs,
+                                           const double *energies, const double *occs);
+/* Frees a pswf_t and everything attached to it (also releases its device copy). */
+void pawpy_gpu_free_pswf(pswf_t *wf);
+/* Releases the device copy of a wavefunction (call before a foreign free). */
+void pawpy_gpu_release(pswf_t *wf);
+/* Makes the device copy of a wavefunction's coefficients resident now. */
+int pawpy_gpu_upload(pswf_t *wf);
+
+/* Device-side timing on the library's stream (CUDA events). */
+void pawpy_gpu_timer_start(void);
+float pawpy_gpu_timer_stop_ms(void); /* synchronizes */
+void pawpy_gpu_synchronize(void);
+/* Kernels launched by this library since the counter was last reset. */
+long long pawpy_gpu_launch_count(int reset);
+/* Per-kernel-family device time: enables CUDA-event bracketing of launches;
+ * pawpy_gpu_kernel_stats writes "name ms launches\n" lines into buf. */
+void pawpy_gpu_profile(int on);
+int pawpy_gpu_kernel_stats(char *buf, int len, int reset);
+/* Bytes of device memory the library holds. */
+long long pawpy_gpu_device_bytes(void);
+/* Byte offset / size of each struct member, for layout checks:
+ * writes "struct member offset\n" lines; returns the length needed. */
+int pawpy_gpu_struct_layout(char *buf, int len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

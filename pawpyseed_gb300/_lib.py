@@ -1,0 +1,138 @@
+"""ctypes binding of libpawpy_gpu.so (the C ABI declared in include/pawpy_gpu.h).
+
+The library is built in-tree (``pawpyseed_gb300/lib/libpawpy_gpu.so``) by
+``pawpyseed_gb300.build``. Loading fails loudly if it is missing: there is no
+other implementation of the path behind this package.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import structs as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpawpy_gpu.so")
+
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_zp = np.ctypeslib.ndpointer(dtype=np.complex128, flags="C_CONTIGUOUS")
+_wfp = C.POINTER(S.pswf_t)
+_ppp = C.POINTER(S.ppot_t)
+_vp = C.c_void_p
+
+PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2}
+
+
+class PAWpyGPUError(RuntimeError):
+    """A failure reported by libpawpy_gpu (status code and message)."""
+
+    def __init__(self, code, msg):
+        super().__init__("libpawpy_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _declare(L):
+    L.pawpy_gpu_last_error.restype = C.c_int
+    L.pawpy_gpu_error_string.restype = C.c_char_p
+    L.pawpy_gpu_read_wavefunctions.restype = _wfp
+    L.pawpy_gpu_read_wavefunctions.argtypes = [C.c_char_p, _dp]
+    L.pawpy_gpu_wavefunction_from_arrays.restype = _wfp
+    L.pawpy_gpu_wavefunction_from_arrays.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
+                                                    _ip, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                                    _dp, _dp]
+    L.pawpy_gpu_free_pswf.argtypes = [_wfp]
+    L.pawpy_gpu_release.argtypes = [_wfp]
+    L.pawpy_gpu_upload.argtypes = [_wfp]
+    L.pawpy_gpu_upload.restype = C.c_int
+    L.get_projector_list.restype = _ppp
+    L.get_projector_list.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double]
+    L.setup_projections.argtypes = [_wfp, _ppp, C.c_int, C.c_int, _ip, _ip, _dp]
+    L.overlap_setup_real.argtypes = [_wfp, _wfp, _ip, _ip, _dp, _dp, _vp, _vp, _vp, _vp,
+                                     C.c_int, C.c_int, C.c_int]
+    L.pseudoprojection.argtypes = [_zp, _wfp, _wfp, C.c_int, C.c_int]
+    L.compensation_terms.argtypes = [_zp, C.c_int, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     _vp, _vp, _vp, _vp, _vp, _vp, _ip, _dp, _ip, _dp, _ip, C.c_int]
+    L.pawpy_gpu_project_all.restype = C.c_int
+    L.pawpy_gpu_project_all.argtypes = [_zp, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    L.fft3d.argtypes = [_zp, _vp, _dp, _dp, _ip, _vp, C.c_int, _ip]
+    L.onto_projector.argtypes = [C.POINTER(S.kpoint_t), C.c_int, C.POINTER(S.real_proj_site_t), C.c_int,
+                                 _vp, _dp, _dp, C.c_int, _ip]
+    L.pawpy_gpu_set_precision.argtypes = [C.c_int]
+    L.pawpy_gpu_get_precision.restype = C.c_int
+    L.pawpy_gpu_set_host_projections.argtypes = [C.c_int]
+    L.pawpy_gpu_timer_stop_ms.restype = C.c_float
+    L.pawpy_gpu_launch_count.restype = C.c_longlong
+    L.pawpy_gpu_launch_count.argtypes = [C.c_int]
+    L.pawpy_gpu_profile.argtypes = [C.c_int]
+    L.pawpy_gpu_kernel_stats.restype = C.c_int
+    L.pawpy_gpu_kernel_stats.argtypes = [C.c_char_p, C.c_int, C.c_int]
+    L.pawpy_gpu_device_bytes.restype = C.c_longlong
+    L.pawpy_gpu_struct_layout.restype = C.c_int
+    L.pawpy_gpu_struct_layout.argtypes = [C.c_char_p, C.c_int]
+
+
+def lib():
+    """The loaded library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libpawpy_gpu.so is not built (run python -m pawpyseed_gb300.build): %s"
+                              % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def check():
+    """Raise PAWpyGPUError if the last library call on this thread failed."""
+    L = lib()
+    code = L.pawpy_gpu_last_error()
+    if code:
+        msg = L.pawpy_gpu_error_string().decode(errors="replace")
+        L.pawpy_gpu_clear_error()
+        raise PAWpyGPUError(code, msg)
+
+
+def ptr(a):
+    """ctypes void* of a numpy array, or NULL when it is empty (as pawpyc.pyx:660-665)."""
+    return None if a is None or len(a) == 0 else a.ctypes.data_as(C.c_void_p)
+
+
+def set_precision(name):
+    lib().pawpy_gpu_set_precision(PRECISIONS[name])
+
+
+def get_precision():
+    v = lib().pawpy_gpu_get_precision()
+    return {b: a for a, b in PRECISIONS.items()}[v]
+
+
+def kernel_stats(reset=True):
+    L = lib()
+    n = L.pawpy_gpu_kernel_stats(None, 0, 0)
+    buf = C.create_string_buffer(max(n, 1))
+    L.pawpy_gpu_kernel_stats(buf, len(buf), int(reset))
+    check()
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, ms, cnt = line.split()
+        out[name] = (float(ms), int(cnt))
+    return out
+
+
+def struct_layout():
+    L = lib()
+    n = L.pawpy_gpu_struct_layout(None, 0)
+    buf = C.create_string_buffer(n)
+    L.pawpy_gpu_struct_layout(buf, n)
+    rows = []
+    for line in buf.value.decode().splitlines():
+        s, m, off = line.split()
+        rows.append((s, m, int(off)))
+    return rows

@@ -1,0 +1,134 @@
+// Internal runtime of libpawpy_gpu: error status, the library stream,
+// stream-ordered device buffers and launch accounting.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pawpy_gpu.h"
+
+namespace pawpy {
+
+// Error raised inside the library; every extern "C" entry point catches it and
+// records the status instead of aborting (the reference exits on failure,
+// utils.c:1100-1118).
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+enum ErrCode {
+  ERR_CUDA = 1,
+  ERR_ARG = 2,
+  ERR_STATE = 3,
+  ERR_IO = 4,
+  ERR_UNSUPPORTED = 5,
+  ERR_ALLOC = 6,
+  ERR_DEVICE_FLAG = 7,
+};
+
+void set_error(int code, const char *msg);
+void clear_error();
+
+#define PAWPY_CUDA(call)                                                          \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      throw ::pawpy::Error(::pawpy::ERR_CUDA, std::string(#call) + ": " +         \
+                                                  cudaGetErrorString(e_));        \
+  } while (0)
+
+#define PAWPY_REQUIRE(cond, msg)                                                  \
+  do {                                                                            \
+    if (!(cond)) throw ::pawpy::Error(::pawpy::ERR_ARG, (msg));                   \
+  } while (0)
+
+// Wraps the body of an extern "C" entry point.
+#define PAWPY_API_BEGIN try { ::pawpy::clear_error();
+#define PAWPY_API_END(ret)                                                        \
+  }                                                                               \
+  catch (const ::pawpy::Error &e) {                                               \
+    ::pawpy::set_error(e.code, e.what());                                         \
+    return ret;                                                                   \
+  }                                                                               \
+  catch (const std::bad_alloc &) {                                                \
+    ::pawpy::set_error(::pawpy::ERR_ALLOC, "host allocation failed");             \
+    return ret;                                                                   \
+  }                                                                               \
+  catch (const std::exception &e) {                                               \
+    ::pawpy::set_error(::pawpy::ERR_STATE, e.what());                             \
+    return ret;                                                                   \
+  }
+
+// The single stream every kernel and copy of the library is ordered on.
+cudaStream_t stream();
+int device();
+void sync();
+
+// Stream-ordered device allocation (cudaMallocAsync from the device's default
+// pool, whose release threshold is raised so that memory is reused between
+// calls instead of returned to the driver).
+void *dmalloc(size_t bytes);
+void dfree(void *p);
+long long device_bytes();
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) { reset(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void alloc(size_t count) {
+    reset();
+    n = count;
+    if (count) p = static_cast<T *>(dmalloc(count * sizeof(T)));
+  }
+  void reset() {
+    if (p) dfree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void zero() {
+    if (n) PAWPY_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), stream()));
+  }
+  void upload(const T *h, size_t count, size_t off = 0) {
+    if (count) PAWPY_CUDA(cudaMemcpyAsync(p + off, h, count * sizeof(T), cudaMemcpyHostToDevice, stream()));
+  }
+  void download(T *h, size_t count, size_t off = 0) const {
+    if (count) PAWPY_CUDA(cudaMemcpyAsync(h, p + off, count * sizeof(T), cudaMemcpyDeviceToHost, stream()));
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Launch accounting: every kernel launch goes through launch_begin/launch_end
+// so that the count (and, when profiling, per-family device time) is known.
+void launch_begin(const char *family);
+void launch_end(const char *family);
+void check_launch(const char *what);
+
+// PAWPY_LAUNCH("family", kernel<<<grid, block, smem, pawpy::stream()>>>(args));
+#define PAWPY_LAUNCH(family, ...)                                                 \
+  do {                                                                            \
+    ::pawpy::launch_begin(family);                                                \
+    __VA_ARGS__;                                                                  \
+    ::pawpy::check_launch(family);                                                \
+    ::pawpy::launch_end(family);                                                  \
+  } while (0)
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace pawpy

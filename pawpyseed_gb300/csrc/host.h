@@ -1,0 +1,44 @@
+// Host-side declarations shared by the translation units of libpawpy_gpu.
+#pragma once
+
+#include <vector>
+
+#include "common.h"
+
+namespace pawpy {
+
+// --- wavefunction files and ownership (host_wavecar.cpp) ---
+double det3(const double *m);
+void reciprocal(const double *lat, double *rec);
+std::vector<int> enumerate_gvectors(const double *rec, const double *k, double encut);
+pswf_t *read_wavecar(const char *path, const double *kws);
+pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const double *lattice,
+                         const double *kpts, const double *weights, const int *nplane,
+                         const int *const *Gs, const pawpy_c64 *const *Cs, const double *energies,
+                         const double *occs);
+void free_pswf_all(pswf_t *wf);
+void free_ppot_array(ppot_t *pps, int n);
+void free_wave_projections(pswf_t *wf);
+
+// --- radial setup (host_radial.cpp) ---
+// Cubic spline coefficients in the reference's convention (utils.c:699-749):
+// b, c, d such that f(x) = y_i + t(b_i + t(c_i + t d_i)), t = x - x_i.
+void spline_coeffs(const double *x, const double *y, int n, double *b, double *c, double *d);
+double spline_integral(const double *x, const double *y, const double *b, const double *c,
+                       const double *d, int n);
+double interp_log(double r, int n, const double *x, const double *f, double *const *s);
+ppot_t *build_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
+                             const double *projectors, const double *aewaves, const double *pswaves,
+                             const double *rmaxs, double grid_encut);
+// conj(<(phi-phit)_1 lm | (phi-phit)_2 l'm'>) matrix of one site pair
+// (reciprocal_offsite_wave_overlap, radial.c:116-196), row-major [P1 x P2].
+void offsite_pair_matrix(const ppot_t *pp1, const ppot_t *pp2, const double *dcoord,
+                         pawpy_c128 *out);
+// Minimum-image Cartesian path coord - center (utils.c:51-73).
+void min_image_path(const double *coord, const double *center, const double *lattice, double *path,
+                    double *r);
+
+// --- device mirror lifetime (engine.cu) ---
+void release_device(pswf_t *wf);
+
+}  // namespace pawpy

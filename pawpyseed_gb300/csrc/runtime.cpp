@@ -1,0 +1,228 @@
+// Error status, the library stream, stream-ordered allocation, launch
+// accounting and timers of libpawpy_gpu.
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "common.h"
+
+namespace pawpy {
+
+static thread_local int g_err = 0;
+static thread_local std::string g_msg;
+
+void set_error(int code, const char *msg) {
+  g_err = code;
+  g_msg = msg ? msg : "";
+}
+void clear_error() {
+  g_err = 0;
+  g_msg.clear();
+}
+
+namespace {
+struct Runtime {
+  bool ready = false;
+  int dev = 0;
+  cudaStream_t s = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  long long launches = 0;
+  long long bytes = 0;
+  std::map<void *, size_t> sizes;
+  bool profile = false;
+  struct Fam {
+    double ms = 0;
+    long long n = 0;
+  };
+  std::map<std::string, Fam> fams;
+  std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::recursive_mutex mu;
+};
+Runtime &rt() {
+  static Runtime r;
+  return r;
+}
+
+void init_locked(Runtime &r) {
+  if (r.ready) return;
+  PAWPY_CUDA(cudaGetDevice(&r.dev));
+  PAWPY_CUDA(cudaStreamCreateWithFlags(&r.s, cudaStreamNonBlocking));
+  PAWPY_CUDA(cudaEventCreate(&r.t0));
+  PAWPY_CUDA(cudaEventCreate(&r.t1));
+  cudaMemPool_t pool;
+  PAWPY_CUDA(cudaDeviceGetDefaultMemPool(&pool, r.dev));
+  uint64_t thr = ~0ull;
+  PAWPY_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  r.ready = true;
+}
+
+cudaEvent_t take_event(Runtime &r) {
+  if (!r.event_pool.empty()) {
+    cudaEvent_t e = r.event_pool.back();
+    r.event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  PAWPY_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void drain_locked(Runtime &r) {
+  for (auto &p : r.pending) {
+    float ms = 0;
+    PAWPY_CUDA(cudaEventSynchronize(p.second.second));
+    PAWPY_CUDA(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+    auto &f = r.fams[p.first];
+    f.ms += ms;
+    f.n += 1;
+    r.event_pool.push_back(p.second.first);
+    r.event_pool.push_back(p.second.second);
+  }
+  r.pending.clear();
+}
+}  // namespace
+
+cudaStream_t stream() {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  init_locked(r);
+  return r.s;
+}
+
+int device() {
+  stream();
+  return rt().dev;
+}
+
+void sync() { PAWPY_CUDA(cudaStreamSynchronize(stream())); }
+
+void *dmalloc(size_t bytes) {
+  cudaStream_t s = stream();
+  void *p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(ERR_ALLOC, std::string("device allocation of ") + std::to_string(bytes) +
+                               " bytes failed: " + cudaGetErrorString(e));
+  }
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  r.sizes[p] = bytes;
+  r.bytes += (long long)bytes;
+  return p;
+}
+
+void dfree(void *p) {
+  if (!p) return;
+  Runtime &r = rt();
+  {
+    std::lock_guard<std::recursive_mutex> g(r.mu);
+    auto it = r.sizes.find(p);
+    if (it != r.sizes.end()) {
+      r.bytes -= (long long)it->second;
+      r.sizes.erase(it);
+    }
+  }
+  cudaFreeAsync(p, stream());
+}
+
+long long device_bytes() { return rt().bytes; }
+
+void launch_begin(const char *family) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  init_locked(r);
+  r.launches++;
+  if (r.profile) {
+    cudaEvent_t a = take_event(r), b = take_event(r);
+    PAWPY_CUDA(cudaEventRecord(a, r.s));
+    r.pending.push_back({family, {a, b}});
+  }
+}
+
+void launch_end(const char *family) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  if (r.profile && !r.pending.empty() && r.pending.back().first == family)
+    PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, r.s));
+}
+
+void check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    throw Error(ERR_CUDA, std::string("launch of ") + what + " failed: " + cudaGetErrorString(e));
+}
+
+}  // namespace pawpy
+
+using namespace pawpy;
+
+extern "C" {
+
+int pawpy_gpu_last_error(void) { return g_err; }
+const char *pawpy_gpu_error_string(void) { return g_msg.c_str(); }
+void pawpy_gpu_clear_error(void) { clear_error(); }
+
+void pawpy_gpu_timer_start(void) {
+  PAWPY_API_BEGIN
+  Runtime &r = rt();
+  stream();
+  PAWPY_CUDA(cudaEventRecord(r.t0, r.s));
+  PAWPY_API_END()
+}
+
+float pawpy_gpu_timer_stop_ms(void) {
+  PAWPY_API_BEGIN
+  Runtime &r = rt();
+  PAWPY_CUDA(cudaEventRecord(r.t1, stream()));
+  PAWPY_CUDA(cudaEventSynchronize(r.t1));
+  float ms = 0;
+  PAWPY_CUDA(cudaEventElapsedTime(&ms, r.t0, r.t1));
+  return ms;
+  PAWPY_API_END(-1.0f)
+}
+
+void pawpy_gpu_synchronize(void) {
+  PAWPY_API_BEGIN
+  sync();
+  PAWPY_API_END()
+}
+
+long long pawpy_gpu_launch_count(int reset) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  long long v = r.launches;
+  if (reset) r.launches = 0;
+  return v;
+}
+
+void pawpy_gpu_profile(int on) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  r.profile = on != 0;
+}
+
+int pawpy_gpu_kernel_stats(char *buf, int len, int reset) {
+  PAWPY_API_BEGIN
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  drain_locked(r);
+  std::string out;
+  for (auto &f : r.fams) {
+    char line[256];
+    snprintf(line, sizeof line, "%s %.6f %lld\n", f.first.c_str(), f.second.ms, f.second.n);
+    out += line;
+  }
+  if (reset) r.fams.clear();
+  if (buf && len > 0) {
+    strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)out.size() + 1;
+  PAWPY_API_END(-1)
+}
+
+long long pawpy_gpu_device_bytes(void) { return device_bytes(); }
+
+}  // extern "C"

@@ -1,0 +1,230 @@
+"""``Projector``: PAW band projections of a defect wavefunction onto a basis.
+
+Mirrors ``pawpyseed.core.projector.Projector`` (projector.py:10-503) and its
+Cython base ``CProjector`` (pawpyc.pyx:628-702) for the ``aug_real`` and
+``pseudo`` methods: site classification (``make_site_lists``), the overlap
+setup, ``single_band_projection``, ``proportion_conduction`` and
+``defect_band_analysis``. ``project_all`` adds the batched form: every defect
+band against every basis band in one device contraction.
+"""
+
+import time
+
+import numpy as np
+
+from . import _lib
+from .vaspio import PAWpyError
+from .wavefunction import Timer, Wavefunction
+
+
+class Projector:
+    METHODS = ["pseudo", "realspace", "aug_recip", "aug_real"]
+
+    def __init__(self, wf, basis, unsym_basis=False, unsym_wf=False, method="aug_real"):
+        self.method = method
+        if method not in self.METHODS:
+            raise PAWpyError("method not recognized for Projector")
+        if method in ("realspace", "aug_recip"):
+            raise PAWpyError("method %r is not part of this library's projection path; "
+                             "use 'aug_real' (the reference default) or 'pseudo'" % method)
+        if wf.ncl or basis.ncl:
+            raise PAWpyError("Projection not supported for noncollinear case!")
+        if unsym_basis or unsym_wf:
+            raise PAWpyError("k-point desymmetrization is not part of this library; "
+                             "give both wavefunctions the same explicit k-point set")
+        if np.linalg.norm(basis.kpts - wf.kpts) > 1e-10:
+            raise PAWpyError("k-point grids for projection are not matched.")
+        if np.linalg.norm(basis.kws - wf.kws) > 1e-10:
+            raise PAWpyError("k-point weights for projection are not matched.")
+        if not wf.structure.same_lattice(basis.structure):
+            raise PAWpyError("Need the lattice to be the same for projections, and they are not")
+        self.wf = wf
+        self.basis = basis
+        if self.method != "pseudo":
+            basis.check_c_projectors()
+            wf.check_c_projectors()
+            self.setup_overlap()
+
+    # -- site classification ----------------------------------------------
+
+    def make_site_lists(self):
+        """M_R, M_S, N_R, N_S, N_RS exactly as projector.py:115-160.
+
+        Sites are identical when they are within 0.02 A (periodic minimum
+        image) and of the same element. The S-side radius of a candidate N_RS
+        pair is read from ``sites[i]`` with i the basis index, as the
+        reference does (projector.py:157).
+        """
+        ref, cur = self.basis.structure, self.wf.structure
+        M_R, M_S = [], []
+        for i in range(len(ref)):
+            for j in range(len(cur)):
+                if ref.distance(i, cur, j) <= 0.02 and ref.species[i] == cur.species[j]:
+                    M_R.append(i)
+                    M_S.append(j)
+        N_R = [i for i in range(len(ref)) if i not in M_R]
+        N_S = [j for j in range(len(cur)) if j not in M_S]
+        N_RS = []
+        for i in N_R:
+            for j in N_S:
+                rmax1 = self.basis.cr.pps[ref.species[i]].rmax
+                rmax2 = self.wf.cr.pps[cur.species[i]].rmax
+                if ref.distance(i, cur, j) < rmax1 + rmax2:
+                    N_RS.append((i, j))
+        return M_R, M_S, N_R, N_S, N_RS
+
+    def setup_overlap(self):
+        M_R, M_S, N_R, N_S, N_RS = self.make_site_lists()
+        N_RS_R = [a for a, _ in N_RS]
+        N_RS_S = [b for _, b in N_RS]
+        self.site_cat = [M_R, M_S, N_R, N_S, N_RS_R, N_RS_S]
+        start = time.monotonic()
+        self._setup_overlap(self.site_cat)
+        Timer.overlap_time(time.monotonic() - start)
+
+    def _setup_overlap(self, site_cat):
+        a = lambda x: np.array(x, dtype=np.int32)  # noqa: E731
+        self.M_R, self.M_S, self.N_R, self.N_S, self.N_RS_R, self.N_RS_S = [a(x) for x in site_cat]
+        L = _lib.lib()
+        L.overlap_setup_real(self.basis.wf_ptr, self.wf.wf_ptr, self.basis.nums, self.wf.nums,
+                             self.basis.coords, self.wf.coords, _lib.ptr(self.N_R), _lib.ptr(self.N_S),
+                             _lib.ptr(self.N_RS_R), _lib.ptr(self.N_RS_S),
+                             len(self.N_R), len(self.N_S), len(self.N_RS_R))
+        _lib.check()
+
+    def _lists(self):
+        return (_lib.ptr(self.M_R), _lib.ptr(self.M_S), _lib.ptr(self.N_R), _lib.ptr(self.N_S),
+                _lib.ptr(self.N_RS_R), _lib.ptr(self.N_RS_S))
+
+    # -- projections --------------------------------------------------------
+
+    def _add_augmentation_terms(self, res, band_num, flip_spin):
+        L = _lib.lib()
+        L.compensation_terms(res, int(band_num), self.wf.wf_ptr, self.basis.wf_ptr,
+                             len(self.M_R), len(self.N_R), len(self.N_S), len(self.N_RS_R),
+                             *self._lists(), self.wf.nums, self.wf.coords, self.basis.nums,
+                             self.basis.coords, self.wf.dimv, int(flip_spin))
+        _lib.check()
+
+    def _single_band_projection_pseudo(self, band_num, flip_spin=False):
+        return self.wf.pseudoprojection(band_num, self.basis, flip_spin)
+
+    def _single_band_projection_aug_real(self, band_num, flip_spin=False):
+        res = self.wf.pseudoprojection(band_num, self.basis, flip_spin)
+        start = time.monotonic()
+        self._add_augmentation_terms(res, band_num, flip_spin)
+        Timer.augmentation_time(time.monotonic() - start)
+        return res
+
+    def single_band_projection(self, band_num, flip_spin=False):
+        """<basis;b,k,s|wf;band_num,k,s> for all b, k, s: res[b*nwk*nspin + s*nwk + k]."""
+        if band_num >= self.wf.nband or band_num < 0:
+            raise ValueError("Band index out of range (0-indexed)")
+        if self.method == "pseudo":
+            return self._single_band_projection_pseudo(band_num, flip_spin)
+        return self._single_band_projection_aug_real(band_num, flip_spin)
+
+    def project_all(self, flip_spin=False):
+        """All defect bands at once: out[band_num] == single_band_projection(band_num).
+
+        Returns complex128 [nband_wf, nband_basis*nwk*nspin]. The pseudo overlap
+        and the PAW terms are one contraction per k-point on the device.
+        """
+        if self.method == "pseudo":
+            return np.array([self.single_band_projection(b, flip_spin) for b in range(self.wf.nband)])
+        nk = self.basis.nwk * self.basis.nspin
+        out = np.zeros((self.wf.nband, self.basis.nband * nk), dtype=np.complex128)
+        L = _lib.lib()
+        L.pawpy_gpu_project_all(out.reshape(-1), self.basis.wf_ptr, self.wf.wf_ptr, len(self.M_R),
+                                len(self.N_R), len(self.N_S), len(self.N_RS_R), *self._lists(), int(flip_spin))
+        _lib.check()
+        return out
+
+    # -- reductions (projector.py:384-503) -----------------------------------
+
+    def proportion_conduction(self, band_num, spinpol=False):
+        basis = self.basis
+        nband, nwk, nspin = basis.nband, basis.nwk, basis.nspin
+        occs = basis._get_occs()
+        res = self.single_band_projection(band_num)
+        if spinpol:
+            c, v = np.zeros(nspin), np.zeros(nspin)
+            for b in range(nband):
+                for s in range(nspin):
+                    ind = b * nspin + s
+                    prop = np.absolute(res[ind * nwk:(ind + 1) * nwk]) ** 2
+                    c[s] += np.dot(prop, (1 - occs[ind * nwk:(ind + 1) * nwk]) * self.wf.kws)
+                    v[s] += np.dot(prop, occs[ind * nwk:(ind + 1) * nwk] * self.wf.kws)
+        else:
+            c, v = 0, 0
+            for i in range(nband * nwk * nspin):
+                if occs[i] > 0.5:
+                    v += np.absolute(res[i]) ** 2 * self.wf.kws[i % nwk] / nspin
+                else:
+                    c += np.absolute(res[i]) ** 2 * self.wf.kws[i % nwk] / nspin
+        if self.method == "pseudo":
+            t = v + c
+            v /= t
+            c /= t
+        if spinpol:
+            v, c = v.tolist(), c.tolist()
+        return v, c
+
+    def defect_band_analysis(self, num_below_ef=20, num_above_ef=20, spinpol=False, return_energies=False,
+                             vbmband=None, band_list=None, analyze_all=False):
+        if num_below_ef < 0 or num_above_ef < 0:
+            raise ValueError("num_above_ef and num_below_ef must both be nonnegative.")
+        nband = self.basis.nband
+        occs = self.wf._get_occs()
+        if analyze_all:
+            totest = list(range(nband))
+        elif band_list:
+            totest = band_list[:]
+        else:
+            vbm = 0
+            for i in range(self.wf.nband):
+                if occs[i * self.wf.nwk * self.wf.nspin] > 0.5:
+                    vbm = i
+            if vbmband is not None:
+                vbm = vbmband
+            min_band, max_band = max(vbm - num_below_ef, 0), min(vbm + num_above_ef, self.wf.nband - 1)
+            totest = list(range(min_band, max_band + 1))
+        results = {b: self.proportion_conduction(b, spinpol=spinpol) for b in totest}
+        if return_energies:
+            return results, self.wf._get_energy_list(totest)
+        return results
+
+    # -- directory helpers (projector.py:274-382) ----------------------------
+
+    @staticmethod
+    def setup_bases(basis_dirs, desymmetrize=False, atomate_compatible=False):
+        if desymmetrize:
+            raise PAWpyError("k-point desymmetrization is not part of this library")
+        bases = []
+        for d in basis_dirs:
+            b = Wavefunction.from_directory(d, False)
+            b.check_c_projectors()
+            bases.append(b)
+        return bases
+
+    @staticmethod
+    def setup_multiple_projections(basis_dir, wf_dirs, method="aug_real", ignore_errors=False,
+                                   desymmetrize=False, atomate_compatible=False):
+        if desymmetrize:
+            raise PAWpyError("k-point desymmetrization is not part of this library")
+        basis = Wavefunction.from_directory(basis_dir, False)
+        errcount = 0
+        pr = None
+        for wf_dir in wf_dirs:
+            try:
+                wf = Wavefunction.from_directory(wf_dir, False)
+                pr = Projector(wf, basis, method=method)
+                yield [wf_dir, pr]
+            except Exception as e:
+                if ignore_errors:
+                    errcount += 1
+                else:
+                    raise PAWpyError("Unable to setup wavefunction in directory %s\nGot the following error:\n%s"
+                                     % (wf_dir, e))
+        if not pr:
+            raise PAWpyError("Could not generate any projector setups")

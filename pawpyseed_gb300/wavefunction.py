@@ -1,0 +1,231 @@
+"""``Wavefunction``: the pawpyseed wavefunction object over the GB300 library.
+
+Mirrors ``pawpyseed.core.wavefunction.Wavefunction`` (wavefunction.py:169-606)
+and its Cython base classes (``PseudoWavefunction``/``CWavefunction``,
+pawpyc.pyx:227-540) for the projection path: construction from VASP files,
+``check_c_projectors`` (species packing and ``setup_projections``),
+``pseudoprojection`` and the occupation/energy accessors. The C structs are
+the reference's (``pswf_t``), created by the library's WAVECAR reader.
+"""
+
+import ctypes as C
+import gzip
+import os
+import shutil
+import tempfile
+import time
+
+import numpy as np
+
+from . import _lib
+from .vaspio import CoreRegion, PAWpyError, Structure, Vasprun, read_poscar
+
+
+class Timer:
+    """Accumulated wall-clock times of the setup stages (pawpyc.pyx:37-49)."""
+
+    ALL_SETUP_TIME = 0.0
+    ALL_OVERLAP_TIME = 0.0
+    ALL_AUGMENTATION_TIME = 0.0
+
+    @staticmethod
+    def setup_time(t):
+        Timer.ALL_SETUP_TIME += t
+
+    @staticmethod
+    def overlap_time(t):
+        Timer.ALL_OVERLAP_TIME += t
+
+    @staticmethod
+    def augmentation_time(t):
+        Timer.ALL_AUGMENTATION_TIME += t
+
+
+def pack_species(cr):
+    """Flat species arrays in the layout get_projector_list expects (pawpyc.pyx:359-381).
+
+    Elements are numbered in POTCAR order, as Wavefunction._make_c_projectors
+    labels them (wavefunction.py:396-402).
+    """
+    labels, ls, wg, pr, ae, ps, rm = [], [], [], [], [], [], []
+    for num, sym in enumerate(cr.pps):
+        pp = cr.pps[sym]
+        labels += [num, len(pp.ls), pp.ndata, len(pp.grid)]
+        rm.append(pp.rmax)
+        ls += list(pp.ls)
+        wg.append(np.asarray(pp.grid, dtype=np.float64))
+        for i in range(len(pp.ls)):
+            pr.append(np.asarray(pp.realprojs[i][: pp.ndata], dtype=np.float64))
+            ae.append(np.asarray(pp.aewaves[i], dtype=np.float64))
+            ps.append(np.asarray(pp.pswaves[i], dtype=np.float64))
+    cat = lambda x: np.ascontiguousarray(np.concatenate(x), dtype=np.float64)  # noqa: E731
+    return (np.array(labels, np.int32), np.array(ls, np.int32), cat(wg), cat(pr), cat(ae), cat(ps),
+            np.array(rm, np.float64))
+
+
+class Wavefunction:
+    """PAW wavefunction of one structure (plane-wave part in device memory on demand).
+
+    Attributes (as the reference): structure, cr, dim, nband, nwk, nspin, encut,
+    kpts, kws, ncl, symprec.
+    """
+
+    def __init__(self, struct, pwf, cr, dim, kpts=None, kws=None, symprec=1e-4, setup_projectors=False):
+        self._ptr = None
+        if not pwf:
+            raise PAWpyError("NULL wavefunction pointer")
+        self._ptr = pwf
+        w = pwf.contents
+        self.nband, self.nwk, self.nspin, self.encut = w.nband, w.nwk, w.nspin, w.encut
+        self.ncl = bool(w.is_ncl)
+        if self.ncl:
+            raise PAWpyError("Pseudowavefunction is noncollinear! Call NCLWavefunction(...) instead")
+        self.structure = struct
+        self.cr = cr
+        self.symprec = symprec
+        self.dim = np.array(dim, dtype=np.int32)
+        if len(dim) != 3:
+            raise PAWpyError("Grid dimensions must be length 3")
+        if kpts is None:
+            kpts = np.array([[w.kpts[k].contents.k[a] for a in range(3)] for k in range(self.nwk)])
+        self.kpts = np.array(kpts, dtype=np.float64)
+        if kws is None:
+            kws = np.array([w.kpts[k].contents.weight for k in range(self.nwk)])
+        self.kws = np.array(kws, dtype=np.float64)
+        self.projector_owner = 0
+        labels = {e: n for n, e in enumerate(cr.pps)}
+        self.nums = np.array([labels[s] for s in struct.species], dtype=np.int32)
+        self.coords = np.ascontiguousarray(struct.frac_coords.reshape(-1), dtype=np.float64)
+        if setup_projectors:
+            self.check_c_projectors()
+
+    # -- construction ------------------------------------------------------
+
+    @staticmethod
+    def from_files(struct="CONTCAR", wavecar="WAVECAR", cr="POTCAR", vr="vasprun.xml",
+                   setup_projectors=False):
+        """Wavefunction.from_files (wavefunction.py:281-322)."""
+        for fname in [struct, wavecar, cr, vr]:
+            if not os.path.isfile(fname):
+                raise FileNotFoundError(f"File {fname} does not exist.")
+        vr = Vasprun(vr)
+        dim = np.array([vr.parameters["NGX"], vr.parameters["NGY"], vr.parameters["NGZ"]])
+        kws = np.ascontiguousarray(vr.actual_kpoints_weights, dtype=np.float64)
+        path = str(wavecar)
+        tmp = None
+        if path.endswith(".gz"):
+            tmp = tempfile.NamedTemporaryFile(delete=False)
+            with gzip.open(path, "rb") as src:
+                shutil.copyfileobj(src, tmp)
+            tmp.close()
+            path = tmp.name
+        try:
+            ptr = _lib.lib().pawpy_gpu_read_wavefunctions(path.encode(), kws)
+            _lib.check()
+        finally:
+            if tmp is not None:
+                os.unlink(tmp.name)
+        return Wavefunction(read_poscar(struct), ptr, CoreRegion(cr), dim, vr.actual_kpoints, kws,
+                            vr.parameters["SYMPREC"], setup_projectors)
+
+    @staticmethod
+    def from_directory(path, setup_projectors=False):
+        files = [os.path.join(path, d) for d in ["CONTCAR", "WAVECAR", "POTCAR", "vasprun.xml"]]
+        return Wavefunction.from_files(*files, setup_projectors)
+
+    @staticmethod
+    def from_arrays(struct, cr, dim, data, setup_projectors=False):
+        """Build from in-memory WAVECAR content (dict of synth.wavefunction_data)."""
+        nk = data["nspin"] * data["nwk"]
+        nplane = np.array([g.shape[0] for g in data["gs"]], dtype=np.int32)
+        gs = [np.ascontiguousarray(g, dtype=np.int32) for g in data["gs"]]
+        cs = [np.ascontiguousarray(c, dtype=np.complex64) for c in data["coeffs"]]
+        gp = (C.c_void_p * nk)(*[g.ctypes.data for g in gs])
+        cp = (C.c_void_p * nk)(*[c.ctypes.data for c in cs])
+        lat = np.ascontiguousarray(np.asarray(data["lattice"]).reshape(-1), dtype=np.float64)
+        kp = np.ascontiguousarray(np.asarray(data["kpts"]).reshape(-1), dtype=np.float64)
+        kws = np.ascontiguousarray(data["weights"], dtype=np.float64)
+        en = np.ascontiguousarray(np.asarray(data["energies"]).reshape(-1), dtype=np.float64)
+        oc = np.ascontiguousarray(np.asarray(data["occs"]).reshape(-1), dtype=np.float64)
+        ptr = _lib.lib().pawpy_gpu_wavefunction_from_arrays(data["nspin"], data["nwk"], data["nband"],
+                                                           float(data["encut"]), lat, kp, kws, nplane,
+                                                           gp, cp, en, oc)
+        _lib.check()
+        return Wavefunction(struct, ptr, cr, dim, data["kpts"], kws, 1e-4, setup_projectors)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            try:
+                _lib.lib().pawpy_gpu_free_pswf(self._ptr)
+            except Exception:
+                pass
+            self._ptr = None
+
+    # -- accessors ---------------------------------------------------------
+
+    @property
+    def wf_ptr(self):
+        return self._ptr
+
+    def check_band_index(self, b):
+        if b < 0 or b >= self.nband:
+            raise ValueError("Invalid band {}. Should be in range [{}, {}]".format(b, 0, self.nband - 1))
+
+    def _get_occs(self):
+        """Occupations in [band][spin*nwk + k] order (pawpyc.pyx:532-538)."""
+        nk = self.nwk * self.nspin
+        w = self._ptr.contents
+        res = np.zeros(self.nband * nk)
+        for k in range(nk):
+            kp = w.kpts[k].contents
+            for b in range(self.nband):
+                res[b * nk + k] = kp.bands[b].contents.occ
+        return res
+
+    def _get_energy_list(self, bands):
+        w = self._ptr.contents
+        out = {}
+        for b in bands:
+            self.check_band_index(b)
+            out[b] = []
+            for s in range(self.nspin):
+                for k in range(self.nwk):
+                    bd = w.kpts[k + s * self.nwk].contents.bands[b].contents
+                    out[b].append([bd.energy, bd.occ])
+        return out
+
+    def upload(self):
+        """Make the plane-wave coefficients resident in device memory now."""
+        _lib.lib().pawpy_gpu_upload(self._ptr)
+        _lib.check()
+
+    # -- projector setup ---------------------------------------------------
+
+    def grid_encut(self):
+        """(pi*dim/abc)^2/0.262 maximised over the axes (wavefunction.py:411)."""
+        return float(np.max((np.pi * self.dim / self.structure.abc) ** 2 / 0.262))
+
+    def _make_c_projectors(self):
+        L = _lib.lib()
+        labels, ls, wg, pr, ae, ps, rm = pack_species(self.cr)
+        pps = L.get_projector_list(len(self.cr.pps), labels, ls, wg, pr, ae, ps, rm, self.grid_encut())
+        _lib.check()
+        self.dimv = np.ascontiguousarray(self.dim, dtype=np.int32)
+        L.setup_projections(self._ptr, pps, len(self.cr.pps), len(self.structure), self.dimv, self.nums,
+                            self.coords)
+        _lib.check()
+        self.projector_owner = 1
+
+    def check_c_projectors(self):
+        """Set up the projector functions and <p|psi> if that has not happened yet."""
+        if not self.projector_owner:
+            start = time.monotonic()
+            self._make_c_projectors()
+            Timer.setup_time(time.monotonic() - start)
+
+    def pseudoprojection(self, band_num, basis, flip_spin=False):
+        """<psi~_basis,b,k|psi~_self,band_num,k> for all basis bands b and k (pawpyc.pyx:311-325)."""
+        res = np.zeros(basis.nband * basis.nwk * basis.nspin, dtype=np.complex128)
+        _lib.lib().pseudoprojection(res, basis._ptr, self._ptr, int(band_num), int(flip_spin))
+        _lib.check()
+        return res

@@ -1,0 +1,97 @@
+import hashlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+# name -> (workload, nband, nk): the reduced workloads the golden fixtures were made from
+CASES = {
+    "cfg0": (0, 32, None),
+    "cfg1s": (1, 8, 2),
+    "cfg2s": (2, 4, None),
+    "cfg3s": (3, 4, 2),
+}
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (runs the library's kernels)")
+
+
+def fingerprint(path):
+    h = hashlib.sha256()
+    for name in ("WAVECAR", "POTCAR", "CONTCAR", "vasprun.xml"):
+        with open(os.path.join(path, name), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+@pytest.fixture(scope="session")
+def workload_dirs(tmp_path_factory):
+    """Lazily written synthetic workloads: name -> {'basis': dir, 'defect': dir}."""
+    from pawpyseed_gb300 import synth
+
+    root = tmp_path_factory.mktemp("workloads")
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            cfg, nb, nk = CASES[name]
+            cache[name] = synth.write_workload(str(root / name), cfg, nband=nb, nk=nk)
+        return cache[name]
+
+    return get
+
+
+@pytest.fixture(scope="session")
+def golden():
+    def get(name):
+        return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+    return get
+
+
+@pytest.fixture(scope="session")
+def oracle_projectors(workload_dirs):
+    """Oracle (FP64 restatement) projector per case, built once per session."""
+    import oracle as orc
+
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            d = workload_dirs(name)
+            b = orc.OracleWavefunction(d["basis"])
+            w = orc.OracleWavefunction(d["defect"])
+            cache[name] = orc.OracleProjector(w, b)
+        return cache[name]
+
+    return get
+
+
+def have_gpu():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _build_lib():
+    """Make sure the in-tree library and the oracle exist before tests import them."""
+    from pawpyseed_gb300 import build as B
+
+    if not os.path.exists(B.LIB):
+        B.build()
+    import oracle as orc
+
+    if not os.path.exists(orc.LIB_PATH):
+        orc.build()

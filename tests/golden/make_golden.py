@@ -1,0 +1,120 @@
+"""Generate the golden vectors under tests/golden/ from the reference pawpyseed C core.
+
+Run in a container where the reference sources are present:
+
+    make -C oracle ref            # builds oracle/_ref/libpawpy_ref.so from the reference C
+    python tests/golden/make_golden.py
+
+Inputs are the seeded synthetic workloads of ``pawpyseed_gb300.synth`` (reduced
+band / k-point counts so the reference finishes in seconds); each fixture
+stores a fingerprint of the inputs it was made from, so a test can tell
+whether its regenerated inputs are the same bytes.
+
+Fixtures:
+* ``fft_ga4.npz``  -- the reference's own fft3d known-answer case
+  (pawpyseed/core/tests/tests.c:28-80): band 0, k-point 0 of the Ga4
+  test_files/WAVECAR on a 20^3 grid, with the reference fft3d output and a
+  direct plane-wave sum.
+* ``<name>.npz``   -- reference ``single_band_projection`` (aug_real) for every
+  defect band: total PAW overlaps, pseudo overlaps, per-band projector
+  coefficients, N_RS pair matrices.
+"""
+
+import hashlib
+import os
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from pawpyseed_gb300 import synth, vaspio  # noqa: E402
+
+CASES = {
+    # name: (workload, nband, nk, flips)
+    "cfg0": (0, 32, None, (False,)),
+    "cfg1s": (1, 8, 2, (False,)),
+    "cfg2s": (2, 4, None, (False,)),
+    "cfg3s": (3, 4, 2, (False, True)),
+}
+
+
+def fingerprint(path):
+    h = hashlib.sha256()
+    for name in ("WAVECAR", "POTCAR", "CONTCAR", "vasprun.xml"):
+        with open(os.path.join(path, name), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def fft_fixture():
+    import ref_harness as rh
+
+    lib = rh.load_ref()
+    wc = "/root/reference/test_files/WAVECAR"
+    d = vaspio.read_wavecar_numpy(wc)
+    g = np.ascontiguousarray(d["gs"][0], dtype=np.int32)
+    c = np.ascontiguousarray(d["coeffs"][0][0], dtype=np.complex64)
+    lat = np.ascontiguousarray(d["lattice"].reshape(-1), dtype=np.float64)
+    fftg = np.array([20, 20, 20], np.int32)
+    x = np.zeros(8000, np.complex128)
+    lib.fft3d(x, None, lat, np.ascontiguousarray(d["kpts"][0]), g.reshape(-1).copy(),
+              c.ctypes.data_as(rh.C.c_void_p), g.shape[0], fftg)
+    f = np.stack(np.meshgrid(np.arange(20), np.arange(20), np.arange(20), indexing="ij"), -1) / 20.0
+    ph = np.exp(2j * np.pi * (f.reshape(-1, 3) @ g.T.astype(np.float64)))
+    direct = ph @ c.astype(np.complex128) / np.sqrt(abs(np.linalg.det(d["lattice"])))
+    np.savez_compressed(os.path.join(HERE, "fft_ga4.npz"), gs=g, cs=c, lattice=d["lattice"],
+                        kpt=d["kpts"][0], fftg=fftg, ref=x, direct=direct)
+    print("fft_ga4: max|ref-direct| = %.3e" % np.abs(x - direct).max())
+
+
+def case_fixture(name, cfg, nband, nk, flips):
+    import ref_harness as rh
+
+    lib = rh.load_ref()
+    tmp = tempfile.mkdtemp()
+    try:
+        paths = synth.write_workload(tmp, cfg, nband=nband, nk=nk)
+        b = rh.RefWavefunction(lib, paths["basis"])
+        d = rh.RefWavefunction(lib, paths["defect"])
+        pr = rh.RefProjector(lib, b, d)
+        out = dict(fp_basis=fingerprint(paths["basis"]), fp_defect=fingerprint(paths["defect"]),
+                   cfg=cfg, nband=nband, nk=-1 if nk is None else nk)
+        for flip in flips:
+            tag = "flip" if flip else "noflip"
+            out["total_" + tag] = np.array([pr.single_band_projection(i, flip) for i in range(d.nband)])
+            out["pseudo_" + tag] = np.array([pr.pseudo(i, flip) for i in range(d.nband)])
+        nkt = b.nwk * b.nspin
+        nbp = min(2, b.nband)
+        out["P_basis"] = np.array([[np.concatenate(b.projections(bb, k)) for bb in range(nbp)]
+                                   for k in range(nkt)])
+        out["P_defect"] = np.array([[np.concatenate(d.projections(bb, k)) for bb in range(nbp)]
+                                    for k in range(nkt)])
+        Q, dc = pr.overlaps_NRS()
+        Q, dc = Q[:6], dc[:6]
+        if Q:
+            out["Q_shapes"] = np.array([q.shape for q in Q])
+            out["Q_flat"] = np.concatenate([q.reshape(-1) for q in Q])
+            out["dcoords"] = dc
+        for k, v in pr.lists.items():
+            out["list_" + k] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "written", {k: getattr(v, "shape", v) for k, v in out.items() if k.startswith("total")})
+        b.free()
+        d.free()
+    finally:
+        shutil.rmtree(tmp)
+
+
+if __name__ == "__main__":
+    which = sys.argv[1:] or ["fft"] + list(CASES)
+    for w in which:
+        if w == "fft":
+            fft_fixture()
+        else:
+            case_fixture(w, *CASES[w])

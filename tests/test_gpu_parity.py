@@ -1,0 +1,190 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+Tolerance: the overlaps must agree with the FP64 evaluation (the oracle) to
+|error| <= 1e-5 (the accuracy target of the band-pair metric); projector
+coefficients to 1e-5 relative to their largest magnitude; the FFT to 1e-5 per
+grid point (the reference's own fft_check bound, core/tests/tests.c:61).
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from conftest import CASES, fingerprint
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def load(dirs):
+    from pawpyseed_gb300.wavefunction import Wavefunction
+
+    return Wavefunction.from_directory(dirs["basis"]), Wavefunction.from_directory(dirs["defect"])
+
+
+def host_projections(wf, k, b):
+    kp = wf.wf_ptr.contents.kpts[k].contents
+    bd = kp.bands[b].contents
+    out = []
+    for s in range(len(wf.structure)):
+        p = bd.projections[s]
+        v = np.ctypeslib.as_array(p.overlaps, shape=(2 * p.total_projs,))
+        out.append(v[0::2] + 1j * v[1::2])
+    return np.concatenate(out)
+
+
+def test_fft3d_known_answer(golden):
+    """fft3d against a direct plane-wave sum on the reference's Ga4 WAVECAR (20^3)."""
+    from pawpyseed_gb300 import _lib
+
+    g = golden("fft_ga4")
+    L = _lib.lib()
+    x = np.zeros(8000, np.complex128)
+    cs = np.ascontiguousarray(g["cs"], dtype=np.complex64)
+    L.fft3d(x, None, np.ascontiguousarray(g["lattice"].reshape(-1)), np.ascontiguousarray(g["kpt"]),
+            np.ascontiguousarray(g["gs"].reshape(-1), dtype=np.int32), cs.ctypes.data_as(C.c_void_p),
+            g["gs"].shape[0], np.ascontiguousarray(g["fftg"], dtype=np.int32))
+    _lib.check()
+    assert np.abs(x - g["direct"]).max() <= 1e-5
+    assert np.abs(x - g["ref"]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["cfg0", "cfg1s"])
+def test_projector_coefficients(name, workload_dirs, oracle_projectors, golden):
+    basis, wf = load(workload_dirs(name))
+    basis.check_c_projectors()
+    op = oracle_projectors(name)
+    for k in range(basis.nwk * basis.nspin):
+        for b in (0, basis.nband - 1):
+            mine = host_projections(basis, k, b)
+            ref = op.basis.P[k][b]
+            assert np.abs(mine - ref).max() <= TOL * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_single_band_projection(name, workload_dirs, oracle_projectors, golden):
+    """Projector.single_band_projection (pseudoprojection + compensation_terms) for every band."""
+    from pawpyseed_gb300.projector import Projector
+
+    dirs = workload_dirs(name)
+    basis, wf = load(dirs)
+    pr = Projector(wf, basis)
+    op = oracle_projectors(name)
+    g = golden(name)
+    same = fingerprint(dirs["basis"]) == str(g["fp_basis"]) and fingerprint(dirs["defect"]) == str(g["fp_defect"])
+    flips = [False, True] if "total_flip" in g.files else [False]
+    for flip in flips:
+        truth = op.full(flip)  # FP64
+        mine = np.array([pr.single_band_projection(b, flip_spin=flip) for b in range(wf.nband)])
+        tv = np.array([op.band_vector(truth, b) for b in range(wf.nband)])
+        assert np.abs(mine - tv).max() <= TOL
+        if same:
+            assert np.abs(mine - g["total_" + ("flip" if flip else "noflip")]).max() <= TOL
+        # the PAW terms alone, against the FP64 sums
+        pseudo = np.array([wf.pseudoprojection(b, basis, flip) for b in range(wf.nband)])
+        comp_truth = np.array([op.band_vector(op.comp_full(flip), b) for b in range(wf.nband)])
+        assert np.abs((mine - pseudo) - comp_truth).max() <= 1e-7
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_project_all_matches_band_loop(name, workload_dirs, oracle_projectors):
+    """The batched contraction equals the per-band ABI path and the FP64 truth."""
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs(name))
+    pr = Projector(wf, basis)
+    op = oracle_projectors(name)
+    full = pr.project_all()
+    loop = np.array([pr.single_band_projection(b) for b in range(wf.nband)])
+    truth = op.full()
+    tv = np.array([op.band_vector(truth, b) for b in range(wf.nband)])
+    assert full.shape == loop.shape
+    assert np.abs(full - tv).max() <= TOL
+    assert np.abs(full - loop).max() <= 2e-6
+
+
+def test_results_deterministic_and_cached(workload_dirs):
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs("cfg0"))
+    pr = Projector(wf, basis)
+    a = pr.project_all()
+    b = pr.project_all()
+    assert np.array_equal(a, b)
+    x = pr.single_band_projection(3)
+    y = pr.single_band_projection(3)
+    assert np.array_equal(x, y)
+
+
+def test_pseudo_method_and_reductions(workload_dirs, oracle_projectors):
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs("cfg0"))
+    pr = Projector(wf, basis, method="pseudo")
+    op = oracle_projectors("cfg0")
+    ps = op.pseudo_full()
+    for b in (0, 7, 31):
+        assert np.abs(pr.single_band_projection(b) - op.band_vector(ps, b)).max() <= TOL
+    v, c = pr.proportion_conduction(4)
+    assert abs(v + c - 1) < 1e-12
+    res = pr.defect_band_analysis(4, 10, False)
+    assert len(res) == 15
+    with pytest.raises(ValueError):
+        pr.single_band_projection(32)
+    with pytest.raises(ValueError):
+        pr.single_band_projection(-1)
+
+
+def test_defect_band_analysis_aug_real(workload_dirs, oracle_projectors):
+    """proportion_conduction on aug_real overlaps equals the FP64 reduction."""
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs("cfg3s"))
+    pr = Projector(wf, basis)
+    op = oracle_projectors("cfg3s")
+    truth = op.full()
+    occs = basis._get_occs()
+    nk = basis.nwk * basis.nspin
+    for b in range(wf.nband):
+        res = op.band_vector(truth, b)
+        v = sum(abs(res[i]) ** 2 * wf.kws[i % basis.nwk] / basis.nspin for i in range(len(res)) if occs[i] > 0.5)
+        mv, mc = pr.proportion_conduction(b)
+        assert abs(mv - v) < 1e-6
+    sp = pr.defect_band_analysis(analyze_all=True, spinpol=True)
+    assert len(sp) == basis.nband and len(sp[0][0]) == 2
+
+
+def test_self_projection_of_bands_is_identity_on_pseudo_part(workload_dirs):
+    """Projecting a structure onto itself: pseudo overlaps of normalised bands have unit diagonal."""
+    from pawpyseed_gb300.projector import Projector
+    from pawpyseed_gb300.wavefunction import Wavefunction
+
+    d = workload_dirs("cfg0")
+    a = Wavefunction.from_directory(d["basis"])
+    b = Wavefunction.from_directory(d["basis"])
+    pr = Projector(a, b, method="pseudo")
+    nk = a.nwk * a.nspin
+    for band in (0, 9, 31):
+        res = pr.single_band_projection(band)
+        diag = res[band * nk:(band + 1) * nk]
+        assert np.abs(diag - 1).max() < 2e-6
+
+
+def test_errors_do_not_abort(workload_dirs):
+    """Misuse reaches Python as an exception, never a process exit."""
+    from pawpyseed_gb300 import _lib
+
+    basis, wf = load(workload_dirs("cfg0"))
+    L = _lib.lib()
+    res = np.zeros(basis.nband * basis.nwk, np.complex128)
+    L.pseudoprojection(res, basis.wf_ptr, wf.wf_ptr, 1000, 0)
+    with pytest.raises(_lib.PAWpyGPUError):
+        _lib.check()
+    # compensation before overlap_setup_real on this pair
+    L.compensation_terms(res, 0, wf.wf_ptr, basis.wf_ptr, 0, 0, 0, 0, None, None, None, None, None, None,
+                         wf.nums, wf.coords, basis.nums, basis.coords, wf.dim, 0)
+    with pytest.raises(_lib.PAWpyGPUError):
+        _lib.check()

@@ -1,0 +1,208 @@
+"""Host-side logic of the library, without a GPU: ABI exports, struct layout,
+the WAVECAR reader, the radial (per-element) setup, file formats and site lists."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import CASES, ROOT, fingerprint
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "pawpy_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+
+
+def test_library_exports_every_header_symbol():
+    from pawpyseed_gb300 import _lib
+
+    L = _lib.lib()
+    syms = header_symbols()
+    assert "pseudoprojection" in syms and "compensation_terms" in syms and "fft3d" in syms
+    for s in syms:
+        assert hasattr(L, s), s
+
+
+def test_struct_layout_matches_reference_layout():
+    from pawpyseed_gb300 import _lib, structs
+
+    lib_rows = {(s, m): o for s, m, o in _lib.struct_layout()}
+    ct_rows = {(s, m): o for s, m, o in structs.layout_table()}
+    assert set(lib_rows) == set(ct_rows)
+    for k, v in ct_rows.items():
+        assert lib_rows[k] == v, k
+
+
+def test_wavecar_reader_matches_numpy_reader(workload_dirs):
+    from pawpyseed_gb300 import _lib, vaspio
+
+    d = workload_dirs("cfg3s")["basis"]
+    ref = vaspio.read_wavecar_numpy(os.path.join(d, "WAVECAR"))
+    kws = np.full(ref["nwk"], 1.0 / ref["nwk"])
+    L = _lib.lib()
+    p = L.pawpy_gpu_read_wavefunctions(os.path.join(d, "WAVECAR").encode(), kws)
+    _lib.check()
+    try:
+        w = p.contents
+        assert (w.nspin, w.nwk, w.nband) == (ref["nspin"], ref["nwk"], ref["nband"])
+        for k in range(w.nspin * w.nwk):
+            kp = w.kpts[k].contents
+            g = np.ctypeslib.as_array(kp.Gs, shape=(3 * kp.num_waves,)).reshape(-1, 3)
+            assert np.array_equal(g, ref["gs"][k])
+            for b in (0, w.nband - 1):
+                c = np.ctypeslib.as_array(C.cast(kp.bands[b].contents.Cs, C.POINTER(C.c_float)),
+                                          shape=(2 * kp.num_waves,)).view(np.complex64)
+                assert np.array_equal(c, ref["coeffs"][k][b])
+                assert kp.bands[b].contents.occ == ref["occs"][k][b]
+    finally:
+        L.pawpy_gpu_free_pswf(p)
+
+
+def test_reference_wavecar_fixture_gsphere(golden):
+    """The plane-wave enumeration reproduces the Ga4 WAVECAR's counts (945 at k0)."""
+    from pawpyseed_gb300 import vaspio
+
+    g = golden("fft_ga4")
+    gs = vaspio.gvectors(g["lattice"], g["kpt"], 320.0)
+    assert np.array_equal(gs, g["gs"])
+
+
+def test_reader_errors_are_reported_not_fatal(tmp_path):
+    from pawpyseed_gb300 import _lib
+
+    L = _lib.lib()
+    bad = tmp_path / "WAVECAR"
+    bad.write_bytes(b"\0" * 16)
+    p = L.pawpy_gpu_read_wavefunctions(str(bad).encode(), np.ones(1))
+    assert not p
+    with pytest.raises(_lib.PAWpyGPUError):
+        _lib.check()
+    p = L.pawpy_gpu_read_wavefunctions(str(tmp_path / "missing").encode(), np.ones(1))
+    assert not p
+    assert L.pawpy_gpu_last_error() != 0
+    L.pawpy_gpu_clear_error()
+
+
+def test_projector_list_matches_oracle():
+    """get_projector_list (host FP64) against the oracle's element setup."""
+    import oracle as orc
+
+    from pawpyseed_gb300 import _lib, synth, vaspio
+    from pawpyseed_gb300.wavefunction import pack_species
+
+    cr = vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
+    labels, ls, wg, pr, ae, ps, rm = pack_species(cr)
+    L = _lib.lib()
+    for ge in (640.0, 1150.0):
+        pps = L.get_projector_list(2, labels, ls, wg, pr, ae, ps, rm, ge)
+        _lib.check()
+        for e, sym in enumerate(cr.pps):
+            o = orc.OSpecies(cr.pps[sym], ge)
+            pp = pps[e]
+            nd, ng = pp.proj_gridsize, pp.wave_gridsize
+            assert pp.total_projs == o.total and pp.num_projs == o.nproj
+            for k in range(pp.num_projs):
+                f = pp.funcs[k]
+                sdw = np.ctypeslib.as_array(f.smooth_diffwave, shape=(nd,))
+                kw = np.ctypeslib.as_array(f.kwave, shape=(ng,))
+                assert np.allclose(sdw, o.sdw[k * nd:(k + 1) * nd], rtol=0, atol=1e-12 * np.abs(sdw).max())
+                assert np.allclose(kw, o.kwave[k * ng:(k + 1) * ng], rtol=0, atol=1e-12 * np.abs(kw).max())
+            n = pp.num_projs
+            aeov = np.ctypeslib.as_array(pp.aepw_overlap_matrix, shape=(n * n,))
+            psov = np.ctypeslib.as_array(pp.pspw_overlap_matrix, shape=(n * n,))
+            assert np.allclose(aeov, o.aeov, atol=1e-13) and np.allclose(psov, o.psov, atol=1e-13)
+
+
+def test_potcar_parser_reads_generated_dataset():
+    from pawpyseed_gb300 import synth, vaspio
+
+    cr = vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
+    assert list(cr.pps) == ["A", "B"]
+    a = synth.species_arrays("B")
+    pp = cr.pps["B"]
+    assert pp.ls == [0, 0, 1, 1, 2, 2] and pp.ndata == 100 and pp.rmax == 1.2
+    assert np.allclose(pp.grid, a["grid"], rtol=1e-9)
+    for i in range(6):
+        assert np.allclose(pp.realprojs[i], a["realprojs"][i], rtol=1e-8, atol=1e-12)
+        assert np.allclose(pp.aewaves[i], a["aewaves"][i], rtol=1e-8, atol=1e-12)
+
+
+def test_potcar_parser_agrees_with_reference_parser():
+    """Our POTCAR parser and the reference's Pseudopotential give the same arrays."""
+    import importlib.util
+    import sys
+    import types
+
+    src = "/root/reference/pawpyseed/core/wavefunction.py"
+    if not os.path.exists(src):
+        pytest.skip("reference sources not present")
+    from pawpyseed_gb300 import synth, vaspio
+
+    stubs = {}
+    for name in ["pymatgen", "pymatgen.io", "pymatgen.io.vasp", "pymatgen.io.vasp.inputs",
+                 "pymatgen.io.vasp.outputs", "pawpyseed", "pawpyseed.core", "pawpyseed.core.symmetry",
+                 "pawpyseed.core.utils"]:
+        stubs[name] = types.ModuleType(name)
+    stubs["pymatgen.io.vasp.inputs"].Poscar = stubs["pymatgen.io.vasp.inputs"].Potcar = object
+    stubs["pymatgen.io.vasp.outputs"].Vasprun = object
+    stubs["pawpyseed.core"].pawpyc = types.SimpleNamespace(CWavefunction=object)
+    saved = {k: sys.modules.get(k) for k in stubs}
+    sys.modules.update(stubs)
+    try:
+        spec = importlib.util.spec_from_file_location("ref_wavefunction", src)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        txt = synth.potcar_text(["B"])
+        ref = mod.Pseudopotential(txt[:-15])
+        mine = vaspio.CoreRegion(txt).pps["B"]
+        assert [int(x) for x in ref.ls] == mine.ls and ref.ndata == mine.ndata and ref.rmax == mine.rmax
+        assert np.array_equal(ref.grid, mine.grid)
+        for i in range(len(mine.ls)):
+            assert np.array_equal(ref.realprojs[i], mine.realprojs[i])
+            assert np.array_equal(ref.aewaves[i], mine.aewaves[i])
+            assert np.array_equal(ref.pswaves[i], mine.pswaves[i])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_site_lists_match_reference(name, workload_dirs, golden):
+    """Projector.make_site_lists reproduces the reference's classification."""
+    from pawpyseed_gb300 import vaspio
+
+    d = workload_dirs(name)
+    g = golden(name)
+    b = vaspio.read_poscar(os.path.join(d["basis"], "CONTCAR"))
+    w = vaspio.read_poscar(os.path.join(d["defect"], "CONTCAR"))
+    bcr = vaspio.CoreRegion(os.path.join(d["basis"], "POTCAR"))
+    wcr = vaspio.CoreRegion(os.path.join(d["defect"], "POTCAR"))
+
+    class P:  # the Projector method on its own, without a device
+        pass
+
+    from pawpyseed_gb300.projector import Projector
+
+    p = P()
+    p.basis = type("W", (), {"structure": b, "cr": bcr})()
+    p.wf = type("W", (), {"structure": w, "cr": wcr})()
+    M_R, M_S, N_R, N_S, N_RS = Projector.make_site_lists(p)
+    assert M_R == list(g["list_M_R"]) and M_S == list(g["list_M_S"])
+    assert N_R == list(g["list_N_R"]) and N_S == list(g["list_N_S"])
+    assert [a for a, _ in N_RS] == list(g["list_N_RS_R"]) and [c for _, c in N_RS] == list(g["list_N_RS_S"])
+
+
+def test_synthetic_inputs_are_reproducible(workload_dirs, golden):
+    """Regenerating a workload gives the fixture's bytes (reported, not required)."""
+    d = workload_dirs("cfg0")
+    g = golden("cfg0")
+    if fingerprint(d["basis"]) != str(g["fp_basis"]):
+        pytest.skip("this platform's numpy regenerates different bytes; tolerance tests still apply")

@@ -1,0 +1,104 @@
+"""The oracle (CPU FP64 restatement) pinned against the reference's golden vectors.
+
+The golden fixtures were produced by the reference pawpyseed C core itself
+(tests/golden/make_golden.py). Inputs are regenerated here from the same seeds;
+when the regenerated bytes differ (fingerprint mismatch) the exact comparison
+is skipped and only the tolerance comparison runs.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import CASES, fingerprint
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_oracle_matches_reference(name, workload_dirs, golden, oracle_projectors):
+    g = golden(name)
+    d = workload_dirs(name)
+    same_inputs = fingerprint(d["basis"]) == str(g["fp_basis"]) and fingerprint(d["defect"]) == str(g["fp_defect"])
+    op = oracle_projectors(name)
+    flips = [False, True] if "total_flip" in g.files else [False]
+    for flip in flips:
+        tag = "flip" if flip else "noflip"
+        ref_total, ref_pseudo = g["total_" + tag], g["pseudo_" + tag]
+        # pseudo overlaps accumulated in single precision, like the reference's cblas_cdotc_sub
+        p32 = op.pseudo_full(flip, fp32=True)
+        p32v = np.array([op.band_vector(p32, b) for b in range(op.wf.nband)])
+        comp = op.comp_full(flip)
+        compv = np.array([op.band_vector(comp, b) for b in range(op.wf.nband)])
+        scale = np.abs(ref_total).max()
+        if same_inputs:
+            assert np.abs(p32v - ref_pseudo).max() <= 1e-6 * scale
+            # PAW terms in FP64: agreement to rounding
+            assert np.abs(compv - (ref_total - ref_pseudo)).max() <= 1e-12 * max(1.0, scale)
+        else:
+            assert np.abs(p32v + compv - ref_total).max() <= 1e-5
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_oracle_projections_and_pairs(name, workload_dirs, golden, oracle_projectors):
+    g = golden(name)
+    d = workload_dirs(name)
+    if fingerprint(d["basis"]) != str(g["fp_basis"]):
+        pytest.skip("regenerated inputs differ in bytes from the fixture's")
+    op = oracle_projectors(name)
+    nbp = g["P_basis"].shape[1]
+    for k in range(g["P_basis"].shape[0]):
+        assert np.abs(op.basis.P[k][:nbp] - g["P_basis"][k]).max() <= 1e-13
+        assert np.abs(op.wf.P[k][:nbp] - g["P_defect"][k]).max() <= 1e-13
+    if "Q_flat" in g.files:
+        off = 0
+        for i, shp in enumerate(g["Q_shapes"]):
+            n = int(shp[0] * shp[1])
+            q = g["Q_flat"][off:off + n].reshape(shp)
+            off += n
+            assert np.abs(op.Q[i] - q).max() <= 1e-13
+            assert np.abs(op.dcoords[i] - g["dcoords"][i]).max() <= 1e-14
+    lists = [op.M_R, op.M_S, op.N_R, op.N_S, op.N_RS_R, op.N_RS_S]
+    for key, mine in zip(["M_R", "M_S", "N_R", "N_S", "N_RS_R", "N_RS_S"], lists):
+        assert list(g["list_" + key]) == list(mine)
+
+
+def test_oracle_fft_known_answer(golden):
+    """The reference's own fft_check case (core/tests/tests.c:28-80): Ga4, 20^3."""
+    import oracle as orc
+
+    g = golden("fft_ga4")
+    x = np.zeros(2 * 8000)
+    orc.lib().oracle_fft3d(x, np.ascontiguousarray(g["gs"].reshape(-1), dtype=np.int32),
+                           np.ascontiguousarray(g["cs"].view(np.float32)), g["gs"].shape[0],
+                           np.ascontiguousarray(g["fftg"], dtype=np.int32), float(abs(np.linalg.det(g["lattice"]))))
+    xc = x[0::2] + 1j * x[1::2]
+    assert np.abs(xc - g["direct"]).max() <= 1e-5  # the reference test's tolerance (tests.c:61)
+    assert np.abs(xc - g["ref"]).max() <= 1e-12
+
+
+def test_oracle_ylm_convention():
+    """Complex Condon-Shortley Y_lm, as the reference's test_Ylm (test_core.py:68-90) pins."""
+    import ctypes as C
+
+    import oracle as orc
+    from scipy.special import sph_harm_y
+
+    L = orc.lib()
+    rng = np.random.default_rng(0)
+    for l in range(4):
+        for m in range(-l, l + 1):
+            for th, ph in rng.uniform([0, 0], [np.pi, 2 * np.pi], size=(20, 2)):
+                re, im = C.c_double(), C.c_double()
+                L.oracle_ylm(l, m, th, ph, C.byref(re), C.byref(im))
+                ref = sph_harm_y(l, m, th, ph)
+                assert abs(complex(re.value, im.value) - ref) < 1e-12
+
+
+def test_oracle_wigner_table():
+    """SBTFACS regenerated from Racah's formula: spot values from sympy-free identities."""
+    import oracle as orc
+
+    # w3j(l,l,0;0,0,0)^2 = 1/(2l+1); w3j(1,1,2;0,0,0) = sqrt(2/15)
+    for l in range(4):
+        assert abs(orc.wigner3j(l, l, 0, 0, 0, 0) ** 2 - 1 / (2 * l + 1)) < 1e-14
+    assert abs(orc.wigner3j(1, 1, 2, 0, 0, 0) - np.sqrt(2 / 15)) < 1e-14
+    t = orc.sbtfacs().reshape(4, 4, 4, 7, 4)
+    assert abs(t[0, 0, 0, 0, 0] - 1 / np.sqrt(4 * np.pi)) < 1e-14
