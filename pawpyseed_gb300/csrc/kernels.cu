@@ -182,7 +182,8 @@ __device__ __forceinline__ void d_to_cart(const double *f, const double *L, doub
   o[2] = t2;
 }
 
-__device__ __forceinline__ double d_norm(const double *v) { return pow(v[0] * v[0] + v[1] * v[1] + v[2] * v[2], 0.5); }
+// |v| rounded once, as the reference's pow(x, 0.5) (a correctly rounded square root) gives it
+__device__ __forceinline__ double d_norm(const double *v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
 __device__ __forceinline__ void box_point(const SiteDesc &s, long long lin, int *ijk) {
   int w3 = 2 * s.g[2] + 1, w2 = 2 * s.g[1] + 1;
@@ -314,7 +315,7 @@ __global__ void k_sphere_fill(const SiteDesc *__restrict__ sites, const SpeciesD
       double theta = 0, phi = 0;
       if (r != 0) {
         theta = acos(t[2] / r);
-        if (r - fabs(t[2]) == 0)
+        if (r - fabs(t[2]) == 0 || t[0] * t[0] + t[1] * t[1] == 0)
           phi = 0;
         else
           phi = acos(t[0] / sqrt(t[0] * t[0] + t[1] * t[1]));
