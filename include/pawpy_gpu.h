@@ -285,6 +285,9 @@ void pawpy_gpu_profile(int on);
 int pawpy_gpu_kernel_stats(char *buf, int len, int reset);
 /* Bytes of device memory the library holds. */
 long long pawpy_gpu_device_bytes(void);
+/* Whether the current device reads pageable host memory coherently (bit 0:
+ * cudaDevAttrPageableMemoryAccess, bit 1: ...UsesHostPageTables); -1 on error. */
+int pawpy_gpu_pageable_memory_access(void);
 /* Byte offset / size of each struct member, for layout checks:
  * writes "struct member offset\n" lines; returns the length needed. */
 int pawpy_gpu_struct_layout(char *buf, int len);

@@ -39,9 +39,13 @@ struct SpeciesTables {
 };
 
 struct SphereSet {
-  int nsites = 0, Ptot = 0, max_total = 0, nkp = 0;
+  int nsites = 0, Ptot = 0, max_total = 0, nkp = 0, nseg = 0;
   long long npts = 0, nvals = 0;
   std::vector<SiteDesc> host;
+  std::vector<SegFill> segs;      // site-major, box-row order within a site
+  std::vector<int> seg_plane;     // wrapped plane index j of each segment
+  std::vector<long long> site_pt, site_val;  // first point / first table value of each site
+  std::vector<int> site_npts;
   DevBuf<SiteDesc> sites;
   DevBuf<int> idx;
   DevBuf<float2> tab, phase;
@@ -51,6 +55,7 @@ struct SphereSet {
 struct DevKpt {
   int W = 0, Wpad = 0, g1min = 0, n1 = 0;
   std::vector<int> perm;     // sorted position -> original plane-wave index
+  std::vector<int> invperm;  // original plane-wave index -> sorted position
   std::vector<int> gsorted;  // [W][3] in sorted order
   DevBuf<int> perm_d, plane_start, plane_off;
   int off_N2 = 0, off_N3 = 0;
@@ -75,7 +80,8 @@ struct DevWF {
   SphereSet proj;
   std::vector<int> site_lmoff;
   DevBuf<float2> P;
-  bool p_ready = false;
+  bool tables_ready = false;  // element and sphere tables built (setup_projections called)
+  bool p_ready = false;       // P holds <p|psi> of every band
   Radices r[3];
   DevBuf<float2> tw[3];
 };
@@ -172,6 +178,8 @@ static DevWF &mirror(pswf_t *wf) {
     std::stable_sort(q.perm.begin(), q.perm.end(), [G](int a, int b) {
       return std::tie(G[3 * a], G[3 * a + 1], G[3 * a + 2]) < std::tie(G[3 * b], G[3 * b + 1], G[3 * b + 2]);
     });
+    q.invperm.resize(q.W);
+    for (int t = 0; t < q.W; t++) q.invperm[q.perm[t]] = t;
     q.gsorted.resize(3 * (size_t)q.W);
     for (int t = 0; t < q.W; t++)
       for (int a = 0; a < 3; a++) q.gsorted[3 * t + a] = G[3 * q.perm[t] + a];
@@ -185,7 +193,21 @@ static DevWF &mirror(pswf_t *wf) {
   return ref;
 }
 
-// Uploads the coefficients of every band into the sorted device layout.
+static int pageable_access() {
+  static int v = -1;
+  if (v < 0) {
+    int a = 0, b = 0, dev = device();
+    PAWPY_CUDA(cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev));
+    PAWPY_CUDA(cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+    v = (a && b) ? 1 : 0;
+  }
+  return v;
+}
+
+// Uploads the coefficients of every band into the sorted device layout. Where
+// the device reads pageable host memory through the host page tables (e.g. a
+// Grace-Blackwell node), a kernel reads the band arrays in place; otherwise
+// each band is copied with cudaMemcpyAsync and permuted on the device.
 static void ensure_coeffs(DevWF &d) {
   if (d.c_ready) return;
   size_t total = 0;
@@ -193,6 +215,23 @@ static void ensure_coeffs(DevWF &d) {
   d.C.alloc(total);
   int maxW = 0;
   for (auto &q : d.kp) maxW = std::max(maxW, q.W);
+  if (pageable_access()) {
+    std::vector<const float2 *> hp((size_t)d.nk * d.nband);
+    for (int k = 0; k < d.nk; k++)
+      for (int b = 0; b < d.nband; b++)
+        hp[(size_t)k * d.nband + b] = reinterpret_cast<const float2 *>(d.wf->kpts[k]->bands[b]->Cs);
+    DevBuf<const float2 *> hpd(hp.size());
+    hpd.upload(hp.data(), hp.size());
+    for (int k = 0; k < d.nk; k++) {
+      DevKpt &q = d.kp[k];
+      DevBuf<int> inv(std::max(1, q.W));
+      inv.upload(q.invperm.data(), q.W);
+      launch_load_host_bands(hpd.p + (size_t)k * d.nband, q.W, inv.p, d.C.p + q.c_off, q.Wpad, d.nband);
+    }
+    sync();  // the host arrays must stay untouched until the reads are done
+    d.c_ready = true;
+    return;
+  }
   DevBuf<float2> raw((size_t)d.nband * maxW);
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
@@ -228,6 +267,7 @@ static void set_grid(DevWF &d, const int *fftg) {
   }
   for (auto &q : d.kp) q.off_N2 = q.off_N3 = 0;
   d.p_ready = false;
+  d.tables_ready = false;
 }
 
 // Plane offsets (j*N3 + k) of the sorted plane waves for the current grid.
@@ -258,6 +298,8 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
   t->nproj = np;
   t->total = pp.total_projs;
   PAWPY_REQUIRE(t->total <= 32, "more than 32 projector channels per element");
+  for (int k = 0; k < np; k++)
+    PAWPY_REQUIRE(pp.funcs[k].l >= 0 && pp.funcs[k].l <= 3, "projector channels need 0 <= l <= 3");
   std::vector<double> pf((size_t)np * nd), ps((size_t)np * 3 * nd), sf((size_t)np * nd), ss((size_t)np * 3 * nd);
   for (int k = 0; k < np; k++) {
     const funcset_t &f = pp.funcs[k];
@@ -297,6 +339,11 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
       s.lm_l[i] = t->lm_l[i];
       s.lm_m[i] = t->lm_m[i];
       s.lm_f[i] = t->lm_n[i];
+      int l = t->lm_l[i], m = t->lm_m[i];
+      double f1 = 1, f2 = 1;
+      for (int q = 2; q <= l - m; q++) f1 *= q;
+      for (int q = 2; q <= l + m; q++) f2 *= q;
+      s.lm_norm[i] = std::sqrt((2 * l + 1) / (4 * M_PI) * f1 / f2);
     }
   }
   t->D.assign((size_t)t->total * t->total, 0.0);
@@ -311,9 +358,10 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
 static double vnorm(const double *v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
 // Sphere tables of sites site_nums (indices into coords/labels) of elements
-// `sp` on the grid of `g` (lattice lat). Follows setup_site (utils.c:590-696):
-// the half box per axis (|a_j x a_k| rmax / V) N + 1, the centre
-// round(coord N), the cutoff (ndata_p - 1) rmax / ndata_{labels[s]}.
+// `sp` on the grid of lattice `lat`. Follows setup_site (utils.c:590-696): the
+// half box per axis (|a_j x a_k| rmax / V) N + 1, the centre round(coord N),
+// the cutoff (ndata_p - 1) rmax / ndata_{labels[s]} (the reference indexes the
+// denominator by the list position s). Tables carry dV V^-1/2.
 static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const int *labels,
                           const double *coords, const std::vector<std::unique_ptr<SpeciesTables>> &sp,
                           bool smooth, const double *lat, const int *N, double vol,
@@ -333,6 +381,7 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
   cross(lat + 0, lat + 6, c13);
   cross(lat + 0, lat + 3, c12);
   S.host.resize(S.nsites);
+  std::vector<int2> slabs;
   int lmoff = 0;
   for (int s = 0; s < S.nsites; s++) {
     int p = site_nums[s];
@@ -347,7 +396,6 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
     h.g[1] = (int)(vnorm(c13) * rmax / vol * N[1]) + 1;
     h.g[2] = (int)(vnorm(c12) * rmax / vol * N[2]) + 1;
     for (int a = 0; a < 3; a++) h.c[a] = (int)std::round(coords[3 * p + a] * N[a]);
-    // denominator read through labels[s] (the list position), as the reference does
     int e_s = labels[s];
     PAWPY_REQUIRE(e_s >= 0 && e_s < (int)sp.size(), "site label out of range");
     h.R0 = (spd.size - 1) * rmax / sd[e_s].size;
@@ -355,6 +403,7 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
     h.lm_off = lmoff;
     lmoff += h.total;
     S.max_total = std::max(S.max_total, h.total);
+    for (int jb = 0; jb <= 2 * h.g[1]; jb++) slabs.push_back(make_int2(s, jb));
   }
   S.Ptot = lmoff;
   DevBuf<double> Ld(9);
@@ -363,22 +412,44 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
   Nd.upload(N, 3);
   S.sites.alloc(S.nsites);
   S.sites.upload(S.host.data(), S.nsites);
-  DevBuf<int> counts(S.nsites);
-  launch_sphere_count(S.sites.p, S.nsites, Ld.p, Nd.p, counts.p);
-  std::vector<int> hc(S.nsites);
-  counts.download(hc.data(), S.nsites);
+  DevBuf<int2> slabs_d(slabs.size());
+  slabs_d.upload(slabs.data(), slabs.size());
+  DevBuf<int> counts(slabs.size());
+  launch_slab_count(S.sites.p, slabs_d.p, (int)slabs.size(), Ld.p, Nd.p, counts.p);
+  std::vector<int> hc(slabs.size());
+  counts.download(hc.data(), hc.size());
   sync();
   long long pt = 0, val = 0;
+  S.site_pt.assign(S.nsites, 0);
+  S.site_val.assign(S.nsites, 0);
+  S.site_npts.assign(S.nsites, 0);
+  for (size_t q = 0; q < slabs.size(); q++) S.site_npts[slabs[q].x] += hc[q];
   for (int s = 0; s < S.nsites; s++) {
-    S.host[s].npts = hc[s];
-    S.host[s].pt_off = pt;
-    S.host[s].val_off = val;
-    pt += hc[s];
-    val += (long long)hc[s] * S.host[s].total;
+    S.site_pt[s] = pt;
+    S.site_val[s] = val;
+    pt += S.site_npts[s];
+    val += (long long)S.site_npts[s] * S.host[s].total;
   }
+  pt = 0;
+  for (size_t q = 0; q < slabs.size(); q++) {
+    if (hc[q] == 0) continue;
+    int s = slabs[q].x;
+    SegFill f;
+    f.site = s;
+    f.jb = slabs[q].y;
+    f.pt_off = pt;
+    f.npts = hc[q];
+    f.site_pt = S.site_pt[s];
+    f.site_npts = S.site_npts[s];
+    f.site_val = S.site_val[s];
+    S.segs.push_back(f);
+    int j = f.jb - S.host[s].g[1] + S.host[s].c[1];
+    S.seg_plane.push_back(((j % N[1]) + N[1]) % N[1]);
+    pt += hc[q];
+  }
+  S.nseg = (int)S.segs.size();
   S.npts = pt;
   S.nvals = val;
-  S.sites.upload(S.host.data(), S.nsites);
   S.species.alloc(sd.size());
   S.species.upload(sd.data(), sd.size());
   S.nkp = (int)kpts.size();
@@ -391,44 +462,141 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
   S.idx.alloc(std::max(1LL, pt));
   S.tab.alloc(std::max(1LL, val));
   S.phase.alloc(std::max(1LL, pt * S.nkp));
-  double dv = vol / N[0] / N[1] / N[2];
-  launch_sphere_fill(S.sites.p, S.nsites, S.species.p, Ld.p, Nd.p, dv, kcd.p, S.nkp, pt, S.idx.p, S.tab.p,
-                     S.phase.p);
+  DevBuf<SegFill> segs_d(std::max(1, S.nseg));
+  segs_d.upload(S.segs.data(), S.nseg);
+  double wscale = vol / N[0] / N[1] / N[2] * std::pow(vol, -0.5);
+  launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, Ld.p, Nd.p, wscale, kcd.p, S.nkp, pt, S.idx.p,
+                  S.tab.p, S.phase.p);
   sync();
 }
 
-// Batched FFT + gather of every band of wavefunction d onto sphere sets.
-// outs[i] receives [nk][nband][sets[i]->Ptot].
+// One FFT pass over every band of wavefunction d, gathering onto several
+// sphere sets at once. outs[i] receives [nk][nband][sets[i]->Ptot].
 static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
                           const std::vector<float2 *> &outs) {
   ensure_coeffs(d);
-  long long grid = (long long)d.N[0] * d.N[1] * d.N[2];
+  // merged point space (X) over the sets; segments sorted by plane for the pick
+  std::vector<GatherSeg> segs;
+  std::vector<int> plane_of;
+  std::vector<ChunkContract> chunks;
+  struct SetMaps {
+    std::vector<int> col_site, col_lm, site_ptr, chunk_off;
+  };
+  std::vector<SetMaps> maps(sets.size());
+  long long xtot = 0;
+  int ptot = 0, max_total = 0;
+  const int CHUNK = 512;
+  for (size_t i = 0; i < sets.size(); i++) {
+    const SphereSet &S = *sets[i];
+    for (int q = 0; q < S.nseg; q++) {
+      const SegFill &f = S.segs[q];
+      GatherSeg g;
+      g.idx = S.idx.p + f.pt_off;
+      g.phase = S.phase.p + f.pt_off;
+      g.phase_stride = S.npts;
+      g.x_off = xtot + f.pt_off;
+      g.npts = f.npts;
+      segs.push_back(g);
+      plane_of.push_back(S.seg_plane[q]);
+    }
+    SetMaps &m = maps[i];
+    m.col_site.resize(S.Ptot);
+    m.col_lm.resize(S.Ptot);
+    m.site_ptr.assign(S.nsites + 1, 0);
+    for (int s = 0; s < S.nsites; s++) {
+      int T = S.host[s].total;
+      for (int t = 0; t < T; t++) {
+        m.col_site[S.host[s].lm_off + t] = s;
+        m.col_lm[S.host[s].lm_off + t] = t;
+      }
+      int n = S.site_npts[s];
+      int nch = std::max(1, (n + CHUNK - 1) / CHUNK);
+      for (int c = 0; c < nch; c++) {
+        ChunkContract cc;
+        int p0 = (int)((long long)n * c / nch), p1 = (int)((long long)n * (c + 1) / nch);
+        cc.tab = S.tab.p + S.site_val[s] + p0;
+        cc.x_off = xtot + S.site_pt[s] + p0;
+        cc.site_npts = n;
+        cc.npts = p1 - p0;
+        cc.total = T;
+        cc.part_off = ptot;
+        m.chunk_off.push_back(ptot);
+        ptot += T;
+        chunks.push_back(cc);
+      }
+      m.site_ptr[s + 1] = (int)m.chunk_off.size();
+      max_total = std::max(max_total, T);
+    }
+    xtot += S.npts;
+  }
+  std::vector<int> order(segs.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return plane_of[a] < plane_of[b]; });
+  std::vector<GatherSeg> sorted(segs.size());
+  std::vector<int> pstart(d.N[1] + 1, 0);
+  for (size_t q = 0; q < order.size(); q++) {
+    sorted[q] = segs[order[q]];
+    pstart[plane_of[order[q]] + 1]++;
+  }
+  for (int j = 0; j < d.N[1]; j++) pstart[j + 1] += pstart[j];
+  DevBuf<GatherSeg> segs_d(std::max<size_t>(1, sorted.size()));
+  segs_d.upload(sorted.data(), sorted.size());
+  DevBuf<int> pstart_d(pstart.size());
+  pstart_d.upload(pstart.data(), pstart.size());
+  DevBuf<ChunkContract> ch_d(std::max<size_t>(1, chunks.size()));
+  ch_d.upload(chunks.data(), chunks.size());
+  struct SetMapsDev {
+    DevBuf<int> col_site, col_lm, site_ptr, chunk_off;
+  };
+  std::vector<SetMapsDev> mdev(sets.size());
+  for (size_t i = 0; i < sets.size(); i++) {
+    auto up = [](DevBuf<int> &b, const std::vector<int> &v) {
+      b.alloc(std::max<size_t>(1, v.size()));
+      b.upload(v.data(), v.size());
+    };
+    up(mdev[i].col_site, maps[i].col_site);
+    up(mdev[i].col_lm, maps[i].col_lm);
+    up(mdev[i].site_ptr, maps[i].site_ptr);
+    up(mdev[i].chunk_off, maps[i].chunk_off);
+  }
   int maxn1 = 0;
   for (auto &q : d.kp) maxn1 = std::max(maxn1, q.n1);
-  // batch of bands bounded by a 2 GiB workspace
-  long long per_band = ((long long)maxn1 * d.N[1] * d.N[2] + grid) * (long long)sizeof(float2);
-  int batch = (int)std::max(1LL, std::min<long long>(d.nband, (2LL << 30) / std::max(1LL, per_band)));
-  DevBuf<float2> H((size_t)batch * maxn1 * d.N[1] * d.N[2]);
-  DevBuf<float2> U((size_t)batch * grid);
-  float scale = (float)std::pow(d.vol, -0.5);
+  // FFT sub-batch: keep the plane-FFT intermediate near L2 size (~96 MiB)
+  long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
+  int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, (96LL << 20) / std::max(1LL, hband)));
+  // contraction batch: picked points and partial sums of up to 2 GiB
+  long long xstride = (xtot + 3) / 4 * 4;
+  long long per_band = (xstride + ptot) * (long long)sizeof(float2);
+  int cbatch = (int)std::max<long long>(fbatch, std::min<long long>(d.nband, (2LL << 30) / std::max(1LL, per_band)));
+  cbatch = std::max(1, cbatch / fbatch) * fbatch;
+  cbatch = std::min(cbatch, d.nband);
+  DevBuf<float2> H((size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
+  DevBuf<float2> X((size_t)cbatch * std::max(1LL, xstride));
+  DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
     ensure_planes(d, q);
     PlaneGeom g{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
-    for (int b0 = 0; b0 < d.nband; b0 += batch) {
-      int nb = std::min(batch, d.nband - b0);
-      launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
-                        d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-      launch_fft_x(H.p, g, d.r[0], d.tw[0].p, scale, U.p, nb);
+    if (xtot == 0) continue;
+    for (int c0 = 0; c0 < d.nband; c0 += cbatch) {
+      int cn = std::min(cbatch, d.nband - c0);
+      for (int b0 = c0; b0 < c0 + cn; b0 += fbatch) {
+        int nb = std::min(fbatch, c0 + cn - b0);
+        launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
+                          d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
+        launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, X.p + (size_t)(b0 - c0) * xstride,
+                          xstride, nb);
+      }
+      launch_chunk_contract(ch_d.p, (int)chunks.size(), max_total, X.p, xstride, partial.p, ptot, cn);
       for (size_t i = 0; i < sets.size(); i++) {
         const SphereSet &S = *sets[i];
         if (S.nsites == 0) continue;
-        float2 *P = outs[i] + ((size_t)k * d.nband + b0) * S.Ptot;
-        launch_sphere_gather(S.sites.p, S.nsites, S.idx.p, S.tab.p, S.phase.p + (size_t)k * S.npts, U.p, grid,
-                             P, S.Ptot, nb, S.max_total);
+        launch_chunk_reduce(partial.p, ptot, mdev[i].col_site.p, mdev[i].col_lm.p, mdev[i].site_ptr.p,
+                            mdev[i].chunk_off.p, outs[i], S.Ptot, cn, (long long)k * d.nband + c0);
       }
     }
   }
+  sync();
 }
 
 // ============================================================= host projection_t output
@@ -484,8 +652,14 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   d.site_lmoff.resize(num_sites);
   for (int s = 0; s < num_sites; s++) d.site_lmoff[s] = d.proj.host[s].lm_off;
   d.P.alloc((size_t)d.nk * d.nband * d.proj.Ptot);
-  project_bands(d, {&d.proj}, {d.P.p});
-  d.p_ready = true;
+  d.tables_ready = true;
+  d.p_ready = false;
+  // With host projections off the transform is deferred, so that overlap_setup_real can gather the
+  // smoothed partial waves in the same FFT pass (the reference transforms every band twice).
+  if (g_host_proj) {
+    project_bands(d, {&d.proj}, {d.P.p});
+    d.p_ready = true;
+  }
   {
     // results of earlier pairs involving this wavefunction are stale now
     std::lock_guard<std::recursive_mutex> lk(g_mu);
@@ -548,7 +722,7 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   PAWPY_REQUIRE(wf_R && wf_S, "overlap_setup_real: NULL wavefunction");
   DevWF &R = mirror(wf_R);
   DevWF &S = mirror(wf_S);
-  PAWPY_REQUIRE(R.p_ready && S.p_ready, "overlap_setup_real needs setup_projections on both wavefunctions");
+  PAWPY_REQUIRE(R.tables_ready && S.tables_ready, "overlap_setup_real needs setup_projections on both wavefunctions");
   PAWPY_REQUIRE(R.nk == S.nk, "basis and defect differ in k-points");
   PairState &ps = pair_state(wf_R, wf_S);
   ps.N_R.assign(N_R, N_R + (N_R ? nNR : 0));
@@ -565,8 +739,24 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   build_spheres(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, R.lattice, R.N, R.vol, R.kp, R.rec);
   ps.WP_S.alloc(std::max<size_t>(1, (size_t)S.nk * S.nband * ps.sm_NR.Ptot));
   ps.WP_R.alloc(std::max<size_t>(1, (size_t)R.nk * R.nband * ps.sm_NS.Ptot));
-  if (nNR > 0) project_bands(S, {&ps.sm_NR}, {ps.WP_S.p});
-  if (nNS > 0) project_bands(R, {&ps.sm_NS}, {ps.WP_R.p});
+  // one FFT pass per wavefunction: pending <p|psi> and the smoothed-partial-wave projections together
+  for (int side = 0; side < 2; side++) {
+    DevWF &W = side == 0 ? S : R;
+    const SphereSet *sm = side == 0 ? &ps.sm_NR : &ps.sm_NS;
+    float2 *wp = side == 0 ? ps.WP_S.p : ps.WP_R.p;
+    std::vector<const SphereSet *> sets;
+    std::vector<float2 *> outs;
+    if (!W.p_ready) {
+      sets.push_back(&W.proj);
+      outs.push_back(W.P.p);
+    }
+    if (sm->nsites > 0) {
+      sets.push_back(sm);
+      outs.push_back(wp);
+    }
+    if (!sets.empty()) project_bands(W, sets, outs);
+    W.p_ready = true;
+  }
   // N_RS pair matrices (projector.c:682-719)
   ps.Q.assign(nNRS, {});
   ps.dcoords.assign(3 * (size_t)nNRS, 0.0);
@@ -706,7 +896,16 @@ static void ensure_pseudo(PairState &ps, int flip) {
 }
 
 // Column maps of the augmentation (see aug.cu) for the given site lists.
+static void ensure_projections(DevWF &d) {
+  PAWPY_REQUIRE(d.tables_ready, "setup_projections has not been called for this wavefunction");
+  if (d.p_ready) return;
+  project_bands(d, {&d.proj}, {d.P.p});
+  d.p_ready = true;
+}
+
 static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip) {
+  ensure_projections(*ps.R);
+  ensure_projections(*ps.S);
   AugKey key;
   for (int i = 0; i < 6; i++) key.lists[i] = lists[i];
   key.flip = flip ? 1 : 0;

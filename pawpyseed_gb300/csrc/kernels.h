@@ -11,6 +11,10 @@ namespace pawpy {
 // ---- coefficients ----
 // C[b][t] = Cu[b][perm[t]] for t < W, 0 for W <= t < Wpad (b < nb)
 void launch_permute(const float2 *Cu, int W, const int *perm, float2 *C, int Wpad, int nb);
+// C[b][invperm[w]] = host_bands[b][w] read straight from pageable host memory (devices that
+// access it through the host page tables), zero for the padding W <= t < Wpad
+void launch_load_host_bands(const float2 *const *host_bands, int W, const int *invperm, float2 *C, int Wpad,
+                            int nb);
 
 // ---- FFT (backward, exp(+i)) ----
 struct PlaneGeom {
@@ -21,9 +25,6 @@ struct PlaneGeom {
 void launch_fft_planes(const float2 *C, int Wpad, const int *plane_start, const int *plane_off,
                        const PlaneGeom &g, const Radices &r2, const Radices &r3, const float2 *tw2,
                        const float2 *tw3, float2 *H, int nb);
-// u[b][i][j][k] = scale * sum_p H[b][p][j][k] exp(2 pi i (g1min+p) i / N1)
-void launch_fft_x(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
-                  float scale, float2 *u, int nb);
 // Generic in-place transform of full grids along one axis (single-band paths).
 void launch_fft_axis(float2 *grid, int nb, int N1, int N2, int N3, int axis, const Radices &r,
                      const float2 *tw);
@@ -42,29 +43,59 @@ struct SpeciesDev {      // radial data of one element, device pointers
   double grid_rmax;      // the linear grid's rmax
   int r0_size;           // proj_gridsize used for the cutoff denominator
   int lm_l[32], lm_m[32], lm_f[32];
+  double lm_norm[32];    // sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) of each channel
 };
 struct SiteDesc {
   double coord[3];
   int species;
   int g[3], c[3];        // half box and centre (grid units)
-  double R0;
-  long long pt_off;      // first point of this site in the concatenated tables
-  long long val_off;     // first table value of this site (tables are [total][npts] per site)
-  int npts;
+  double R0;             // sphere cutoff
   int lm_off;            // first lm channel of this site in the output vector
-  int total;
+  int total;             // lm channels
 };
-// pass 1: count points inside each sphere -> counts[s]
-void launch_sphere_count(const SiteDesc *sites, int nsites, const double *lattice, const int *fftg,
-                         int *counts);
-// pass 2: indices, conj(radial*Ylm)*dV in lm-major tables, and exp(i k.path) for nkp k-points
-void launch_sphere_fill(const SiteDesc *sites, int nsites, const SpeciesDev *species,
-                        const double *lattice, const int *fftg, double dv, const double *kcart,
-                        int nkp, long long total_pts, int *idx, float2 *tab, float2 *phase);
-// P[b][lm_off+lm] = sum_pt tab[lm][pt] * u[b][idx[pt]] * phase[pt]  (one k-point)
-void launch_sphere_gather(const SiteDesc *sites, int nsites, const int *idx, const float2 *tab,
-                          const float2 *phase, const float2 *u, long long grid, float2 *P, int Ptot,
-                          int nb, int max_total);
+// one slab of a site's box (fixed box row jb along the second axis) with points
+struct SegFill {
+  int site, jb;
+  long long pt_off;      // first point of the segment in the set's point arrays
+  int npts;
+  long long site_pt;     // first point of the segment's site
+  int site_npts;         // points of the site
+  long long site_val;    // first table value of the site (tables are [total][site_npts] per site)
+};
+// a segment as the point pick sees it
+struct GatherSeg {
+  const int *idx;        // i*N3 + k inside the plane
+  const float2 *phase;   // exp(i k.path): phase[kq*phase_stride + p]
+  long long phase_stride;
+  long long x_off;       // position of the segment's first point in the picked-point vector
+  int npts;
+};
+// a chunk (<= 512 consecutive points) of one site as the contraction sees it
+struct ChunkContract {
+  const float2 *tab;     // the site's table [total][site_npts], offset to the chunk's first point
+  long long x_off;       // first point of the chunk in the picked-point vector
+  int site_npts;         // row stride of the site's table
+  int npts, total;
+  int part_off;          // offset of the chunk's partial sums in the per-band partial vector
+};
+// pass 1: count the inside points of every slab
+void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, const double *lattice,
+                       const int *fftg, int *counts);
+// pass 2: compact and tabulate every non-empty slab (FP64, stored complex64)
+void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
+                     const double *lattice, const int *fftg, double wscale, const double *kcart, int nkp,
+                     long long total_pts, int *idx, float2 *tab, float2 *phase);
+// x-axis transform of each plane j of nb bands, then X[b][x_off + p] = u(point p) exp(i k.path_p) for
+// the segments of plane j (segs sorted by plane; plane_start[N2+1])
+void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
+                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb);
+// partial[b][part_off + lm] = sum_p X[b][x_off + p] * tab[lm][p] over each chunk, bands b < nb
+void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
+                           long long xstride, float2 *partial, int ptot, int nb);
+// P[(band_base + b)*Ptot + o] = sum of partial[b][chunk_off[e] + col_lm[o]] over the chunks e of the
+// site of column o (site_ptr CSR), in chunk order
+void launch_chunk_reduce(const float2 *partial, int ptot, const int *col_site, const int *col_lm,
+                         const int *site_ptr, const int *chunk_off, float2 *P, int Ptot, int nb, long long band_base);
 
 // ---- overlap GEMM (FP32 complex, SIMT) ----
 // For each batch z < nz: out_z[n][m] = sum_k conj(A_z[m][k]) * B_z[n][k], with the K range split

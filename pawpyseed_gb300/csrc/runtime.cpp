@@ -225,4 +225,13 @@ int pawpy_gpu_kernel_stats(char *buf, int len, int reset) {
 
 long long pawpy_gpu_device_bytes(void) { return device_bytes(); }
 
+int pawpy_gpu_pageable_memory_access(void) {
+  PAWPY_API_BEGIN
+  int dev = device(), a = 0, b = 0;
+  PAWPY_CUDA(cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev));
+  PAWPY_CUDA(cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+  return (a ? 1 : 0) | (b ? 2 : 0);
+  PAWPY_API_END(-1)
+}
+
 }  // extern "C"

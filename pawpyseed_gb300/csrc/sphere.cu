@@ -1,0 +1,365 @@
+// Augmentation-sphere tables, the sphere-point pick fused into the last FFT
+// pass, and the per-site contraction that gives <p_lm|psi>.
+//
+// A site's sphere (setup_site, utils.c:590-696) is cut into slabs: the grid
+// points of its box with one fixed index j along the second lattice axis.
+// Non-empty slabs are "segments". Tables are built per segment, in double
+// precision, with the points of a segment in (i, k) order:
+//   idx  = i*N3 + k (position inside the N1 x N3 plane j)
+//   tab  = conj(p(r) Y_lm(theta, phi)) * dV * V^-1/2   [total][site points]
+//   phase= exp(i k.path) for every k-point              [nkp][all points]
+// (onto_projector_helper, projector.c:223-274, applies dV and exp(i k.path);
+// fft3d, linalg.c:33-38, the V^-1/2 that is folded in here.)
+//
+// The x-axis FFT kernel owns one plane j of one band in shared memory after
+// its transform and writes u(point) exp(i k.path) for every sphere point in
+// that plane into a compact vector X (the real-space grid never goes to HBM).
+// The contraction sum_p X[b][p] tab[lm][p] of each site then runs as a small
+// register-blocked complex product over (bands x lm channels).
+#include <cuda_runtime.h>
+
+#include "fft_tmpl.cuh"
+#include "kernels.h"
+
+namespace pawpy {
+
+__device__ __forceinline__ void s_to_cart(const double *f, const double *L, double *o) {
+  double t0 = f[0] * L[0] + f[1] * L[3] + f[2] * L[6];
+  double t1 = f[0] * L[1] + f[1] * L[4] + f[2] * L[7];
+  double t2 = f[0] * L[2] + f[1] * L[5] + f[2] * L[8];
+  o[0] = t0;
+  o[1] = t1;
+  o[2] = t2;
+}
+
+// |v| rounded once, as the reference's pow(x, 0.5) (a correctly rounded square root) gives it
+__device__ __forceinline__ double s_norm(const double *v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+__device__ __forceinline__ int box_i(const SiteDesc &s, int a, int off) { return off - s.g[a] + s.c[a]; }
+
+// grid point (i, j, k) of slab (site s, box row jb), linear (i,k) index q; returns inside and the path
+__device__ __forceinline__ bool slab_point(const SiteDesc &s, int jb, int q, const double *L, const int *N,
+                                           int *ijk, double *path) {
+  int w2 = 2 * s.g[2] + 1;
+  ijk[0] = box_i(s, 0, q / w2);
+  ijk[1] = box_i(s, 1, jb);
+  ijk[2] = box_i(s, 2, q % w2);
+  double fr[3] = {(double)ijk[0] / N[0] - s.coord[0], (double)ijk[1] / N[1] - s.coord[1],
+                  (double)ijk[2] / N[2] - s.coord[2]};
+  s_to_cart(fr, L, path);
+  return s_norm(path) < s.R0;
+}
+
+__global__ void k_slab_count(const SiteDesc *__restrict__ sites, const int2 *__restrict__ slabs,
+                             const double *__restrict__ Lg, const int *__restrict__ Ng, int *__restrict__ counts) {
+  __shared__ int total;
+  const int2 sl = slabs[blockIdx.x];
+  const SiteDesc s = sites[sl.x];
+  double L[9];
+  int N[3] = {Ng[0], Ng[1], Ng[2]};
+  for (int i = 0; i < 9; i++) L[i] = Lg[i];
+  if (threadIdx.x == 0) total = 0;
+  __syncthreads();
+  int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1), c = 0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    int ijk[3];
+    double path[3];
+    if (slab_point(s, sl.y, q, L, N, ijk, path)) c++;
+  }
+  atomicAdd(&total, c);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, const double *lattice,
+                       const int *fftg, int *counts) {
+  if (nslabs <= 0) return;
+  PAWPY_LAUNCH("sphere_count", k_slab_count<<<nslabs, 256, 0, stream()>>>(sites, slabs, lattice, fftg, counts));
+}
+
+// One CTA per segment: compact the slab's inside points in (i, k) order and
+// tabulate them (double precision, rounded to complex64 at the end).
+__global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__restrict__ segs,
+                           const SpeciesDev *__restrict__ species, const double *__restrict__ Lg,
+                           const int *__restrict__ Ng, double wscale, const double *__restrict__ kcart, int nkp,
+                           long long total_pts, int *__restrict__ idx, float2 *__restrict__ tab,
+                           float2 *__restrict__ phase) {
+  __shared__ int warp_cnt[32];
+  __shared__ int base_s;
+  const SegFill sg = segs[blockIdx.x];
+  const SiteDesc s = sites[sg.site];
+  const SpeciesDev &sp = species[s.species];
+  double L[9];
+  int N[3] = {Ng[0], Ng[1], Ng[2]};
+  for (int i = 0; i < 9; i++) L[i] = Lg[i];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) base_s = 0;
+  __syncthreads();
+  const int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1);
+  for (int start = 0; start < n; start += blockDim.x) {
+    int q = start + threadIdx.x;
+    int ijk[3];
+    double path[3];
+    bool in = q < n && slab_point(s, sg.jb, q, L, N, ijk, path);
+    unsigned m = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) warp_cnt[wid] = __popc(m);
+    __syncthreads();
+    int before = 0, chunk = 0;
+    for (int w = 0; w < nw; w++) {
+      if (w < wid) before += warp_cnt[w];
+      chunk += warp_cnt[w];
+    }
+    int pos = base_s + before + __popc(m & ((1u << lane) - 1u));
+    if (in && pos < sg.npts) {
+      int ii = ((ijk[0] % N[0]) + N[0]) % N[0];
+      int jj = ((ijk[1] % N[1]) + N[1]) % N[1];
+      int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
+      idx[sg.pt_off + pos] = ii * N[2] + kk;
+      // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73)
+      double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
+      double t[3] = {0, 0, 0}, r = INFINITY;
+      for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++)
+          for (int c = -1; c <= 1; c++) {
+            double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
+            double v[3];
+            s_to_cart(f, L, v);
+            double dd = s_norm(v);
+            if (dd < r) {
+              r = dd;
+              t[0] = v[0];
+              t[1] = v[1];
+              t[2] = v[2];
+            }
+          }
+      // Y_lm(theta, phi) of the displacement t without transcendental calls:
+      // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
+      // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
+      double ct = 1.0, cp = 1.0, sp_ = 0.0;
+      if (r != 0) {
+        ct = t[2] / r;
+        double rho = sqrt(t[0] * t[0] + t[1] * t[1]);
+        if (rho != 0 && r - fabs(t[2]) != 0) {
+          cp = t[0] / rho;
+          sp_ = t[1] / rho;
+        }
+      }
+      double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+      // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence
+      double P[4][4];
+      P[0][0] = 1.0;
+      for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * st * P[m - 1][m - 1];
+      for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ct * P[m][m];
+      for (int m = 0; m <= 1; m++)
+        for (int l = m + 2; l <= 3; l++) P[l][m] = ((2 * l - 1) * ct * P[l - 1][m] - (l + m - 1) * P[l - 2][m]) / (l - m);
+      double er[4] = {1.0, cp, 0, 0}, ei[4] = {0.0, sp_, 0, 0};
+      for (int m = 2; m <= 3; m++) {
+        er[m] = er[m - 1] * cp - ei[m - 1] * sp_;
+        ei[m] = er[m - 1] * sp_ + ei[m - 1] * cp;
+      }
+      // linear-grid spline interpolation (proj_interpolate, utils.c:461-475); x_j = rmax/size*j
+      double xlast = sp.grid_rmax / sp.size * (sp.size - 1);
+      int ind = (int)(r / sp.grid_rmax * sp.size);
+      if (ind > sp.size - 2) ind = sp.size - 2;
+      double dd = r - sp.grid_rmax / sp.size * ind;
+      double rad = 0.0;
+      int last_f = -1;
+      for (int lm = 0; lm < sp.total; lm++) {
+        int l = sp.lm_l[lm], mm = sp.lm_m[lm], fi = sp.lm_f[lm];
+        if (fi != last_f) {
+          const double *f = sp.f + (long long)fi * sp.size;
+          const double *sb = sp.spl + (long long)fi * 3 * sp.size;
+          rad = r > xlast ? 0.0 : f[ind] + dd * (sb[ind] + dd * (sb[sp.size + ind] + dd * sb[2 * sp.size + ind]));
+          last_f = fi;
+        }
+        int am = mm < 0 ? -mm : mm;
+        double plm = l <= 3 ? P[l][am] : 0.0;
+        // m = -a < 0: P_l^{-a} = (-1)^a (l-a)!/(l+a)! P_l^a (utils.c:379-380)
+        double y = sp.lm_norm[lm] * plm * rad * wscale;
+        if (mm < 0) {
+          double ratio = 1.0;
+          for (int q = l - am + 1; q <= l + am; q++) ratio *= q;  // (l+|m|)!/(l-|m|)!
+          y = y / ratio * ((am & 1) ? -1.0 : 1.0);
+        }
+        double cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
+        // conj(radial * Y_lm) * dV * V^-1/2
+        tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] =
+            make_float2((float)(y * cs), (float)(-y * sn));
+      }
+      for (int kq = 0; kq < nkp; kq++) {
+        double kr = kcart[3 * kq] * path[0] + kcart[3 * kq + 1] * path[1] + kcart[3 * kq + 2] * path[2];
+        double sn, cs;
+        sincos(kr, &sn, &cs);
+        phase[(long long)kq * total_pts + sg.pt_off + pos] = make_float2((float)cs, (float)sn);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base_s += chunk;
+    __syncthreads();
+  }
+}
+
+void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
+                     const double *lattice, const int *fftg, double wscale, const double *kcart, int nkp,
+                     long long total_pts, int *idx, float2 *tab, float2 *phase) {
+  if (nseg <= 0) return;
+  PAWPY_LAUNCH("sphere_fill", k_seg_fill<<<nseg, 128, 0, stream()>>>(sites, segs, species, lattice, fftg, wscale,
+                                                                    kcart, nkp, total_pts, idx, tab, phase));
+}
+
+// ---------------------------------------------------------------------------
+// x-axis transform of plane j, then pick the sphere points lying in it.
+
+__global__ void __launch_bounds__(256) k_fft_x_pick(const float2 *__restrict__ H, PlaneGeom g, Radices r1,
+                                                    const float2 *__restrict__ tw1g,
+                                                    const GatherSeg *__restrict__ segs,
+                                                    const int *__restrict__ plane_start, int kq,
+                                                    float2 *__restrict__ X, long long xstride) {
+  extern __shared__ float2 sm[];
+  const int tile = g.N1 * g.N3;
+  float2 *a = sm, *b = sm + tile, *tw1 = sm + 2 * tile;
+  const int j = blockIdx.x, band = blockIdx.y;
+  for (int i = threadIdx.x; i < g.N1; i += blockDim.x) tw1[i] = tw1g[i];
+  for (int i = threadIdx.x; i < tile; i += blockDim.x) {
+    int row = i / g.N3, k = i - row * g.N3;
+    int p = row - g.g1min;
+    p = ((p % g.N1) + g.N1) % g.N1;
+    float2 v = make_float2(0.f, 0.f);
+    if (p < g.n1) v = H[(((long long)band * g.n1 + p) * g.N2 + j) * g.N3 + k];
+    a[i] = v;
+  }
+  __syncthreads();
+  const float2 *u = block_fft_any<1, false>(a, b, r1, g.N3, 1, g.N3, tw1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  float2 *xb = X + (long long)band * xstride;
+  for (int si = plane_start[j] + warp; si < plane_start[j + 1]; si += nwarp) {
+    const GatherSeg sg = segs[si];
+    const float2 *ph = sg.phase + (long long)kq * sg.phase_stride;
+    for (int p = lane; p < sg.npts; p += 32) xb[sg.x_off + p] = cmul(u[sg.idx[p]], ph[p]);
+  }
+}
+
+void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
+                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb) {
+  if (nb <= 0) return;
+  size_t smem = sizeof(float2) * (2 * (size_t)g.N1 * g.N3 + g.N1);
+  PAWPY_REQUIRE(smem <= 227 * 1024, "FFT tile does not fit in shared memory");
+  static size_t conf = 0;
+  if (smem > 48 * 1024 && smem > conf) {
+    PAWPY_CUDA(cudaFuncSetAttribute(k_fft_x_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    conf = smem;
+  }
+  dim3 grid(g.N2, nb);
+  PAWPY_LAUNCH("fft_x_pick", k_fft_x_pick<<<grid, 256, smem, stream()>>>(H, g, r1, tw1, segs, plane_start, kq, X,
+                                                                        xstride));
+}
+
+// ---------------------------------------------------------------------------
+// <p_lm|psi_b> = sum_p X[b][p] tab[lm][p], chunk by chunk.
+//
+// One CTA per (chunk, block of 32 bands), 128 threads: thread t owns the band
+// pair (2*(t/8), 2*(t/8)+1) and the channels lm = t%8 + 8q. Points go through
+// shared memory 64 at a time (rows padded against bank conflicts). Each
+// table value read feeds two bands.
+namespace {
+constexpr int CB = 32, CP = 64, CPP = CP + 1, CT = 128;
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(CT) k_chunk_contract(const ChunkContract *__restrict__ chunks,
+                                                       const float2 *__restrict__ X, long long xstride,
+                                                       float2 *__restrict__ partial, int ptot, int nb) {
+  __shared__ float2 xs[CB][CPP];
+  __shared__ float2 ts[8 * NQ][CPP];
+  const ChunkContract cc = chunks[blockIdx.x];
+  const int b0 = blockIdx.y * CB;
+  const int tid = threadIdx.x, bp = tid >> 3, lq = tid & 7;
+  float ar[2][NQ], ai[2][NQ];
+#pragma unroll
+  for (int h = 0; h < 2; h++)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) ar[h][q] = ai[h][q] = 0.f;
+  for (int p0 = 0; p0 < cc.npts; p0 += CP) {
+    const int np = min(CP, cc.npts - p0);
+#pragma unroll 4
+    for (int e = tid; e < CB * CP; e += CT) {
+      int bb = e / CP, pp = e - bb * CP;
+      float2 v = make_float2(0.f, 0.f);
+      if (pp < np && b0 + bb < nb) v = X[(long long)(b0 + bb) * xstride + cc.x_off + p0 + pp];
+      xs[bb][pp] = v;
+    }
+    for (int e = tid; e < cc.total * CP; e += CT) {
+      int t = e / CP, pp = e - t * CP;
+      ts[t][pp] = pp < np ? cc.tab[(long long)t * cc.site_npts + p0 + pp] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int pp = 0; pp < np; pp++) {
+      float2 x0 = xs[2 * bp][pp], x1 = xs[2 * bp + 1][pp];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) {
+        if (lq + 8 * q < cc.total) {
+          float2 v = ts[lq + 8 * q][pp];
+          ar[0][q] = fmaf(v.x, x0.x, fmaf(-v.y, x0.y, ar[0][q]));
+          ai[0][q] = fmaf(v.x, x0.y, fmaf(v.y, x0.x, ai[0][q]));
+          ar[1][q] = fmaf(v.x, x1.x, fmaf(-v.y, x1.y, ar[1][q]));
+          ai[1][q] = fmaf(v.x, x1.y, fmaf(v.y, x1.x, ai[1][q]));
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    int band = b0 + 2 * bp + h;
+    if (band >= nb) continue;
+    float2 *o = partial + (long long)band * ptot + cc.part_off;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      int t = lq + 8 * q;
+      if (t < cc.total) o[t] = make_float2(ar[h][q], ai[h][q]);
+    }
+  }
+}
+
+void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
+                           long long xstride, float2 *partial, int ptot, int nb) {
+  if (nchunks <= 0 || nb <= 0) return;
+  dim3 grid(nchunks, ceil_div(nb, CB));
+  if (max_total <= 8)
+    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<1><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
+  else if (max_total <= 24)
+    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<3><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
+  else if (max_total <= 32)
+    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<4><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
+  else
+    throw Error(ERR_UNSUPPORTED, "more than 32 projector channels on one site");
+}
+
+__global__ void k_chunk_reduce(const float2 *__restrict__ partial, int ptot, const int *__restrict__ col_site,
+                               const int *__restrict__ col_lm, const int *__restrict__ site_ptr,
+                               const int *__restrict__ chunk_off, float2 *__restrict__ P, int Ptot, int nb,
+                               long long band_base) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  int b = blockIdx.y;
+  if (o >= Ptot || b >= nb) return;
+  int s = col_site[o], lm = col_lm[o];
+  const float2 *pb = partial + (long long)b * ptot;
+  float re = 0.f, im = 0.f;
+  for (int e = site_ptr[s]; e < site_ptr[s + 1]; e++) {
+    float2 v = pb[chunk_off[e] + lm];
+    re += v.x;
+    im += v.y;
+  }
+  P[(band_base + b) * Ptot + o] = make_float2(re, im);
+}
+
+void launch_chunk_reduce(const float2 *partial, int ptot, const int *col_site, const int *col_lm,
+                         const int *site_ptr, const int *chunk_off, float2 *P, int Ptot, int nb, long long band_base) {
+  if (Ptot <= 0 || nb <= 0) return;
+  dim3 grid(ceil_div(Ptot, 128), nb);
+  PAWPY_LAUNCH("sphere_reduce", k_chunk_reduce<<<grid, 128, 0, stream()>>>(partial, ptot, col_site, col_lm,
+                                                                          site_ptr, chunk_off, P, Ptot, nb,
+                                                                          band_base));
+}
+
+}  // namespace pawpy

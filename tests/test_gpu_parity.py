@@ -106,6 +106,29 @@ def test_project_all_matches_band_loop(name, workload_dirs, oracle_projectors):
     assert np.abs(full - loop).max() <= 2e-6
 
 
+@pytest.mark.parametrize("name", ["cfg1s", "cfg2s", "cfg3s"])
+def test_deferred_projections_single_fft_pass(name, workload_dirs, oracle_projectors):
+    """With host projection_t output off, <p|psi> and the smoothed-partial-wave projections of a
+    wavefunction come from one FFT pass; results equal the FP64 truth."""
+    from pawpyseed_gb300 import _lib
+    from pawpyseed_gb300.projector import Projector
+
+    L = _lib.lib()
+    L.pawpy_gpu_set_host_projections(0)
+    try:
+        basis, wf = load(workload_dirs(name))
+        pr = Projector(wf, basis)
+        full = pr.project_all()
+        op = oracle_projectors(name)
+        truth = op.full()
+        tv = np.array([op.band_vector(truth, b) for b in range(wf.nband)])
+        assert np.abs(full - tv).max() <= TOL
+        one = pr.single_band_projection(wf.nband - 1)
+        assert np.abs(one - tv[-1]).max() <= TOL
+    finally:
+        L.pawpy_gpu_set_host_projections(1)
+
+
 def test_results_deterministic_and_cached(workload_dirs):
     from pawpyseed_gb300.projector import Projector
 
