@@ -273,6 +273,25 @@ void pawpy_gpu_release(pswf_t *wf);
 /* Makes the device copy of a wavefunction's coefficients resident now. */
 int pawpy_gpu_upload(pswf_t *wf);
 
+/* No counterpart in the reference. Overlap contraction for callers that cannot
+ * allocate device memory (a process whose device memory belongs to another
+ * allocator or a fixed up-front budget, or a loop that must not pay the device
+ * synchronisation of cudaMalloc/cudaFree):
+ *   out[n*M + m] = sum_{k<K} conj(A[m*lda + k]) * B[n*ldb + k]
+ * on caller-owned device buffers (complex64, A/B 16-byte aligned, lda/ldb even
+ * and >= K, K a multiple of 16 with zero padding), FP32 accumulation, split-K
+ * partial sums reduced in a fixed order -- the contraction of pseudoprojection.
+ * It allocates nothing: partial sums and the launch descriptor live in a
+ * static device array of 32 MiB (+256 B) that every GPU loading the library
+ * holds until exit; outputs larger than M*N = 4,194,304 values are rejected.
+ * The first call on each device looks up that array's device address (make it
+ * before any stream capture). Calls share the array, so calls whose work
+ * overlaps on the GPU (e.g. on different streams) race. stream: a
+ * cudaStream_t, or NULL for the library's stream; the call is asynchronous.
+ * Returns the split count used (>= 1) or a negative status. */
+int pawpy_gpu_overlap_noalloc(const pawpy_c64 *A, long long lda, const pawpy_c64 *B, long long ldb,
+                              int M, int N, int K, pawpy_c64 *out, void *stream);
+
 /* Device-side timing on the library's stream (CUDA events). */
 void pawpy_gpu_timer_start(void);
 float pawpy_gpu_timer_stop_ms(void); /* synchronizes */

@@ -119,6 +119,8 @@ struct DevBuf {
 void launch_begin(const char *family);
 void launch_end(const char *family);
 void check_launch(const char *what);
+// Counts launches made outside PAWPY_LAUNCH (no events, no allocation).
+void note_launches(int n);
 
 // PAWPY_LAUNCH("family", kernel<<<grid, block, smem, pawpy::stream()>>>(args));
 #define PAWPY_LAUNCH(family, ...)                                                 \

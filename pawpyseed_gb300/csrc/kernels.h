@@ -109,6 +109,11 @@ struct GemmBatch {
 // One grouped launch over nz batches (uneven K allowed). splits > 1 needs a
 // workspace of splits*nz*N*M float2 and reduces in split order.
 void launch_zgemm_f32(const GemmBatch *batches_dev, int nz, int M, int N, int splits, float2 *workspace);
+// The two kernels behind launch_zgemm_f32 (64x64 tiles, 256 threads; grid (M/64, N/64, nz*splits)
+// and (M*N/1024, nz)), for callers that launch them on their own stream.
+__global__ void __launch_bounds__(256) k_zgemm_f32(const GemmBatch *batches, int M, int N, int splits,
+                                                   float2 *ws, int nz);
+__global__ void k_split_reduce(const GemmBatch *batches, const float2 *ws, int M, int N, int splits, int nz);
 
 // ---- augmentation columns of the PAW terms ----
 // A[kslice][b][c] = src[c] < Pt ? P[kslice][b][src[c]] : WP[kslice][b][src[c]-Pt]; zero for c >= Kc

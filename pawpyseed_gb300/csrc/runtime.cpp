@@ -148,6 +148,12 @@ void launch_end(const char *family) {
     PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, r.s));
 }
 
+void note_launches(int n) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  r.launches += n;
+}
+
 void check_launch(const char *what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
