@@ -640,6 +640,7 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   wf->num_elems = num_elems;
   wf->num_sites = num_sites;
   wf->pps = pps;
+  for (int e = 0; e < num_elems; e++) pps[e].num_cart_gridpts = cart_gridpts_bound(pps[e], wf->lattice, fftg);
   set_grid(d, fftg);
   d.species.clear();
   for (int e = 0; e < num_elems; e++) d.species.push_back(species_tables(pps[e]));
@@ -757,17 +758,30 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
     if (!sets.empty()) project_bands(W, sets, outs);
     W.p_ready = true;
   }
-  // N_RS pair matrices (projector.c:682-719)
+  // N_RS pair matrices (projector.c:682-719): radial integrals on the device, assembly on the host
   ps.Q.assign(nNRS, {});
   ps.dcoords.assign(3 * (size_t)nNRS, 0.0);
-  for (int i = 0; i < nNRS; i++) {
-    int s1 = ps.N_RS_R[i], s2 = ps.N_RS_S[i];
-    const ppot_t *p1 = wf_R->pps + labels_R[s1];
-    const ppot_t *p2 = wf_S->pps + labels_S[s2];
-    double r;
-    min_image_path(coords_S + 3 * s2, coords_R + 3 * s1, wf_R->lattice, ps.dcoords.data() + 3 * i, &r);
-    ps.Q[i].assign((size_t)p1->total_projs * p2->total_projs, 0.0);
-    offsite_pair_matrix(p1, p2, ps.dcoords.data() + 3 * i, reinterpret_cast<pawpy_c128 *>(ps.Q[i].data()));
+  {
+    std::vector<int> eR(nNRS), eS(nNRS);
+    std::vector<double> Rs(nNRS);
+    for (int i = 0; i < nNRS; i++) {
+      int s1 = ps.N_RS_R[i], s2 = ps.N_RS_S[i];
+      double r;
+      min_image_path(coords_S + 3 * s2, coords_R + 3 * s1, wf_R->lattice, ps.dcoords.data() + 3 * i, &r);
+      eR[i] = labels_R[s1];
+      eS[i] = labels_S[s2];
+      Rs[i] = pair_distance(ps.dcoords.data() + 3 * i);
+    }
+    std::vector<std::vector<double>> I;
+    std::vector<int> Lmax;
+    offsite_radial_integrals(wf_R->pps, wf_S->pps, eR, eS, Rs, I, Lmax);
+    for (int i = 0; i < nNRS; i++) {
+      const ppot_t *p1 = wf_R->pps + eR[i];
+      const ppot_t *p2 = wf_S->pps + eS[i];
+      ps.Q[i].assign((size_t)p1->total_projs * p2->total_projs, 0.0);
+      offsite_pair_matrix(p1, p2, ps.dcoords.data() + 3 * i, I[i].data(), Lmax[i],
+                          reinterpret_cast<pawpy_c128 *>(ps.Q[i].data()));
+    }
   }
   // host-visible results with the reference's ownership (freed by free_pswf)
   if (wf_S->overlaps) {
@@ -1059,7 +1073,7 @@ int pawpy_gpu_upload(pswf_t *wf) {
 ppot_t *get_projector_list(int num_els, int *labels, int *ls, double *wave_grids, double *projectors,
                            double *aewaves, double *pswaves, double *rmaxs, double grid_encut) {
   PAWPY_API_BEGIN
-  return build_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
+  return device_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
   PAWPY_API_END(nullptr)
 }
 

@@ -27,13 +27,24 @@ void spline_coeffs(const double *x, const double *y, int n, double *b, double *c
 double spline_integral(const double *x, const double *y, const double *b, const double *c,
                        const double *d, int n);
 double interp_log(double r, int n, const double *x, const double *f, double *const *s);
-ppot_t *build_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
-                             const double *projectors, const double *aewaves, const double *pswaves,
-                             const double *rmaxs, double grid_encut);
+// w with spline_integral(x, y, spline(y)) = sum_i w_i y_i (the integral is linear in y)
+void spline_integral_weights(const double *x, int n, double *w);
+// get_projector_list on the device (radial.cu)
+ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
+                              const double *projectors, const double *aewaves, const double *pswaves,
+                              const double *rmaxs, double grid_encut);
 // conj(<(phi-phit)_1 lm | (phi-phit)_2 l'm'>) matrix of one site pair
-// (reciprocal_offsite_wave_overlap, radial.c:116-196), row-major [P1 x P2].
-void offsite_pair_matrix(const ppot_t *pp1, const ppot_t *pp2, const double *dcoord,
-                         pawpy_c128 *out);
+// (reciprocal_offsite_wave_overlap, radial.c:116-196), row-major [P1 x P2],
+// from its radial integrals I[f1][f2][L] (L <= Lmax).
+void offsite_pair_matrix(const ppot_t *pp1, const ppot_t *pp2, const double *dcoord, const double *I,
+                         int Lmax, pawpy_c128 *out);
+double pair_distance(const double *dcoord);
+// ppot_t.num_cart_gridpts of add_num_cart_gridpts (projector.c:455-505)
+int cart_gridpts_bound(const ppot_t &pp, const double *lattice, const int *fftg);
+// I[p][f1][f2][L] = int f1(k) f2(k) k^2 j_L(k R_p) dk of every pair on the device (radial.cu)
+void offsite_radial_integrals(const ppot_t *ppR, const ppot_t *ppS, const std::vector<int> &eR,
+                              const std::vector<int> &eS, const std::vector<double> &R,
+                              std::vector<std::vector<double>> &I, std::vector<int> &Lmax);
 // Minimum-image Cartesian path coord - center (utils.c:51-73).
 void min_image_path(const double *coord, const double *center, const double *lattice, double *path,
                     double *r);

@@ -1,15 +1,9 @@
-// Radial (per-element) setup of the PAW datasets, in double precision:
-// get_projector_list (projector.c:20-171), make_pwave_overlap_matrices
-// (projector.c:507-558), the spherical Bessel transforms they use
-// (sbt.c:24-215; Talman's NumSBT, Comput. Phys. Commun. 180 (2009) 332) and
-// the off-site partial-wave overlap of a site pair (radial.c:116-196).
-//
-// The results must equal the reference's to rounding, so the algorithms are
-// the reference's: the same spline (a clamped-start / natural-end cubic whose
-// first slope is the first secant, utils.c:699-749), the same 2N-point
-// logarithmic extension and multiplier table of the transform, the same
-// k-space filter at sqrt(c*grid_encut), the same 500-point k quadrature.
-// Each is written here in its own form.
+// Host double-precision pieces of the radial work: the reference's spline
+// (a clamped-start / natural-end cubic whose first slope is the first secant,
+// utils.c:699-749) and its integral, log-grid interpolation (utils.c:477-489),
+// and the off-site partial-wave overlap of a site pair (radial.c:116-196)
+// with its 500-point k quadrature. The per-element setup runs on the device
+// (radial.cu).
 #include <cmath>
 #include <complex>
 #include <cstdlib>
@@ -65,6 +59,52 @@ double spline_integral(const double *x, const double *y, const double *b, const 
   return s;
 }
 
+// Weights w with spline_integral(x, y, spline_coeffs(x, y)) = sum_i w_i y_i for
+// every y: the spline (utils.c:699-749) and its integral are linear in y, so w
+// is the gradient of the integral, obtained in O(n) by running the recurrences
+// in reverse. Per interval the integral is h (y_i + y_{i+1})/2 - h^3 (M_i + M_{i+1})/24
+// with M the second derivatives of the tridiagonal sweep.
+void spline_integral_weights(const double *x, int n, double *w) {
+  std::vector<double> h(n), cc(n), alpha(n), beta(n), gam(n, 0.0), Mbar(n, 0.0), bbar(n, 0.0), ddbar(n, 0.0);
+  for (int i = 0; i < n - 1; i++) h[i] = x[i + 1] - x[i];
+  // forward sweep coefficients (depend on x only): b_i = alpha_i dd_i + beta_i b_{i-1}, M_i = c_i M_{i+1} + b_i
+  cc[0] = -0.5;
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * cc[i - 1] + 2;
+    cc[i] = (sig - 1) / p;
+    alpha[i] = 6 / (x[i + 1] - x[i - 1]) / p;
+    beta[i] = -sig / p;
+  }
+  cc[n - 1] = 0;
+  for (int i = 0; i < n; i++) w[i] = 0;
+  for (int i = 0; i < n - 1; i++) {
+    w[i] += h[i] / 2;
+    w[i + 1] += h[i] / 2;
+    double g = -h[i] * h[i] * h[i] / 24;
+    gam[i] += g;
+    gam[i + 1] += g;
+  }
+  // adjoint of M_i = c_i M_{i+1} + b_i (computed for i = n-2 .. 0; M_{n-1} = 0)
+  for (int i = 0; i <= n - 2; i++) {
+    Mbar[i] += gam[i];
+    Mbar[i + 1] += cc[i] * Mbar[i];
+    bbar[i] += Mbar[i];
+  }
+  // adjoint of b_i = alpha_i dd_i + beta_i b_{i-1} (i = 1 .. n-2; b_0 = 0 because the first
+  // slope equals the first secant)
+  for (int i = n - 2; i >= 1; i--) {
+    ddbar[i] += alpha[i] * bbar[i];
+    bbar[i - 1] += beta[i] * bbar[i];
+  }
+  // adjoint of dd_i = (y_{i+1} - y_i)/h_i - (y_i - y_{i-1})/h_{i-1}
+  for (int i = 1; i <= n - 2; i++) {
+    w[i + 1] += ddbar[i] / h[i];
+    w[i] -= ddbar[i] / h[i] + ddbar[i] / h[i - 1];
+    w[i - 1] += ddbar[i] / h[i - 1];
+  }
+}
+
 double interp_log(double r, int n, const double *x, const double *f, double *const *s) {
   if (r > x[n - 1]) return 0;
   if (r < x[0]) return f[0];
@@ -72,247 +112,6 @@ double interp_log(double r, int n, const double *x, const double *f, double *con
   if (i > n - 2) i = n - 2;
   double t = r - x[i];
   return f[i] + t * (s[0][i] + t * (s[1][i] + t * s[2][i]));
-}
-
-static double **new_spline(const double *x, const double *y, int n) {
-  double **s = static_cast<double **>(std::malloc(3 * sizeof(double *)));
-  if (!s) throw std::bad_alloc();
-  for (int j = 0; j < 3; j++) {
-    s[j] = static_cast<double *>(std::malloc(sizeof(double) * n));
-    if (!s[j]) throw std::bad_alloc();
-  }
-  spline_coeffs(x, y, n, s[0], s[1], s[2]);
-  return s;
-}
-
-static double *dup(const double *src, int n) {
-  double *p = static_cast<double *>(std::malloc(sizeof(double) * (n > 0 ? n : 1)));
-  if (!p) throw std::bad_alloc();
-  for (int i = 0; i < n; i++) p[i] = src[i];
-  return p;
-}
-
-// ------------------------------------------------- 1D FFT for the transform
-
-// Mixed-radix Stockham transform with the exp(+i) sign of a DFTI backward
-// transform (unnormalised), for the 2N-point lengths of the Bessel transform.
-struct Fft1 {
-  int n;
-  std::vector<int> radix;
-  std::vector<cd> w;  // exp(+2 pi i m/n)
-  explicit Fft1(int len) : n(len), w(len) {
-    int m = len;
-    for (int q = 2; m > 1; q++)
-      while (m % q == 0) {
-        radix.push_back(q);
-        m /= q;
-      }
-    for (int i = 0; i < len; i++) {
-      double a = 2.0 * M_PI * i / len;
-      w[i] = cd(std::cos(a), std::sin(a));
-    }
-  }
-  void operator()(std::vector<cd> &x) const {
-    std::vector<cd> y(n), v(64), o(64);
-    cd *src = x.data(), *dst = y.data();
-    long span = 1;
-    for (int R : radix) {
-      long m = n / R;
-      for (long j = 0; j < m; j++) {
-        long k = j % span;
-        long tstep = n / (span * R);
-        for (int r = 0; r < R; r++) v[r] = src[j + r * m] * w[(k * r * tstep) % n];
-        for (int q = 0; q < R; q++) {
-          cd acc = 0;
-          for (int r = 0; r < R; r++) acc += v[r] * w[(long)((r * q) % R) * (n / R)];
-          o[q] = acc;
-        }
-        long base = (j / span) * span * R + k;
-        for (int q = 0; q < R; q++) dst[base + q * span] = o[q];
-      }
-      std::swap(src, dst);
-      span *= R;
-    }
-    if (src != x.data()) std::copy(src, src + n, x.begin());
-  }
-};
-
-// ---------------------------------------------- spherical Bessel transform
-
-struct Sbt {
-  int N, lmax;
-  std::vector<double> ks, rs;
-  std::vector<std::vector<cd>> M;
-  Fft1 fft;
-  // r: logarithmic grid of n points; encut sets the top of the k grid.
-  Sbt(double encut, int lmax_in, int n, const double *r)
-      : N(2 * n), lmax(lmax_in == 0 ? 1 : lmax_in), ks(2 * n), rs(2 * n), fft(2 * n) {
-    double drho = std::log(r[1] / r[0]);
-    double dt = 2 * M_PI / N / drho;
-    double kmin = std::pow(encut * kC, 0.5) * std::exp(-(N / 2 - 1) * drho);
-    double kappamin = std::log(kmin);
-    for (int i = 0; i < N; i++) {
-      ks[i] = kmin * std::exp(i * drho);
-      rs[i] = r[0] * std::exp((i - N / 2) * drho);
-    }
-    double rhomin = std::log(rs[0]);
-    M.assign(lmax + 1, std::vector<cd>(N));
-    for (int i = 0; i < N; i++) {
-      double t = i * dt;
-      // arg Gamma(1/2 + i t): shift by 10 then Stirling's series
-      double rad = std::sqrt(10.5 * 10.5 + t * t);
-      double ph = std::atan((2 * t) / 21);
-      double g = -10 * ph - t * std::log(rad) + t + std::sin(ph) / (12 * rad) -
-                 std::sin(3 * ph) / (360 * std::pow(rad, 3)) +
-                 std::sin(5 * ph) / (1260 * std::pow(rad, 5)) -
-                 std::sin(7 * ph) / (1680 * std::pow(rad, 7));
-      for (int j = 1; j <= 10; j++) g += std::atan((2 * t) / (2 * j - 1));
-      double h = -std::atan(std::tanh(M_PI * t / 2));
-      double phase = g + h + (kappamin + rhomin) * t;
-      cd m0 = std::sqrt(M_PI / 2) * std::exp(cd(0, phase)) / (double)N;
-      if (i == 0) m0 *= 0.5;
-      M[0][i] = m0;
-      M[1][i] = std::exp(cd(0, 2 * (-h - std::atan(2 * t)))) * m0;
-      for (int l = 1; l < lmax; l++)
-        M[l + 1][i] = std::exp(cd(0, 2 * -std::atan(2 * t / (2 * l + 1)))) * M[l - 1][i];
-    }
-  }
-  // transform of r*f given on the original grid (n points) -> n values on ks[0..n)
-  std::vector<double> forward(const double *f, int l) const {
-    int n = N / 2;
-    std::vector<cd> x(N);
-    double C = f[0] / std::pow(rs[n], l + 1);
-    for (int i = 0; i < N; i++) {
-      double fs = i < n ? C * std::pow(rs[i], l + 1) : f[i - n];
-      x[i] = std::pow(rs[i], 0.5) * fs;
-    }
-    fft(x);
-    for (int i = 0; i < N; i++) x[i] = i < n ? x[i] * M[l][i] : cd(0);
-    fft(x);
-    std::vector<double> out(n);
-    for (int p = 0; p < n; p++) out[p] = x[p].real() * 2 / std::pow(ks[p], 1.5);
-    return out;
-  }
-  // inverse of forward (roles of the two grids exchanged)
-  std::vector<double> inverse(const double *fk, int l) const {
-    int n = N / 2;
-    std::vector<cd> x(N);
-    for (int i = 0; i < N; i++) x[i] = i < n ? std::pow(ks[i], 1.5) * fk[i] : 0.0;
-    fft(x);
-    for (int i = 0; i < N; i++) x[i] = i < n ? x[i] * M[l][i] : cd(0);
-    fft(x);
-    std::vector<double> out(n);
-    for (int p = 0; p < n; p++) out[p] = x[p + n].real() / M_PI * 2 * 2 / std::pow(rs[p + n], 1.5);
-    return out;
-  }
-};
-
-// ------------------------------------------------------- element datasets
-
-ppot_t *build_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
-                             const double *projectors, const double *aewaves, const double *pswaves,
-                             const double *rmaxs, double grid_encut) {
-  PAWPY_REQUIRE(num_els > 0 && labels && ls && wave_grids && projectors && aewaves && pswaves && rmaxs,
-                "get_projector_list: missing input array");
-  ppot_t *pps = static_cast<ppot_t *>(std::calloc(num_els, sizeof(ppot_t)));
-  if (!pps) throw std::bad_alloc();
-  long wg_off = 0, p_off = 0, w_off = 0, l_off = 0;
-  try {
-    for (int e = 0; e < num_els; e++) {
-      ppot_t &pp = pps[e];
-      pp.num_projs = labels[4 * e + 1];
-      pp.proj_gridsize = labels[4 * e + 2];
-      pp.wave_gridsize = labels[4 * e + 3];
-      pp.rmax = rmaxs[e];
-      int nd = pp.proj_gridsize, ng = pp.wave_gridsize, np = pp.num_projs;
-      PAWPY_REQUIRE(nd >= 3 && ng >= 3 && np >= 1, "get_projector_list: bad element dimensions");
-      pp.wave_grid = dup(wave_grids + wg_off, ng);
-      wg_off += ng;
-      pp.kwave_grid = static_cast<double *>(std::calloc(ng, sizeof(double)));
-      pp.proj_grid = static_cast<double *>(std::malloc(sizeof(double) * nd));
-      pp.smooth_grid = static_cast<double *>(std::malloc(sizeof(double) * nd));
-      pp.funcs = static_cast<funcset_t *>(std::calloc(np, sizeof(funcset_t)));
-      if (!pp.kwave_grid || !pp.proj_grid || !pp.smooth_grid || !pp.funcs) throw std::bad_alloc();
-      for (int j = 0; j < nd; j++) pp.proj_grid[j] = pp.rmax / nd * j;
-      pp.wave_rmax = pp.wave_grid[ng - 1];
-      for (int j = 0; j < nd; j++) pp.smooth_grid[j] = pp.wave_rmax / nd * j;
-      // the reference rebuilds the log grid as a running product of its first ratio
-      std::vector<double> dense(ng);
-      dense[0] = pp.wave_grid[0];
-      double ratio = std::pow(pp.wave_grid[1] / pp.wave_grid[0], 1.0);
-      for (int i = 1; i < ng; i++) dense[i] = dense[i - 1] * ratio;
-      pp.lmax = 0;
-      pp.total_projs = 0;
-      for (int k = 0; k < np; k++) {
-        funcset_t &f = pp.funcs[k];
-        f.l = ls[l_off++];
-        if (f.l > pp.lmax) pp.lmax = f.l;
-        pp.total_projs += 2 * f.l + 1;
-        f.aewave = dup(aewaves + w_off, ng);
-        f.pswave = dup(pswaves + w_off, ng);
-        f.diffwave = static_cast<double *>(std::malloc(sizeof(double) * ng));
-        if (!f.diffwave) throw std::bad_alloc();
-        for (int i = 0; i < ng; i++) f.diffwave[i] = f.aewave[i] - f.pswave[i];
-        w_off += ng;
-        f.proj = dup(projectors + p_off, nd);
-        p_off += nd;
-        f.proj_spline = new_spline(pp.proj_grid, f.proj, nd);
-        f.aewave_spline = new_spline(pp.wave_grid, f.aewave, ng);
-        f.pswave_spline = new_spline(pp.wave_grid, f.pswave, ng);
-        f.diffwave_spline = new_spline(pp.wave_grid, f.diffwave, ng);
-      }
-      Sbt sbt(1e7, pp.lmax, ng, pp.wave_grid);
-      for (int i = 0; i < ng; i++) pp.kwave_grid[i] = sbt.ks[i];
-      double kcut = std::pow(kC * grid_encut, 0.5);
-      for (int k = 0; k < np; k++) {
-        funcset_t &f = pp.funcs[k];
-        std::vector<double> kw = sbt.forward(f.diffwave, f.l);
-        f.kwave = dup(kw.data(), ng);
-        f.kwave_spline = new_spline(pp.kwave_grid, f.kwave, ng);
-        // drop every k at or above sqrt(c * grid_encut), transform back
-        std::vector<double> lowk(ng, 0.0);
-        for (int q = 0; q < ng && pp.kwave_grid[q] < kcut; q++) lowk[q] = f.kwave[q];
-        std::vector<double> sm = sbt.inverse(lowk.data(), f.l);
-        double **ss = new_spline(dense.data(), sm.data(), ng);
-        double *sdw = static_cast<double *>(std::malloc(sizeof(double) * nd));
-        if (!sdw) throw std::bad_alloc();
-        for (int p = 1; p < nd; p++) sdw[p] = interp_log(pp.smooth_grid[p], ng, dense.data(), sm.data(), ss);
-        sdw[0] = f.l > 0 ? 0.0 : sdw[1];
-        for (int j = 0; j < 3; j++) std::free(ss[j]);
-        std::free(ss);
-        f.smooth_diffwave = sdw;
-        f.smooth_diffwave_spline = new_spline(pp.smooth_grid, sdw, nd);
-      }
-      // partial-wave overlap integrals between channels of equal l
-      pp.pspw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      pp.aepw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      pp.diff_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      if (!pp.pspw_overlap_matrix || !pp.aepw_overlap_matrix || !pp.diff_overlap_matrix)
-        throw std::bad_alloc();
-      std::vector<double> prod(ng), sb(ng), sc(ng), sd(ng);
-      for (int i = 0; i < np; i++)
-        for (int j = i; j < np; j++) {
-          if (pp.funcs[i].l != pp.funcs[j].l) continue;
-          const funcset_t &a = pp.funcs[i], &b = pp.funcs[j];
-          double *mats[3] = {pp.pspw_overlap_matrix, pp.aepw_overlap_matrix, pp.diff_overlap_matrix};
-          for (int which = 0; which < 3; which++) {
-            for (int q = 0; q < ng; q++) {
-              if (which == 0) prod[q] = a.pswave[q] * b.pswave[q];
-              else if (which == 1) prod[q] = a.aewave[q] * b.aewave[q];
-              else prod[q] = (a.aewave[q] - a.pswave[q]) * (b.aewave[q] - b.pswave[q]);
-            }
-            spline_coeffs(pp.wave_grid, prod.data(), ng, sb.data(), sc.data(), sd.data());
-            double v = spline_integral(pp.wave_grid, prod.data(), sb.data(), sc.data(), sd.data(), ng);
-            mats[which][i * np + j] = v;
-            mats[which][j * np + i] = v;
-          }
-        }
-    }
-  } catch (...) {
-    free_ppot_array(pps, num_els);
-    throw;
-  }
-  return pps;
 }
 
 // ---------------------------------------------------- off-site pair matrix
@@ -375,70 +174,104 @@ static double bessel_fac(int lx, int ly, int L, int mx, int my) {
          std::sqrt((2 * lx + 1) * (2 * ly + 1) * (2 * L + 1) / 4.0 / M_PI);
 }
 
-static cd offsite_one(const double *dc, const ppot_t *p1, int f1, const ppot_t *p2, int f2, int l1,
-                      int m1, int l2, int m2) {
-  int lx = l1, ly = l2, mx = m1, my = m2;
-  if (l1 < l2) {
-    lx = l2;
-    ly = l1;
-    mx = m2;
-    my = m1;
+// |d| and the angles of the pair displacement, as radial.c:146-160
+static void pair_geometry(const double *dc, double *R, double *th, double *ph) {
+  *R = std::pow(dc[0] * dc[0] + dc[1] * dc[1] + dc[2] * dc[2], 0.5);
+  *th = 0;
+  *ph = 0;
+  if (*R < 10e-12) {
+    *R = 0;
+    return;
   }
-  if (my < 0) {
-    mx = -mx;
-    my = -my;
-  }
-  const double *k1 = p1->kwave_grid, *k2 = p2->kwave_grid;
-  int n1 = p1->wave_gridsize, n2 = p2->wave_gridsize;
-  double kmax = std::min(k1[n1 - 1], k2[n2 - 1]);
-  double kmin = std::max(k1[0], k2[0]);
-  double R = std::pow(dc[0] * dc[0] + dc[1] * dc[1] + dc[2] * dc[2], 0.5), th = 0, ph = 0;
-  if (R < 10e-12) {
-    R = 0;
-  } else {
-    th = std::acos(dc[2] / R);
-    ph = R - std::fabs(dc[2]) < 10e-12 ? 0 : std::acos(dc[0] / std::pow(dc[0] * dc[0] + dc[1] * dc[1], 0.5));
-    if (dc[1] < 0) ph = 2 * M_PI - ph;
-  }
-  const int K = 500;
-  std::vector<double> kg(K), fn(K), b(K), c(K), d(K);
-  cd total = 0;
-  double sign = std::pow(-1, m1) * 8;
-  int lo = std::abs(l1 - l2);
-  for (int L = lo; L <= l1 + l2; L += 2) {
-    for (int q = 0; q < K; q++) {
-      kg[q] = kmin * std::pow(kmax / kmin, (double)q / K);
-      double kk = kg[q];
-      fn[q] = interp_log(kk, n1, k1, p1->funcs[f1].kwave, p1->funcs[f1].kwave_spline) *
-              interp_log(kk, n2, k2, p2->funcs[f2].kwave, p2->funcs[f2].kwave_spline) * kk * kk *
-              bessel_up(kk * R, L);
-    }
-    spline_coeffs(kg.data(), fn.data(), K, b.data(), c.data(), d.data());
-    double integ = spline_integral(kg.data(), fn.data(), b.data(), c.data(), d.data(), K);
-    if (R > 10e-10) {
-      static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
-      total += integ * bessel_fac(lx, ly, L, mx, my) * ylm(L, m1 - m2, th, ph) *
-               ipow[((l2 + L - l1) % 4 + 4) % 4] * sign;
-    } else if (L == 0 && l1 == l2 && m1 == m2) {
-      total += integ * 2 / M_PI;
-    }
-  }
-  return total;
+  *th = std::acos(dc[2] / *R);
+  *ph = *R - std::fabs(dc[2]) < 10e-12 ? 0 : std::acos(dc[0] / std::pow(dc[0] * dc[0] + dc[1] * dc[1], 0.5));
+  if (dc[1] < 0) *ph = 2 * M_PI - *ph;
 }
 
-void offsite_pair_matrix(const ppot_t *p1, const ppot_t *p2, const double *dcoord, pawpy_c128 *out) {
+double pair_distance(const double *dcoord) {
+  double R, th, ph;
+  pair_geometry(dcoord, &R, &th, &ph);
+  return R;
+}
+
+void offsite_pair_matrix(const ppot_t *p1, const ppot_t *p2, const double *dcoord, const double *I, int Lmax,
+                         pawpy_c128 *out) {
+  double R, th, ph;
+  pair_geometry(dcoord, &R, &th, &ph);
+  static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+  int nf2 = p2->num_projs;
   int t1 = 0;
-  for (int j = 0; j < p1->num_projs; j++) {
-    int l1 = p1->funcs[j].l;
+  for (int f1 = 0; f1 < p1->num_projs; f1++) {
+    int l1 = p1->funcs[f1].l;
     for (int m1 = -l1; m1 <= l1; m1++, t1++) {
       int t2 = 0;
-      for (int k = 0; k < p2->num_projs; k++) {
-        int l2 = p2->funcs[k].l;
-        for (int m2 = -l2; m2 <= l2; m2++, t2++)
-          out[(long)t1 * p2->total_projs + t2] = std::conj(offsite_one(dcoord, p1, j, p2, k, l1, m1, l2, m2));
+      for (int f2 = 0; f2 < nf2; f2++) {
+        int l2 = p2->funcs[f2].l;
+        for (int m2 = -l2; m2 <= l2; m2++, t2++) {
+          int lx = l1, ly = l2, mx = m1, my = m2;
+          if (l1 < l2) {
+            lx = l2;
+            ly = l1;
+            mx = m2;
+            my = m1;
+          }
+          if (my < 0) {
+            mx = -mx;
+            my = -my;
+          }
+          cd total = 0;
+          double sign = std::pow(-1, m1) * 8;
+          int lo = std::abs(l1 - l2);
+          for (int L = lo; L <= l1 + l2; L += 2) {
+            double integ = I[((long)f1 * nf2 + f2) * (Lmax + 1) + L];
+            if (R > 10e-10)
+              total += integ * bessel_fac(lx, ly, L, mx, my) * ylm(L, m1 - m2, th, ph) *
+                       ipow[((l2 + L - l1) % 4 + 4) % 4] * sign;
+            else if (L == 0 && l1 == l2 && m1 == m2)
+              total += integ * 2 / M_PI;
+          }
+          out[(long)t1 * p2->total_projs + t2] = std::conj(total);
+        }
       }
     }
   }
+}
+
+// Upper bound on the grid points inside an element's largest sphere, as
+// add_num_cart_gridpts (projector.c:455-505) computes it for ppot_t.num_cart_gridpts.
+int cart_gridpts_bound(const ppot_t &pp, const double *lat, const int *fftg) {
+  auto dot = [](const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  auto mag = [&](const double *a) { return std::pow(dot(a, a), 0.5); };
+  auto cross = [](const double *a, const double *b, double *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  double m1 = mag(lat), m2 = mag(lat + 3), m3 = mag(lat + 6), v[3];
+  double rmax = pp.rmax;
+  if (pp.wave_grid[pp.wave_gridsize - 1] > rmax) rmax = pp.wave_grid[pp.wave_gridsize - 1];
+  double p12 = std::acos(dot(lat, lat + 3) / (m1 * m2));
+  cross(lat, lat + 3, v);
+  double s = dot(lat + 6, v) / (mag(v) * m3);
+  double a1 = rmax * fftg[0] / (m1 * std::fabs(std::sin(p12))) + 1;
+  double a2 = rmax * fftg[1] / (m2 * std::fabs(std::sin(p12))) + 1;
+  double a3 = rmax * fftg[2] / (m3 * std::fabs(s)) + 1;
+  int nA = (int)(4.0 / 3.0 * M_PI * a1 * a2 * a3) + 1;
+  double p13 = std::acos(dot(lat, lat + 6) / (m1 * m3));
+  cross(lat, lat + 6, v);
+  s = dot(lat + 3, v) / (mag(v) * m2);
+  double b1 = rmax * fftg[0] / (m1 * std::fabs(std::sin(p13))) + 1;
+  double b2 = rmax * fftg[1] / (m2 * std::fabs(s)) + 1;
+  double b3 = rmax * fftg[2] / (m3 * std::fabs(std::sin(p13))) + 1;
+  int nB = (int)(4.0 / 3.0 * M_PI * b1 * b2 * b3) + 1;
+  double p23 = std::acos(dot(lat + 3, lat + 6) / (m2 * m3));
+  cross(lat + 3, lat + 6, v);
+  s = dot(lat, v) / (mag(v) * m1);
+  double c1 = rmax * fftg[0] / (m1 * std::fabs(s)) + 1;
+  double c2 = rmax * fftg[1] / (m2 * std::fabs(std::sin(p23))) + 1;
+  double c3 = rmax * fftg[2] / (m3 * std::fabs(std::sin(p23))) + 1;
+  int nC = (int)(4.0 / 3.0 * M_PI * c1 * c2 * c3) + 1;
+  return std::max(nA, std::max(nB, nC));
 }
 
 void min_image_path(const double *coord, const double *center, const double *L, double *path, double *r) {

@@ -52,6 +52,37 @@ def test_fft3d_known_answer(golden):
     assert np.abs(x - g["ref"]).max() <= 1e-5
 
 
+def test_projector_list_matches_oracle():
+    """get_projector_list (device FP64) against the oracle's element setup."""
+    import oracle as orc
+
+    from pawpyseed_gb300 import _lib, synth, vaspio
+    from pawpyseed_gb300.wavefunction import pack_species
+
+    cr = vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
+    labels, ls, wg, pr, ae, ps, rm = pack_species(cr)
+    L = _lib.lib()
+    for ge in (640.0, 1150.0):
+        pps = L.get_projector_list(2, labels, ls, wg, pr, ae, ps, rm, ge)
+        _lib.check()
+        for e, sym in enumerate(cr.pps):
+            o = orc.OSpecies(cr.pps[sym], ge)
+            pp = pps[e]
+            nd, ng = pp.proj_gridsize, pp.wave_gridsize
+            assert pp.total_projs == o.total and pp.num_projs == o.nproj
+            for k in range(pp.num_projs):
+                f = pp.funcs[k]
+                sdw = np.ctypeslib.as_array(f.smooth_diffwave, shape=(nd,))
+                kw = np.ctypeslib.as_array(f.kwave, shape=(ng,))
+                # FP64 round-off of two 800-point transforms (device twiddles vs the oracle's)
+                assert np.allclose(sdw, o.sdw[k * nd:(k + 1) * nd], rtol=0, atol=1e-10 * np.abs(sdw).max())
+                assert np.allclose(kw, o.kwave[k * ng:(k + 1) * ng], rtol=0, atol=1e-10 * np.abs(kw).max())
+            n = pp.num_projs
+            aeov = np.ctypeslib.as_array(pp.aepw_overlap_matrix, shape=(n * n,))
+            psov = np.ctypeslib.as_array(pp.pspw_overlap_matrix, shape=(n * n,))
+            assert np.allclose(aeov, o.aeov, atol=1e-13) and np.allclose(psov, o.psov, atol=1e-13)
+
+
 @pytest.mark.parametrize("name", ["cfg0", "cfg1s"])
 def test_projector_coefficients(name, workload_dirs, oracle_projectors, golden):
     basis, wf = load(workload_dirs(name))

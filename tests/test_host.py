@@ -88,36 +88,6 @@ def test_reader_errors_are_reported_not_fatal(tmp_path):
     L.pawpy_gpu_clear_error()
 
 
-def test_projector_list_matches_oracle():
-    """get_projector_list (host FP64) against the oracle's element setup."""
-    import oracle as orc
-
-    from pawpyseed_gb300 import _lib, synth, vaspio
-    from pawpyseed_gb300.wavefunction import pack_species
-
-    cr = vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
-    labels, ls, wg, pr, ae, ps, rm = pack_species(cr)
-    L = _lib.lib()
-    for ge in (640.0, 1150.0):
-        pps = L.get_projector_list(2, labels, ls, wg, pr, ae, ps, rm, ge)
-        _lib.check()
-        for e, sym in enumerate(cr.pps):
-            o = orc.OSpecies(cr.pps[sym], ge)
-            pp = pps[e]
-            nd, ng = pp.proj_gridsize, pp.wave_gridsize
-            assert pp.total_projs == o.total and pp.num_projs == o.nproj
-            for k in range(pp.num_projs):
-                f = pp.funcs[k]
-                sdw = np.ctypeslib.as_array(f.smooth_diffwave, shape=(nd,))
-                kw = np.ctypeslib.as_array(f.kwave, shape=(ng,))
-                assert np.allclose(sdw, o.sdw[k * nd:(k + 1) * nd], rtol=0, atol=1e-12 * np.abs(sdw).max())
-                assert np.allclose(kw, o.kwave[k * ng:(k + 1) * ng], rtol=0, atol=1e-12 * np.abs(kw).max())
-            n = pp.num_projs
-            aeov = np.ctypeslib.as_array(pp.aepw_overlap_matrix, shape=(n * n,))
-            psov = np.ctypeslib.as_array(pp.pspw_overlap_matrix, shape=(n * n,))
-            assert np.allclose(aeov, o.aeov, atol=1e-13) and np.allclose(psov, o.psov, atol=1e-13)
-
-
 def test_potcar_parser_reads_generated_dataset():
     from pawpyseed_gb300 import synth, vaspio
 
