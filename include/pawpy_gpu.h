@@ -242,6 +242,19 @@ void pawpy_gpu_clear_error(void);
 /* Overlap precision for the device overlap matrices (default FP32). */
 void pawpy_gpu_set_precision(int precision);
 int pawpy_gpu_get_precision(void);
+/* K split of the tensor-core overlap contraction (0 = chosen from the SM
+ * count, the default). No counterpart in the reference. */
+void pawpy_gpu_set_tc_splits(int splits);
+
+/* Batched overlap matrices of host arrays, no counterpart in the reference
+ * (pseudoprojection's contraction, pseudoprojector.c:63-90, on raw matrices):
+ * for z < nz, out[z][n][m] = sum_k conj(A_z[m][k]) B_z[n][k] with A_z of
+ * M x K[z] and B_z of N x K[z], each row-major and packed one batch after
+ * the other; out is nz x N x M. precision is a pawpy_gpu_precision. Returns
+ * 0, or -1 with the status set. */
+int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
+                             pawpy_c64 *out, int precision);
+
 /* Whether setup_projections / overlap_setup_real also fill the host
  * projection_t arrays (default 1, as the reference). */
 void pawpy_gpu_set_host_projections(int on);

@@ -20,6 +20,7 @@ _lib = None
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _zp = np.ctypeslib.ndpointer(dtype=np.complex128, flags="C_CONTIGUOUS")
+_cp = np.ctypeslib.ndpointer(dtype=np.complex64, flags="C_CONTIGUOUS")
 _wfp = C.POINTER(S.pswf_t)
 _ppp = C.POINTER(S.ppot_t)
 _vp = C.c_void_p
@@ -64,6 +65,9 @@ def _declare(L):
                                  _vp, _dp, _dp, C.c_int, _ip]
     L.pawpy_gpu_set_precision.argtypes = [C.c_int]
     L.pawpy_gpu_get_precision.restype = C.c_int
+    L.pawpy_gpu_set_tc_splits.argtypes = [C.c_int]
+    L.pawpy_gpu_overlap_matrix.restype = C.c_int
+    L.pawpy_gpu_overlap_matrix.argtypes = [_cp, _cp, C.c_int, C.c_int, C.c_int, _ip, _cp, C.c_int]
     L.pawpy_gpu_set_host_projections.argtypes = [C.c_int]
     L.pawpy_gpu_timer_stop_ms.restype = C.c_float
     L.pawpy_gpu_launch_count.restype = C.c_longlong
@@ -112,6 +116,23 @@ def set_precision(name):
 def get_precision():
     v = lib().pawpy_gpu_get_precision()
     return {b: a for a, b in PRECISIONS.items()}[v]
+
+
+def overlap_matrix(As, Bs, precision="fp32"):
+    """out[z] = conj(As[z]) @ Bs[z].T for lists of complex64 matrices that
+    share their row counts (M and N) and may differ in K; returns nz x N x M
+    complex64 (out[z][n][m] = <A_z[m] | B_z[n]>)."""
+    M, N, nz = As[0].shape[0], Bs[0].shape[0], len(As)
+    K = np.array([a.shape[1] for a in As], np.int32)
+    for a, b in zip(As, Bs):
+        if a.shape[0] != M or b.shape[0] != N or a.shape[1] != b.shape[1]:
+            raise ValueError("overlap_matrix: inconsistent shapes")
+    A = np.ascontiguousarray(np.concatenate([np.ascontiguousarray(a, np.complex64).ravel() for a in As]))
+    B = np.ascontiguousarray(np.concatenate([np.ascontiguousarray(b, np.complex64).ravel() for b in Bs]))
+    out = np.zeros((nz, N, M), np.complex64)
+    lib().pawpy_gpu_overlap_matrix(A, B, M, N, nz, K, out, PRECISIONS[precision])
+    check()
+    return out
 
 
 def kernel_stats(reset=True):

@@ -124,6 +124,7 @@ static std::recursive_mutex g_mu;
 static std::map<const pswf_t *, std::unique_ptr<DevWF>> g_wfs;
 static std::map<std::pair<const pswf_t *, const pswf_t *>, std::unique_ptr<PairState>> g_pairs;
 static int g_precision = PAWPY_GPU_FP32;
+static int g_tc_splits = 0;  // K split of the tensor-core contraction, 0 = from the SM count
 static bool g_host_proj = true;
 
 void release_device(pswf_t *wf) {
@@ -892,6 +893,10 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   }
   DevBuf<GemmBatch> db(nk);
   db.upload(hb.data(), nk);
+  if (g_precision == PAWPY_GPU_BF16X3 || g_precision == PAWPY_GPU_TF32) {
+    launch_zgemm_tc(db.p, hb, R.nband, S.nband, g_precision == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+    return;
+  }
   int splits = choose_splits(R.nband, S.nband, nk, maxK);
   DevBuf<float2> ws;
   if (splits > 1) ws.alloc((size_t)splits * nk * S.nband * R.nband);
@@ -1054,6 +1059,70 @@ void pawpy_gpu_set_precision(int precision) {
     g_precision = precision;
 }
 int pawpy_gpu_get_precision(void) { return g_precision; }
+void pawpy_gpu_set_tc_splits(int splits) { g_tc_splits = splits < 0 ? 0 : splits; }
+
+int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
+                             pawpy_c64 *out, int precision) {
+  PAWPY_API_BEGIN
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  PAWPY_REQUIRE(A && B && K && out, "pawpy_gpu_overlap_matrix: NULL argument");
+  PAWPY_REQUIRE(M > 0 && N > 0 && nz > 0, "pawpy_gpu_overlap_matrix: empty shape");
+  PAWPY_REQUIRE(precision == PAWPY_GPU_FP32 || precision == PAWPY_GPU_BF16X3 || precision == PAWPY_GPU_TF32,
+                "pawpy_gpu_overlap_matrix: unknown precision");
+  // rows padded to a multiple of 16 elements with zeros (the GEMM's K granule)
+  std::vector<size_t> offA(nz), offB(nz);
+  std::vector<int> Kp(nz);
+  size_t na = 0, nb = 0;
+  int maxK = 0;
+  for (int z = 0; z < nz; z++) {
+    PAWPY_REQUIRE(K[z] >= 0, "pawpy_gpu_overlap_matrix: negative K");
+    Kp[z] = std::max(16, (K[z] + 15) / 16 * 16);
+    offA[z] = na;
+    offB[z] = nb;
+    na += (size_t)M * Kp[z];
+    nb += (size_t)N * Kp[z];
+    maxK = std::max(maxK, Kp[z]);
+  }
+  DevBuf<float2> dA(na), dB(nb), dO((size_t)nz * N * M);
+  dA.zero();
+  dB.zero();
+  const float2 *hA = reinterpret_cast<const float2 *>(A), *hB = reinterpret_cast<const float2 *>(B);
+  size_t ia = 0, ib = 0;
+  std::vector<GemmBatch> hb(nz);
+  for (int z = 0; z < nz; z++) {
+    if (K[z] > 0) {
+      PAWPY_CUDA(cudaMemcpy2DAsync(dA.p + offA[z], Kp[z] * sizeof(float2), hA + ia, K[z] * sizeof(float2),
+                                   K[z] * sizeof(float2), M, cudaMemcpyHostToDevice, stream()));
+      PAWPY_CUDA(cudaMemcpy2DAsync(dB.p + offB[z], Kp[z] * sizeof(float2), hB + ib, K[z] * sizeof(float2),
+                                   K[z] * sizeof(float2), N, cudaMemcpyHostToDevice, stream()));
+    }
+    ia += (size_t)M * K[z];
+    ib += (size_t)N * K[z];
+    GemmBatch &g = hb[z];
+    g.A1 = dA.p + offA[z];
+    g.B1 = dB.p + offB[z];
+    g.A2 = g.B2 = nullptr;
+    g.lda1 = g.ldb1 = Kp[z];
+    g.lda2 = g.ldb2 = 0;
+    g.K1 = Kp[z];
+    g.K2 = 0;
+    g.out = dO.p + (size_t)z * N * M;
+  }
+  DevBuf<GemmBatch> db(nz);
+  db.upload(hb.data(), nz);
+  if (precision == PAWPY_GPU_FP32) {
+    int splits = choose_splits(M, N, nz, maxK);
+    DevBuf<float2> ws;
+    if (splits > 1) ws.alloc((size_t)splits * nz * N * M);
+    launch_zgemm_f32(db.p, nz, M, N, splits, ws.p);
+  } else {
+    launch_zgemm_tc(db.p, hb, M, N, precision == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+  }
+  dO.download(reinterpret_cast<float2 *>(out), dO.n);
+  sync();
+  return 0;
+  PAWPY_API_END(-1)
+}
 void pawpy_gpu_set_host_projections(int on) { g_host_proj = on != 0; }
 
 void pawpy_gpu_release(pswf_t *wf) {

@@ -109,6 +109,15 @@ struct GemmBatch {
 // One grouped launch over nz batches (uneven K allowed). splits > 1 needs a
 // workspace of splits*nz*N*M float2 and reduces in split order.
 void launch_zgemm_f32(const GemmBatch *batches_dev, int nz, int M, int N, int splits, float2 *workspace);
+// The same grouped contraction on the tensor cores (tc_gemm.cu): split-BF16
+// 3-term (tf32 false) or TF32 operands, FP32 accumulation. hb is the host copy
+// of batches_dev. splits_hint <= 0 picks the K split from the SM count.
+// Synchronises and throws if a pipeline wait of the kernel ran out.
+struct TcGemmInfo {
+  int splits = 0, Kc = 0, ctas = 0;
+};
+void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
+                     int splits_hint, TcGemmInfo *info);
 // The two kernels behind launch_zgemm_f32 (64x64 tiles, 256 threads; grid (M/64, N/64, nz*splits)
 // and (M*N/1024, nz)), for callers that launch them on their own stream.
 __global__ void __launch_bounds__(256) k_zgemm_f32(const GemmBatch *batches, int M, int N, int splits,

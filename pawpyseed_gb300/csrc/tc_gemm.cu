@@ -1,0 +1,535 @@
+// Overlap contraction on the 5th-generation tensor cores: the split-BF16
+// (3-term) and TF32 forms of pseudoprojection (pseudoprojector.c:63-90)
+// batched over every band pair and k-point, plus the augmentation columns of
+// the PAW terms appended to K.
+//
+//   out[z][n][m] = sum_k conj(A[m][k]) B[n][k]
+//               = sum_k (ar br + ai bi) + i (ar bi - ai br)
+//
+// Operands are first split into planes, each K-major with K contiguous:
+//   split-BF16: hi_re, hi_im, lo_re, lo_im with x = hi + lo, hi = bf16(x),
+//               lo = bf16(x - hi); products hi*hi + hi*lo + lo*hi (lo*lo,
+//               about 2^-18 of |a||b|, is dropped), FP32 accumulation;
+//   TF32:       re, im in FP32 read as TF32 by the tensor core.
+// One CTA computes a 128 (basis bands) x 128 (defect bands) tile of one
+// k-point over a K range (split-K). A single thread issues TMA copies of
+// 64-byte-wide K blocks (64-byte swizzle) into a ring of shared-memory stages,
+// a second issues tcgen05.mma from them into TMEM, and eight warps drain the
+// accumulators into registers (see k_tc_zgemm). Partial sums over K ranges
+// are reduced in a fixed order by k_split_reduce, so results do not depend on
+// scheduling.
+//
+// Every mbarrier wait is bounded (kWaitNs); a wait that runs out records a
+// status word, stops issuing work, waits (bounded) for the copies and MMAs
+// already issued, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace pawpy {
+
+namespace {
+
+constexpr int TM = 128;          // basis bands per tile (TMEM lanes)
+constexpr int TN = 128;          // defect bands per tile (TMEM columns per accumulator)
+constexpr int ROWB = 64;         // bytes of one K block row (64-byte swizzle span)
+constexpr int DRAIN_WARPS = 8;   // warps 2..9
+constexpr int NTHREADS = 32 * (2 + DRAIN_WARPS);
+constexpr int TMEM_COLS = 4 * TN;  // two sets of (re, im)
+constexpr int FLUSH = 4;         // K blocks per accumulation interval
+constexpr unsigned long long kWaitNs = 4000000000ull;
+
+template <bool TF32>
+struct Prec {
+  static constexpr int NPL = TF32 ? 2 : 4;            // planes per operand
+  static constexpr int ESZ = TF32 ? 4 : 2;            // bytes per element
+  static constexpr int KB = ROWB / ESZ;               // elements per K block
+  static constexpr int KSTEPS = 2;                    // 32-byte MMA K steps per block
+  static constexpr int A_PLANE = TM * ROWB;           // 8 KB
+  static constexpr int B_PLANE = TN * ROWB;           // 8 KB
+  static constexpr int STAGE = NPL * (A_PLANE + B_PLANE);
+  static constexpr int STAGES = TF32 ? 6 : 3;
+  static constexpr int SMEM = STAGES * STAGE + 1024;  // + alignment slack
+  static constexpr int NTERMS = TF32 ? 4 : 12;
+};
+
+// Products of one K step: A plane | B plane << 4 | accumulator (0 re, 1 im)
+// << 8 | negate A << 12. Split-BF16 planes are 0 hi_re, 1 hi_im, 2 lo_re,
+// 3 lo_im; TF32 planes 0 re, 1 im.
+template <bool TF32>
+__host__ __device__ constexpr uint32_t term(int t) {
+  constexpr uint32_t bf16[12] = {0x0000, 0x0020, 0x0002, 0x0011, 0x0031, 0x0013,
+                                 0x0110, 0x0130, 0x0112, 0x1101, 0x1121, 0x1103};
+  constexpr uint32_t tf32[4] = {0x0000, 0x0011, 0x0110, 0x1101};
+  return TF32 ? tf32[t & 3] : bf16[t];
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the completion of the phase with the given parity; false after
+// kWaitNs, or as soon as *abort is set when abort is given.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort = nullptr) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (globaltimer() - t0 > kWaitNs) return false;
+    if (abort && *abort) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 64-byte rows in the
+// 64-byte swizzle layout: 8-row groups 512 bytes apart, descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+  uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>(1) << 16;           // leading byte offset (unused when swizzled)
+  d |= static_cast<uint64_t>(512 >> 4) << 32;    // stride byte offset
+  d |= static_cast<uint64_t>(1) << 46;           // version
+  d |= static_cast<uint64_t>(4) << 61;           // 64-byte swizzle
+  return d;
+}
+
+// Instruction descriptor of kind::f16 (BF16 inputs) or kind::tf32, FP32
+// accumulation, both operands K-major, M = 128, N = 256.
+__host__ __device__ constexpr uint32_t idesc(bool tf32, bool negA) {
+  return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) | ((negA ? 1u : 0u) << 13) |
+         (static_cast<uint32_t>(TN >> 3) << 17) | (static_cast<uint32_t>(TM >> 4) << 24);
+}
+
+template <bool TF32>
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t id, uint32_t acc) {
+  if constexpr (TF32)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(id), "r"(acc));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+}  // namespace
+
+// grid (M tiles, N tiles, nz * splits), NTHREADS threads. kblocks[z]: K
+// blocks of batch z (zero-filled beyond its K); the planes are
+// [plane][z][rows_pad][Kc].
+//
+// Warp 0 issues the TMA copies, warp 1 the MMAs; warps 2..9 drain the
+// accumulators. The MMAs of FLUSH consecutive K blocks go into one of two TMEM
+// accumulator sets (re and im, 128 columns each), starting from zero; the
+// drain warps then add that set to FP32 running sums in registers (rounded to
+// nearest) while the MMAs fill the other set. The tensor core truncates its
+// FP32 accumulator at every instruction, an error biased towards zero that
+// grows with the magnitude it accumulates; draining keeps that magnitude to a
+// few K blocks, so the bias stays near 6 FLUSH 2^-24 |S| whatever K is.
+template <bool TF32>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_tc_zgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               const GemmBatch *__restrict__ batches, const int *__restrict__ kblocks, int M, int N, int Mpad,
+               int Npad, int nz, int splits, float2 *__restrict__ ws, int *__restrict__ status) {
+  using P = Prec<TF32>;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar_full[P::STAGES], bar_empty[P::STAGES];
+  __shared__ __align__(8) unsigned long long bar_accf[2], bar_acce[2], bar_drain;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int z = blockIdx.z / splits, sp = blockIdx.z % splits;
+  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+  const int nkb = kblocks[z];
+  const int kb0 = (int)((long long)nkb * sp / splits), kb1 = (int)((long long)nkb * (sp + 1) / splits);
+  const int nloc = kb1 - kb0;
+  const int nq = (nloc + FLUSH - 1) / FLUSH;  // accumulation intervals
+
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < P::STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    for (int s = 0; s < 2; s++) {
+      mbar_init(smem_u32(&bar_accf[s]), 1);
+      mbar_init(smem_u32(&bar_acce[s]), DRAIN_WARPS);
+    }
+    mbar_init(smem_u32(&bar_drain), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  auto fail = [&](int code) {
+    abort_flag = 1;
+    atomicExch(status, code);
+  };
+
+  if (warp == 0) {
+    if (lane == 0 && nloc > 0) {
+      // TMA producer
+      const int rowsA = nz * Mpad, rowsB = nz * Npad;
+      int last_round[P::STAGES];
+#pragma unroll
+      for (int s = 0; s < P::STAGES; s++) last_round[s] = -1;
+      for (int i = 0; i < nloc; i++) {
+        const int s = i % P::STAGES, r = i / P::STAGES;
+        if (r > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (r - 1) & 1)) {
+          fail(1);
+          break;
+        }
+        if (abort_flag) break;
+        const uint32_t full = smem_u32(&bar_full[s]);
+        const uint32_t st = sbase + s * P::STAGE;
+        mbar_expect_tx(full, P::STAGE);
+        const int x = (kb0 + i) * P::KB;
+#pragma unroll
+        for (int p = 0; p < P::NPL; p++) {
+          tma_load_2d(st + p * P::A_PLANE, &tmA, full, x, p * rowsA + z * Mpad + m0);
+          tma_load_2d(st + P::NPL * P::A_PLANE + p * P::B_PLANE, &tmB, full, x, p * rowsB + z * Npad + n0);
+        }
+        last_round[s] = r;
+      }
+      if (abort_flag) {
+        // let the copies already issued land before the CTA's memory is released
+        for (int s = 0; s < P::STAGES; s++)
+          if (last_round[s] >= 0) mbar_wait(smem_u32(&bar_full[s]), last_round[s] & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t id_pos = idesc(TF32, false), id_neg = idesc(TF32, true);
+      int i = 0;
+      bool stop = false;
+      for (int q = 0; q < nq && !stop; q++) {
+        const int set = q & 1, u = q >> 1;
+        if (u > 0 && !mbar_wait(smem_u32(&bar_acce[set]), (u - 1) & 1)) {
+          fail(2);
+          break;
+        }
+        const uint32_t dset = tmem + set * (2 * TN);
+        bool first[2] = {true, true};
+        const int iend = min(nloc, (q + 1) * FLUSH);
+        for (; i < iend; i++) {
+          const int s = i % P::STAGES, r = i / P::STAGES;
+          if (!mbar_wait(smem_u32(&bar_full[s]), r & 1)) {
+            fail(3);
+            stop = true;
+            break;
+          }
+          if (abort_flag) {
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = sbase + s * P::STAGE;
+#pragma unroll
+          for (int j = 0; j < P::KSTEPS; j++) {
+#pragma unroll
+            for (int t = 0; t < P::NTERMS; t++) {
+              const uint32_t tt = term<TF32>(t);
+              const uint32_t pa = tt & 15u, pb = (tt >> 4) & 15u, acc = (tt >> 8) & 15u;
+              const uint64_t ad = sdesc_sw64(st + pa * P::A_PLANE + j * 32);
+              const uint64_t bd = sdesc_sw64(st + P::NPL * P::A_PLANE + pb * P::B_PLANE + j * 32);
+              umma<TF32>(dset + acc * TN, ad, bd, (tt >> 12) ? id_neg : id_pos, first[acc] ? 0u : 1u);
+              first[acc] = false;
+            }
+          }
+          umma_commit(smem_u32(&bar_empty[s]));
+        }
+        if (!stop) umma_commit(smem_u32(&bar_accf[set]));
+      }
+      umma_commit(smem_u32(&bar_drain));
+    }
+  } else {
+    // drain warps: TMEM lane quarter (warp % 4), column half h
+    const int quarter = warp & 3, h = (warp - 2) >> 2;
+    float sr[TN / 2], si[TN / 2];
+#pragma unroll
+    for (int j = 0; j < TN / 2; j++) sr[j] = si[j] = 0.f;
+    bool good = true;
+    for (int q = 0; q < nq; q++) {
+      const int set = q & 1, u = q >> 1;
+      bool ok = mbar_wait(smem_u32(&bar_accf[set]), u & 1, &abort_flag);
+      if (!ok && !abort_flag) fail(4);
+      if (!__all_sync(0xffffffffu, ok && !abort_flag)) {
+        good = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t base = tmem + (static_cast<uint32_t>(32 * quarter) << 16) + set * (2 * TN) + h * (TN / 2);
+#pragma unroll
+      for (int c = 0; c < TN / 2; c += 16) {
+        float re[16], im[16];
+        tmem_ld16(base + c, re);
+        tmem_ld16(base + TN + c, im);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          sr[c + j] += re[j];
+          si[c + j] += im[j];
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&bar_acce[set]));
+    }
+    if (good) {
+      const int m = m0 + 32 * quarter + lane;
+      float2 *dst = splits == 1 ? batches[z].out : ws + ((long long)sp * nz + z) * (long long)N * M;
+      if (m < M) {
+#pragma unroll
+        for (int j = 0; j < TN / 2; j++) {
+          const int n = n0 + h * (TN / 2) + j;
+          if (n < N) dst[(long long)n * M + m] = make_float2(sr[j], si[j]);
+        }
+      }
+    }
+  }
+
+  // no MMA may still write TMEM when it is freed
+  if (nloc > 0 && !mbar_wait(smem_u32(&bar_drain), 0)) fail(5);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// Splits one operand into planes [plane][z][rows_pad][Kc]: element (z, row, k)
+// is A1[row][k] (k < K1), A2[row][k - K1] (k < K1 + K2) or zero; rows >= rows
+// are zero. side 0 takes the A pointers of the batch, side 1 the B pointers.
+template <bool TF32>
+__global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, int rows, int rows_pad, int Kc,
+                               int nz, void *__restrict__ planes) {
+  const int z = blockIdx.z, row = blockIdx.y;
+  const int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (k0 >= Kc) return;
+  const GemmBatch &bt = batches[z];
+  const float2 *s1 = side ? bt.B1 : bt.A1;
+  const float2 *s2 = side ? bt.B2 : bt.A2;
+  const long long ld1 = side ? bt.ldb1 : bt.lda1, ld2 = side ? bt.ldb2 : bt.lda2;
+  float2 v[4];
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const int k = k0 + e;
+    v[e] = make_float2(0.f, 0.f);
+    if (row < rows) {
+      if (k < bt.K1)
+        v[e] = s1[row * ld1 + k];
+      else if (k < bt.K1 + bt.K2)
+        v[e] = s2[row * ld2 + (k - bt.K1)];
+    }
+  }
+  const size_t plane = (size_t)nz * rows_pad * Kc;
+  const size_t off = ((size_t)z * rows_pad + row) * Kc + k0;
+  if constexpr (TF32) {
+    float *o = static_cast<float *>(planes);
+    *reinterpret_cast<float4 *>(o + off) = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+    *reinterpret_cast<float4 *>(o + plane + off) = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
+  } else {
+    __nv_bfloat16 *o = static_cast<__nv_bfloat16 *>(planes);
+    __nv_bfloat16 h[2][4], l[2][4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const float x[2] = {v[e].x, v[e].y};
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        h[c][e] = __float2bfloat16_rn(x[c]);
+        l[c][e] = __float2bfloat16_rn(x[c] - __bfloat162float(h[c][e]));
+      }
+    }
+    __nv_bfloat16 *dst[4] = {o + off, o + plane + off, o + 2 * plane + off, o + 3 * plane + off};
+    const __nv_bfloat16 *src[4] = {h[0], h[1], l[0], l[1]};
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+      uint2 u;
+      u.x = (uint32_t)__bfloat16_as_ushort(src[p][0]) | ((uint32_t)__bfloat16_as_ushort(src[p][1]) << 16);
+      u.y = (uint32_t)__bfloat16_as_ushort(src[p][2]) | ((uint32_t)__bfloat16_as_ushort(src[p][3]) << 16);
+      *reinterpret_cast<uint2 *>(dst[p]) = u;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    PAWPY_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p)
+      throw Error(ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+CUtensorMap plane_map(void *base, bool tf32, long long Kc, long long rows, int box_rows) {
+  CUtensorMap m;
+  const int esz = tf32 ? 4 : 2;
+  cuuint64_t dims[2] = {(cuuint64_t)Kc, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(Kc * esz)};
+  cuuint32_t box[2] = {(cuuint32_t)(ROWB / esz), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base,
+                           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) PAWPY_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device()));
+  return n;
+}
+
+template <bool TF32>
+void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, int splits_hint,
+            TcGemmInfo *info) {
+  using P = Prec<TF32>;
+  const int nz = (int)hb.size();
+  int maxK = 0, minkb = 1 << 30;
+  std::vector<int> kbl(nz);
+  for (int z = 0; z < nz; z++) {
+    const int K = hb[z].K1 + hb[z].K2;
+    maxK = std::max(maxK, K);
+    kbl[z] = ceil_div(K, P::KB);
+    minkb = std::min(minkb, kbl[z]);
+  }
+  const int Kc = ceil_div(std::max(maxK, 1), P::KB) * P::KB;
+  const int Mpad = ceil_div(M, TM) * TM, Npad = ceil_div(N, TN) * TN;
+  const int tiles = (Mpad / TM) * (Npad / TN) * nz;
+  int splits = splits_hint > 0 ? splits_hint : std::max(1, sm_count() / tiles);
+  splits = std::max(1, std::min(splits, std::max(1, minkb / 4)));
+
+  DevBuf<unsigned char> pa((size_t)P::NPL * nz * Mpad * Kc * P::ESZ);
+  DevBuf<unsigned char> pb((size_t)P::NPL * nz * Npad * Kc * P::ESZ);
+  DevBuf<int> kb_dev(nz);
+  kb_dev.upload(kbl.data(), nz);
+  {
+    dim3 g(ceil_div(Kc / 4, 256), Mpad, nz);
+    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g, 256, 0, stream()>>>(batches_dev, 0, M, Mpad, Kc, nz, pa.p));
+    dim3 g2(ceil_div(Kc / 4, 256), Npad, nz);
+    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g2, 256, 0, stream()>>>(batches_dev, 1, N, Npad, Kc, nz, pb.p));
+  }
+  const CUtensorMap ma = plane_map(pa.p, TF32, Kc, (long long)P::NPL * nz * Mpad, TM);
+  const CUtensorMap mb = plane_map(pb.p, TF32, Kc, (long long)P::NPL * nz * Npad, TN);
+
+  DevBuf<float2> ws;
+  if (splits > 1) ws.alloc((size_t)splits * nz * N * M);
+  DevBuf<int> st(1);
+  st.zero();
+  PAWPY_CUDA(cudaFuncSetAttribute(k_tc_zgemm<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM));
+  dim3 grid(Mpad / TM, Npad / TN, nz * splits);
+  PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
+               k_tc_zgemm<TF32><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev.p, M, N, Mpad,
+                                                                       Npad, nz, splits, ws.p, st.p));
+  if (splits > 1) {
+    dim3 g2(ceil_div((long long)M * N, 256 * 4), nz);
+    PAWPY_LAUNCH("gemm_reduce", k_split_reduce<<<g2, 256, 0, stream()>>>(batches_dev, ws.p, M, N, splits, nz));
+  }
+  int hs = 0;
+  st.download(&hs, 1);
+  sync();
+  if (hs) throw Error(ERR_DEVICE_FLAG, "tensor-core overlap: a pipeline wait timed out (stage " +
+                                           std::to_string(hs) + ")");
+  if (info) {
+    info->splits = splits;
+    info->Kc = Kc;
+    info->ctas = grid.x * grid.y * grid.z;
+  }
+}
+
+}  // namespace
+
+void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
+                     int splits_hint, TcGemmInfo *info) {
+  if (hb.empty() || M <= 0 || N <= 0) return;
+  if (tf32)
+    run_tc<true>(batches_dev, hb, M, N, splits_hint, info);
+  else
+    run_tc<false>(batches_dev, hb, M, N, splits_hint, info);
+}
+
+}  // namespace pawpy
