@@ -54,6 +54,7 @@ struct SphereSet {
 
 struct DevKpt {
   int W = 0, Wpad = 0, g1min = 0, n1 = 0;
+  int g2min = 0, n2 = 0, g3min = 0, n3 = 0;  // occupied ranges of the other two axes
   std::vector<int> perm;     // sorted position -> original plane-wave index
   std::vector<int> invperm;  // original plane-wave index -> sorted position
   std::vector<int> gsorted;  // [W][3] in sorted order
@@ -276,12 +277,21 @@ static void ensure_planes(DevWF &d, DevKpt &q) {
   if (q.off_N2 == d.N[1] && q.off_N3 == d.N[2] && q.plane_off.p) return;
   PAWPY_REQUIRE(q.n1 <= d.N[0], "FFT grid smaller than the plane-wave sphere along the first axis");
   std::vector<int> start(q.n1 + 1, 0), off(q.W);
+  int lo2 = 1 << 30, hi2 = -(1 << 30), lo3 = 1 << 30, hi3 = -(1 << 30);
   for (int t = 0; t < q.W; t++) {
     int g1 = q.gsorted[3 * t], g2 = q.gsorted[3 * t + 1], g3 = q.gsorted[3 * t + 2];
     start[g1 - q.g1min + 1]++;
     int j = ((g2 % d.N[1]) + d.N[1]) % d.N[1], kk = ((g3 % d.N[2]) + d.N[2]) % d.N[2];
     off[t] = j * d.N[2] + kk;
+    lo2 = std::min(lo2, g2);
+    hi2 = std::max(hi2, g2);
+    lo3 = std::min(lo3, g3);
+    hi3 = std::max(hi3, g3);
   }
+  q.g2min = q.W ? lo2 : 0;
+  q.n2 = q.W ? hi2 - lo2 + 1 : 0;
+  q.g3min = q.W ? lo3 : 0;
+  q.n3 = q.W ? hi3 - lo3 + 1 : 0;
   for (int p = 0; p < q.n1; p++) start[p + 1] += start[p];
   q.plane_start.alloc(q.n1 + 1);
   q.plane_start.upload(start.data(), q.n1 + 1);
@@ -473,6 +483,13 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
 
 // One FFT pass over every band of wavefunction d, gathering onto several
 // sphere sets at once. outs[i] receives [nk][nband][sets[i]->Ptot].
+// PAWPY_GPU_FFT=generic selects the shared-memory FFT kernels for every grid
+// (the register kernels are otherwise used for the lengths they are compiled for).
+static bool generic_fft_forced() {
+  const char *e = getenv("PAWPY_GPU_FFT");
+  return e && strcmp(e, "generic") == 0;
+}
+
 static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
                           const std::vector<float2 *> &outs) {
   ensure_coeffs(d);
@@ -578,15 +595,27 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     DevKpt &q = d.kp[k];
     ensure_planes(d, q);
     PlaneGeom g{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
+    g.g2min = q.g2min;
+    g.n2 = q.n2;
+    g.g3min = q.g3min;
+    g.n3 = q.n3;
+    const bool fast = q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
     if (xtot == 0) continue;
     for (int c0 = 0; c0 < d.nband; c0 += cbatch) {
       int cn = std::min(cbatch, d.nband - c0);
       for (int b0 = c0; b0 < c0 + cn; b0 += fbatch) {
         int nb = std::min(fbatch, c0 + cn - b0);
-        launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
-                          d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-        launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, X.p + (size_t)(b0 - c0) * xstride,
-                          xstride, nb);
+        if (fast) {
+          launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p,
+                                 g, H.p, nb);
+          launch_fft_x_pick_fast(H.p, g, segs_d.p, pstart_d.p, k, X.p + (size_t)(b0 - c0) * xstride, xstride,
+                                 nb);
+        } else {
+          launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
+                            d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
+          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k,
+                            X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
+        }
       }
       launch_chunk_contract(ch_d.p, (int)chunks.size(), max_total, X.p, xstride, partial.p, ptot, cn);
       for (size_t i = 0; i < sets.size(); i++) {

@@ -19,13 +19,13 @@ struct Radices {
   int r[12];  // radix of each stage (4 preferred, then 2,3,5,7,...)
 };
 
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 // i*a for s=+1, -i*a for s=-1
-__device__ __forceinline__ float2 rot(float2 a, float s) { return make_float2(-s * a.y, s * a.x); }
+__host__ __device__ __forceinline__ float2 rot(float2 a, float s) { return make_float2(-s * a.y, s * a.x); }
 
 // y = DFT_R(v) with exp(s*2*pi*i*r*q/R); tw holds exp(+2 pi i m/n), n = line length
 template <int S>

@@ -38,7 +38,7 @@ constexpr bool fft_supported(int n) {
 }
 
 template <int R, int N, int S>
-__device__ __forceinline__ void dft_t(float2 (&v)[R], float2 (&o)[R], const float2 *tw) {
+__host__ __device__ __forceinline__ void dft_t(float2 (&v)[R], float2 (&o)[R], const float2 *tw) {
   constexpr float s = (float)S;
   if constexpr (R == 2) {
     o[0] = cadd(v[0], v[1]);

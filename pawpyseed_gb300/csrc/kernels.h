@@ -20,11 +20,22 @@ void launch_load_host_bands(const float2 *const *host_bands, int W, const int *i
 struct PlaneGeom {
   int N1, N2, N3;
   int g1min, n1;  // planes g1 in [g1min, g1min + n1)
+  // rows g2 in [g2min, g2min + n2) and columns g3 in [g3min, g3min + n3)
+  // (mod N2, N3) hold every coefficient of every plane
+  int g2min = 0, n2 = 0, g3min = 0, n3 = 0;
 };
 // H[b][p][j*N3+k] = sum over the plane's coefficients (2D transform of plane p)
 void launch_fft_planes(const float2 *C, int Wpad, const int *plane_start, const int *plane_off,
                        const PlaneGeom &g, const Radices &r2, const Radices &r3, const float2 *tw2,
                        const float2 *tw3, float2 *H, int nb);
+// The same two passes with register line transforms (fft_fast.cu) for the
+// grid lengths compiled there; fft_fast_supported tells whether g is one.
+bool fft_fast_supported(const PlaneGeom &g);
+void launch_fft_planes_fast(const float2 *C, int Wpad, const int *plane_start, const int *plane_off,
+                            const PlaneGeom &g, float2 *H, int nb);
+struct GatherSeg;
+void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const GatherSeg *segs, const int *plane_start,
+                            int kq, float2 *X, long long xstride, int nb);
 // Generic in-place transform of full grids along one axis (single-band paths).
 void launch_fft_axis(float2 *grid, int nb, int N1, int N2, int N3, int axis, const Radices &r,
                      const float2 *tw);

@@ -242,3 +242,16 @@ def test_errors_do_not_abort(workload_dirs):
                          wf.nums, wf.coords, basis.nums, basis.coords, wf.dim, 0)
     with pytest.raises(_lib.PAWpyGPUError):
         _lib.check()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_register_fft_matches_shared_memory_fft(name, workload_dirs, monkeypatch):
+    """The register line-FFT kernels and the generic shared-memory kernels give the same projections."""
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs(name))
+    fast = Projector(wf, basis).project_all()
+    monkeypatch.setenv("PAWPY_GPU_FFT", "generic")
+    basis2, wf2 = load(workload_dirs(name))
+    slow = Projector(wf2, basis2).project_all()
+    assert np.abs(fast - slow).max() <= 1e-6
