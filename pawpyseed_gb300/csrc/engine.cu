@@ -55,6 +55,7 @@ struct SphereSet {
 struct DevKpt {
   int W = 0, Wpad = 0, g1min = 0, n1 = 0;
   int g2min = 0, n2 = 0, g3min = 0, n3 = 0;  // occupied ranges of the other two axes
+  int maxcnt = 0;                             // most coefficients in one plane
   std::vector<int> perm;     // sorted position -> original plane-wave index
   std::vector<int> invperm;  // original plane-wave index -> sorted position
   std::vector<int> gsorted;  // [W][3] in sorted order
@@ -292,6 +293,8 @@ static void ensure_planes(DevWF &d, DevKpt &q) {
   q.n2 = q.W ? hi2 - lo2 + 1 : 0;
   q.g3min = q.W ? lo3 : 0;
   q.n3 = q.W ? hi3 - lo3 + 1 : 0;
+  q.maxcnt = 0;
+  for (int p = 0; p < q.n1; p++) q.maxcnt = std::max(q.maxcnt, start[p + 1]);
   for (int p = 0; p < q.n1; p++) start[p + 1] += start[p];
   q.plane_start.alloc(q.n1 + 1);
   q.plane_start.upload(start.data(), q.n1 + 1);
@@ -559,6 +562,37 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   for (int j = 0; j < d.N[1]; j++) pstart[j + 1] += pstart[j];
   DevBuf<GatherSeg> segs_d(std::max<size_t>(1, sorted.size()));
   segs_d.upload(sorted.data(), sorted.size());
+  // the same points as one list in plane order, for the register FFT's pick
+  std::vector<int> seg_base(std::max<size_t>(1, sorted.size()), 0), plane_first(d.N[1] + 1, 0);
+  int max_plane_pts = 0;
+  {
+    int acc = 0;
+    for (int j = 0; j < d.N[1]; j++) {
+      plane_first[j] = acc;
+      for (int q = pstart[j]; q < pstart[j + 1]; q++) {
+        seg_base[q] = acc;
+        acc += sorted[q].npts;
+      }
+      max_plane_pts = std::max(max_plane_pts, acc - plane_first[j]);
+    }
+    plane_first[d.N[1]] = acc;
+  }
+  DevBuf<int> seg_base_d(seg_base.size()), plane_first_d(plane_first.size());
+  seg_base_d.upload(seg_base.data(), seg_base.size());
+  plane_first_d.upload(plane_first.data(), plane_first.size());
+  const long long npick = plane_first[d.N[1]];
+  DevBuf<int> pick_cell(std::max(1LL, npick)), pick_xo(std::max(1LL, npick));
+  DevBuf<float2> pick_phase(std::max(1LL, npick * d.nk));
+  PickList plist;
+  plist.plane_first = plane_first_d.p;
+  plist.cell = pick_cell.p;
+  plist.xo = pick_xo.p;
+  plist.phase = pick_phase.p;
+  plist.npts = npick;
+  plist.max_plane_pts = max_plane_pts;
+  for (size_t i = 0; i < sets.size(); i++)
+    PAWPY_REQUIRE(sets[i]->nkp == d.nk, "sphere tables and wavefunction differ in k-points");
+  launch_flatten_pick(segs_d.p, seg_base_d.p, (int)sorted.size(), d.nk, plist);
   DevBuf<int> pstart_d(pstart.size());
   pstart_d.upload(pstart.data(), pstart.size());
   DevBuf<ChunkContract> ch_d(std::max<size_t>(1, chunks.size()));
@@ -579,9 +613,12 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   }
   int maxn1 = 0;
   for (auto &q : d.kp) maxn1 = std::max(maxn1, q.n1);
-  // FFT sub-batch: keep the plane-FFT intermediate near L2 size (~96 MiB)
+  // FFT sub-batch: the plane-FFT intermediate H of a sub-batch stays within L2
+  // between the two passes (PAWPY_GPU_FFT_BATCH_MB overrides the size)
   long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
-  int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, (96LL << 20) / std::max(1LL, hband)));
+  long long hcap = 96LL << 20;
+  if (const char *e = getenv("PAWPY_GPU_FFT_BATCH_MB")) hcap = std::max(1LL, atoll(e)) << 20;
+  int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, hcap / std::max(1LL, hband)));
   // contraction batch: picked points and partial sums of up to 2 GiB
   long long xstride = (xtot + 3) / 4 * 4;
   long long per_band = (xstride + ptot) * (long long)sizeof(float2);
@@ -599,6 +636,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     g.n2 = q.n2;
     g.g3min = q.g3min;
     g.n3 = q.n3;
+    g.maxcnt = q.maxcnt;
     const bool fast = q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
     if (xtot == 0) continue;
     for (int c0 = 0; c0 < d.nband; c0 += cbatch) {
@@ -608,8 +646,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
         if (fast) {
           launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p,
                                  g, H.p, nb);
-          launch_fft_x_pick_fast(H.p, g, segs_d.p, pstart_d.p, k, X.p + (size_t)(b0 - c0) * xstride, xstride,
-                                 nb);
+          launch_fft_x_pick_fast(H.p, g, plist, k, X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
         } else {
           launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);

@@ -3,17 +3,20 @@
 // at compile time; other lengths use the shared-memory kernels of kernels.cu
 // and sphere.cu.
 //
-// Pass A, per (band, PP planes g1): scatter the plane's coefficients into a
-// padded shared tile, transform the occupied rows along the third axis, then
-// every column along the second axis straight from registers to H.
-// Pass B, per (band, JJ planes of the second axis): transform every line along
-// the first axis straight from H into a shared tile, then pick the sphere
-// points of those planes (value times Bloch phase) into X.
-// Rows and columns outside the plane-wave sphere are known to be zero and are
-// neither read nor written. PP and JJ are chosen per grid by timing every
-// candidate on the first batch (the results do not depend on them).
+// Pass A: a CTA owns one plane g1 and loops over bands; per band it scatters
+// the plane's coefficients into a padded shared tile, transforms the occupied
+// rows along the third axis, then every column along the second axis straight
+// from registers to H. Pass B: a CTA owns one plane of the second axis and
+// loops over bands; per band it transforms the first axis from H into a
+// shared tile and picks the sphere points of the plane (value times Bloch
+// phase) into X. Both prefetch the next band's input with cp.async while the
+// current one is transformed. Rows and columns outside the plane-wave sphere
+// are known to be zero and are neither read nor written. The number of band
+// groups (CTAs per plane) is chosen per grid by timing the candidates on the
+// first batch (the results do not depend on it).
 #pragma once
 
+#include <algorithm>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -43,131 +46,199 @@ __device__ __forceinline__ int wrapi(int v, int N) {
 
 }  // namespace
 
-template <int N2, int N3, int PP>
-__global__ void __launch_bounds__(FT) k_planes_reg(const float2 *__restrict__ C, int Wpad,
-                                                   const int *__restrict__ pstart, const int *__restrict__ poff,
-                                                   PlaneGeom g, float2 *__restrict__ H) {
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Pass A. grid (n1 planes, G band groups), FT threads: CTA (p, g) transforms
+// plane p of bands g, g + G, ... of the batch. Shared memory: ta [n2][LD] holds
+// the plane's coefficients on the occupied rows (its other cells are zeroed
+// once: the coefficient positions of a plane are the same for every band), tb
+// [n2][LD] the rows after the third-axis transform, stage [2][maxcnt] the
+// coefficients of the current and the next band (cp.async), pos [maxcnt] the
+// cell of each coefficient.
+template <int N2, int N3>
+__global__ void __launch_bounds__(FT) k_planes_pipe(const float2 *__restrict__ C, int Wpad, int nb,
+                                                    const int *__restrict__ pstart, const int *__restrict__ poff,
+                                                    PlaneGeom g, float2 *__restrict__ H) {
   constexpr int LD = padded(N3);
   constexpr int T3 = reg::lanes_for(N3), L3 = N3 / T3;
   constexpr int T2 = reg::lanes_for(N2), L2 = N2 / T2;
-  extern __shared__ float2 tile[];  // [PP][N2][LD]
-  const int band = blockIdx.y, p0 = blockIdx.x * PP;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n2 = g.n2, maxcnt = g.maxcnt;
+  float2 *ta = reinterpret_cast<float2 *>(smraw);
+  float2 *tb = ta + n2 * LD;
+  float2 *stage = tb + n2 * LD;
+  int *pos = reinterpret_cast<int *>(stage + 2 * maxcnt);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int np = min(PP, g.n1 - p0);
+  const int p = blockIdx.x, G = gridDim.y;
+  const int t0 = pstart[p], cnt = pstart[p + 1] - t0;
   const int s2 = wrapi(g.g2min, N2), s3 = wrapi(g.g3min, N3);
-  const int occ = g.n2 * g.n3;
-  for (int e = threadIdx.x; e < np * occ; e += blockDim.x) {
-    const int pl = e / occ, r = e - pl * occ, i = r / g.n3, c = r - i * g.n3;
-    const int row = s2 + i >= N2 ? s2 + i - N2 : s2 + i, col = s3 + c >= N3 ? s3 + c - N3 : s3 + c;
-    tile[(pl * N2 + row) * LD + col] = make_float2(0.f, 0.f);
+  for (int e = threadIdx.x; e < n2 * LD; e += blockDim.x) ta[e] = make_float2(0.f, 0.f);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int o = poff[t0 + t], row = o / N3, col = o - row * N3;
+    int i = row - s2;
+    i += i < 0 ? N2 : 0;
+    pos[t] = i * LD + col;
   }
-  __syncthreads();
-  const float2 *cb = C + (long long)band * Wpad;
-  for (int pl = 0; pl < np; pl++)
-    for (int t = pstart[p0 + pl] + threadIdx.x; t < pstart[p0 + pl + 1]; t += blockDim.x) {
-      const int o = poff[t], row = o / N3, col = o - row * N3;
-      tile[(pl * N2 + row) * LD + col] = cb[t];
+  auto prefetch = [&](int b, int buf) {
+    const float2 *src = C + (long long)b * Wpad + t0;
+    float2 *dst = stage + buf * maxcnt;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_async8(dst + t, src + t);
+    cp_async_commit();
+  };
+  int b = blockIdx.y;
+  if (b < nb) prefetch(b, 0);
+  for (int it = 0; b < nb; it++, b += G) {
+    if (b + G < nb) {
+      prefetch(b + G, (it + 1) & 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
-  __syncthreads();
-  {  // third axis, occupied rows only
-    constexpr int LPW = 32 / T3;
-    const int h = lane / LPW, c = lane % LPW;
-    const int nlines = np * g.n2;
-    for (int g0 = warp * LPW; g0 < nlines; g0 += nw * LPW) {
-      const int line = g0 + c;
-      const bool ok = line < nlines;
-      const int pl = ok ? line / g.n2 : 0, i = ok ? line - pl * g.n2 : 0;
-      const int row = s2 + i >= N2 ? s2 + i - N2 : s2 + i;
-      float2 *rp = tile + (pl * N2 + row) * LD;
-      float2 x[L3];
+    __syncthreads();  // this band's coefficients landed; the previous band is done with ta and tb
+    const float2 *sv = stage + (it & 1) * maxcnt;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) ta[pos[t]] = sv[t];
+    __syncthreads();
+    {  // third axis, occupied rows
+      constexpr int LPW = 32 / T3;
+      const int h = lane / LPW, c = lane % LPW;
+      for (int g0 = warp * LPW; g0 < n2; g0 += nw * LPW) {
+        const int i = g0 + c;
+        const bool ok = i < n2;
+        const float2 *rp = ta + (ok ? i : 0) * LD;
+        float2 x[L3];
 #pragma unroll
-      for (int m = 0; m < L3; m++) {
-        const int col = h + T3 * m;
-        x[m] = ok && occupied(col, s3, g.n3, N3) ? rp[col] : make_float2(0.f, 0.f);
-      }
-      reg::line_fft<N3, T3, 1>(x, h);
-      if (ok) {
-        const int o = L3 * reg::bitrev(h, T3);
+        for (int m = 0; m < L3; m++) {
+          const int col = h + T3 * m;
+          x[m] = ok && occupied(col, s3, g.n3, N3) ? rp[col] : make_float2(0.f, 0.f);
+        }
+        reg::line_fft<N3, T3, 1>(x, h);
+        if (ok) {
+          float2 *wp = tb + i * LD + L3 * reg::bitrev(h, T3);
 #pragma unroll
-        for (int k = 0; k < L3; k++) rp[o + k] = x[k];
+          for (int k = 0; k < L3; k++) wp[k] = x[k];
+        }
       }
     }
-  }
-  __syncthreads();
-  {  // second axis, every column, to H
-    constexpr int LPW = 32 / T2;
-    const int h = lane / LPW, c = lane % LPW;
-    const int nlines = np * N3;
-    for (int g0 = warp * LPW; g0 < nlines; g0 += nw * LPW) {
-      const int line = g0 + c;
-      const bool ok = line < nlines;
-      const int pl = ok ? line / N3 : 0, col = ok ? line - pl * N3 : 0;
-      const float2 *cp = tile + pl * N2 * LD + col;
-      float2 x[L2];
+    __syncthreads();
+    {  // second axis, every column, to H
+      constexpr int LPW = 32 / T2;
+      const int h = lane / LPW, c = lane % LPW;
+      float2 *out = H + ((long long)b * g.n1 + p) * (N2 * N3);
+      for (int g0 = warp * LPW; g0 < N3; g0 += nw * LPW) {
+        const int col = g0 + c;
+        const bool ok = col < N3;
+        float2 x[L2];
 #pragma unroll
-      for (int m = 0; m < L2; m++) {
-        const int row = h + T2 * m;
-        x[m] = ok && occupied(row, s2, g.n2, N2) ? cp[row * LD] : make_float2(0.f, 0.f);
-      }
-      reg::line_fft<N2, T2, 1>(x, h);
-      if (ok) {
-        float2 *out = H + ((long long)band * g.n1 + p0 + pl) * (N2 * N3) + col;
-        const int o = L2 * reg::bitrev(h, T2);
+        for (int m = 0; m < L2; m++) {
+          int i = h + T2 * m - s2;
+          i += i < 0 ? N2 : 0;
+          x[m] = ok && i < n2 ? tb[i * LD + col] : make_float2(0.f, 0.f);
+        }
+        reg::line_fft<N2, T2, 1>(x, h);
+        if (ok) {
+          const int o = L2 * reg::bitrev(h, T2);
 #pragma unroll
-        for (int k = 0; k < L2; k++) out[(o + k) * N3] = x[k];
+          for (int k = 0; k < L2; k++) out[(o + k) * N3 + col] = x[k];
+        }
       }
     }
   }
 }
 
-template <int N1, int N3, int JJ>
-__global__ void __launch_bounds__(FT) k_xpick_reg(const float2 *__restrict__ H, PlaneGeom g,
-                                                  const GatherSeg *__restrict__ segs,
-                                                  const int *__restrict__ plane_start, int kq,
-                                                  float2 *__restrict__ X, long long xstride) {
+// Pass B. grid (N2 planes j, G band groups), FT threads: CTA (j, g) transforms
+// the first axis of plane j of bands g, g + G, ... and picks its sphere
+// points. The pick list of plane j is points [plane_first[j],
+// plane_first[j + 1]) of cell (i N3 + k within the plane), xo (position in X)
+// and phase (Bloch phase at this k-point). Shared memory: stage [2][n1][N3]
+// the plane's H rows of the current and the next band (cp.async), tile
+// [N1][LD] the transformed plane and, when the plane has at most pts_cap
+// points, a copy of its pick list (the same for every band).
+template <int N1, int N3>
+__global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H, int nb, PlaneGeom g,
+                                                   const int *__restrict__ plane_first,
+                                                   const int *__restrict__ cell, const int *__restrict__ xo,
+                                                   const float2 *__restrict__ phase, int pts_cap,
+                                                   float2 *__restrict__ X, long long xstride) {
   constexpr int LD = padded(N3);
   constexpr int T1 = reg::lanes_for(N1), L1 = N1 / T1;
-  extern __shared__ float2 tile[];  // [JJ][N1][LD]
-  const int band = blockIdx.y, j0 = blockIdx.x * JJ;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n1 = g.n1, per = n1 * N3;
+  float2 *stage = reinterpret_cast<float2 *>(smraw);
+  float2 *tile = stage + 2 * per;
+  float2 *pph = tile + N1 * LD;
+  int *pto = reinterpret_cast<int *>(pph + pts_cap);
+  int *pxo = pto + pts_cap;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int nj = min(JJ, g.N2 - j0);
+  const int j = blockIdx.x, G = gridDim.y;
   const int s1 = wrapi(g.g1min, N1);
-  {
-    constexpr int LPW = 32 / T1;
-    const int h = lane / LPW, c = lane % LPW;
-    const int nlines = nj * N3;
-    for (int g0 = warp * LPW; g0 < nlines; g0 += nw * LPW) {
-      const int line = g0 + c;
-      const bool ok = line < nlines;
-      const int jl = ok ? line / N3 : 0, z = ok ? line - jl * N3 : 0;
-      const float2 *hp = H + ((long long)band * g.n1 * g.N2 + j0 + jl) * N3 + z;
-      const int pstride = g.N2 * N3;  // n1 * N2 * N3 < 2^31
-      float2 x[L1];
+  const long long pstride = (long long)g.N2 * N3;
+  auto prefetch = [&](int b, int buf) {
+    const float2 *src = H + ((long long)b * n1 * g.N2 + j) * N3;
+    float2 *dst = stage + buf * per;
+    for (int e = threadIdx.x; e < per; e += blockDim.x) {
+      const int p = e / N3, z = e - p * N3;
+      cp_async8(dst + e, src + p * pstride + z);
+    }
+    cp_async_commit();
+  };
+  const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
+  const bool staged = npj <= pts_cap;
+  int b = blockIdx.y;
+  if (b < nb) prefetch(b, 0);
+  if (staged)
+    for (int q = threadIdx.x; q < npj; q += blockDim.x) {
+      const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
+      pto[q] = xr * LD + z;
+      pxo[q] = xo[pf + q];
+      pph[q] = phase[pf + q];
+    }
+  for (int it = 0; b < nb; it++, b += G) {
+    if (b + G < nb) {
+      prefetch(b + G, (it + 1) & 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // this band's rows landed; the previous band's pick is done with the tile
+    {
+      constexpr int LPW = 32 / T1;
+      const int h = lane / LPW, c = lane % LPW;
+      const float2 *sv = stage + (it & 1) * per;
+      for (int g0 = warp * LPW; g0 < N3; g0 += nw * LPW) {
+        const int z = g0 + c;
+        const bool ok = z < N3;
+        float2 x[L1];
 #pragma unroll
-      for (int m = 0; m < L1; m++) {
-        int p = h + T1 * m - s1;
-        p += p < 0 ? N1 : 0;
-        x[m] = ok && p < g.n1 ? hp[p * pstride] : make_float2(0.f, 0.f);
-      }
-      reg::line_fft<N1, T1, 1>(x, h);
-      if (ok) {
-        float2 *tp = tile + (jl * N1 + L1 * reg::bitrev(h, T1)) * LD + z;
+        for (int m = 0; m < L1; m++) {
+          int pp = h + T1 * m - s1;
+          pp += pp < 0 ? N1 : 0;
+          x[m] = ok && pp < n1 ? sv[pp * N3 + z] : make_float2(0.f, 0.f);
+        }
+        reg::line_fft<N1, T1, 1>(x, h);
+        if (ok) {
+          float2 *tp = tile + (L1 * reg::bitrev(h, T1)) * LD + z;
 #pragma unroll
-        for (int k = 0; k < L1; k++) tp[k * LD] = x[k];
+          for (int k = 0; k < L1; k++) tp[k * LD] = x[k];
+        }
       }
     }
-  }
-  __syncthreads();
-  float2 *xb = X + (long long)band * xstride;
-  for (int jl = 0; jl < nj; jl++) {
-    const int j = j0 + jl;
-    const float2 *tp = tile + jl * N1 * LD;
-    for (int si = plane_start[j] + warp; si < plane_start[j + 1]; si += nw) {
-      const GatherSeg sg = segs[si];
-      const float2 *ph = sg.phase + (long long)kq * sg.phase_stride;
-      for (int p = lane; p < sg.npts; p += 32) {
-        const int idx = sg.idx[p], xr = idx / N3, z = idx - xr * N3;
-        xb[sg.x_off + p] = cmul(tp[xr * LD + z], ph[p]);
+    __syncthreads();
+    float2 *xb = X + (long long)b * xstride;
+    if (staged) {
+      for (int q = threadIdx.x; q < npj; q += blockDim.x) xb[pxo[q]] = cmul(tile[pto[q]], pph[q]);
+    } else {
+      for (int q = threadIdx.x; q < npj; q += blockDim.x) {
+        const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
+        xb[xo[pf + q]] = cmul(tile[xr * LD + z], phase[pf + q]);
       }
     }
   }
@@ -179,7 +250,12 @@ namespace fftfast {
 
 constexpr size_t kSmemCap = 200 * 1024;
 
-inline size_t tile_bytes(int planes, int rows, int cols) { return sizeof(float2) * (size_t)planes * rows * padded(cols); }
+inline size_t planes_smem(const PlaneGeom &g) {
+  return sizeof(float2) * (2 * (size_t)g.n2 * padded(g.N3) + 2 * (size_t)g.maxcnt) + sizeof(int) * (size_t)g.maxcnt;
+}
+inline size_t xpick_smem(const PlaneGeom &g, int pts_cap = 0) {
+  return sizeof(float2) * (2 * (size_t)g.n1 * g.N3 + (size_t)g.N1 * padded(g.N3)) + 16 * (size_t)pts_cap;
+}
 
 inline void allow_smem(const void *fn, size_t bytes) {
   static std::map<const void *, size_t> done;
@@ -190,7 +266,15 @@ inline void allow_smem(const void *fn, size_t bytes) {
   }
 }
 
-// tuned tile counts per (pass, N1, N2, N3)
+// CTAs of fn resident on the whole device at once (FT threads, smem bytes)
+inline int resident_ctas(const void *fn, size_t smem) {
+  int per_sm = 0, nsm = 0;
+  PAWPY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, FT, smem));
+  PAWPY_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device()));
+  return std::max(1, per_sm) * nsm;
+}
+
+// tuned choices per (pass, N1, N2, N3)
 inline std::map<std::tuple<int, int, int, int>, int> &tuned() {
   static std::map<std::tuple<int, int, int, int>, int> t;
   return t;

@@ -1,24 +1,16 @@
-// Dispatch and tile tuning of pass B of the band FFT (k_xpick_reg).
+// Dispatch and tuning of pass B of the band FFT (k_xpick_pipe).
 #include "fft_fast.cuh"
 
 namespace pawpy {
 
 namespace {
 
-using PickFn = void (*)(const float2 *, PlaneGeom, const GatherSeg *, const int *, int, float2 *, long long);
+using PickFn = void (*)(const float2 *, int, PlaneGeom, const int *, const int *, const int *, const float2 *, int,
+                       float2 *, long long);
 
-template <int N1, int N3>
-PickFn pick_fn(int jj) {
-  switch (jj) {
-    case 1: return k_xpick_reg<N1, N3, 1>;
-    case 2: return k_xpick_reg<N1, N3, 2>;
-    default: return k_xpick_reg<N1, N3, 4>;
-  }
-}
-
-PickFn find_pick(int n1, int n3, int jj) {
+PickFn find_pick(int n1, int n3) {
 #define X(a, b) \
-  if (n1 == a && n3 == b) return pick_fn<a, b>(jj);
+  if (n1 == a && n3 == b) return k_xpick_pipe<a, b>;
   PAWPY_FFT_PAIRS(X)
 #undef X
   return nullptr;
@@ -29,26 +21,48 @@ PickFn find_pick(int n1, int n3, int jj) {
 bool fft_planes_fast_supported(int n2, int n3);
 
 bool fft_fast_supported(const PlaneGeom &g) {
-  return fft_planes_fast_supported(g.N2, g.N3) && find_pick(g.N1, g.N3, 1) && g.n2 > 0 && g.n3 > 0;
+  return fft_planes_fast_supported(g.N2, g.N3) && find_pick(g.N1, g.N3) && g.n2 > 0 && g.n3 > 0 &&
+         fftfast::planes_smem(g) <= fftfast::kSmemCap && fftfast::xpick_smem(g) <= fftfast::kSmemCap;
 }
 
-void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const GatherSeg *segs, const int *plane_start,
-                            int kq, float2 *X, long long xstride, int nb) {
+void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
+                            long long xstride, int nb) {
   using namespace fftfast;
   if (nb <= 0) return;
-  auto run = [&](int jj) {
-    PickFn fn = find_pick(g.N1, g.N3, jj);
-    PAWPY_REQUIRE(fn, "no register FFT for this grid");
-    size_t smem = tile_bytes(jj, g.N1, g.N3);
-    allow_smem((const void *)fn, smem);
-    dim3 grid(ceil_div(g.N2, jj), nb);
-    PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, g, segs, plane_start, kq, X, xstride));
+  PickFn fn = find_pick(g.N1, g.N3);
+  PAWPY_REQUIRE(fn, "no register FFT for this grid");
+  // stage the pick lists when they fit; planes with more points read them from global memory
+  const int cap = xpick_smem(g, pl.max_plane_pts) <= kSmemCap ? pl.max_plane_pts : 0;
+  const size_t smem = xpick_smem(g, cap);
+  allow_smem((const void *)fn, smem);
+  const int waves = resident_ctas((const void *)fn, smem);
+  const float2 *ph = pl.phase + (long long)kq * pl.npts;
+  auto run = [&](int mult) {
+    const int G = std::max(1, std::min(nb, ceil_div((long long)waves * mult, g.N2)));
+    dim3 grid(g.N2, G);
+    PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, cap, X,
+                                                                xstride));
   };
-  std::vector<int> cands;
-  for (int jj : {1, 2, 4})
-    if (tile_bytes(jj, g.N1, g.N3) <= kSmemCap) cands.push_back(jj);
-  int jj = tune(std::make_tuple(1, g.N1, g.N2, g.N3), cands, run);
-  run(jj);
+  int mult = tune(std::make_tuple(1, g.N1, g.N2, g.N3), {1, 2, 4}, run);
+  run(mult);
+}
+
+// One CTA per segment: its points go to positions base[si] + p of the flat list.
+__global__ void k_flatten_pick(const GatherSeg *__restrict__ segs, const int *__restrict__ base, int nkp,
+                               long long Q, int *__restrict__ cell, int *__restrict__ xo, float2 *__restrict__ phase) {
+  const GatherSeg sg = segs[blockIdx.x];
+  const int q0 = base[blockIdx.x];
+  for (int p = threadIdx.x; p < sg.npts; p += blockDim.x) {
+    cell[q0 + p] = sg.idx[p];
+    xo[q0 + p] = (int)(sg.x_off + p);
+    for (int k = 0; k < nkp; k++) phase[k * Q + q0 + p] = sg.phase[k * sg.phase_stride + p];
+  }
+}
+
+void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl) {
+  if (nsegs <= 0) return;
+  PAWPY_LAUNCH("pick_list", k_flatten_pick<<<nsegs, 128, 0, stream()>>>(segs, base, nkp, pl.npts, pl.cell, pl.xo,
+                                                                         pl.phase));
 }
 
 }  // namespace pawpy

@@ -23,6 +23,7 @@ struct PlaneGeom {
   // rows g2 in [g2min, g2min + n2) and columns g3 in [g3min, g3min + n3)
   // (mod N2, N3) hold every coefficient of every plane
   int g2min = 0, n2 = 0, g3min = 0, n3 = 0;
+  int maxcnt = 0;  // most coefficients in one plane
 };
 // H[b][p][j*N3+k] = sum over the plane's coefficients (2D transform of plane p)
 void launch_fft_planes(const float2 *C, int Wpad, const int *plane_start, const int *plane_off,
@@ -34,8 +35,20 @@ bool fft_fast_supported(const PlaneGeom &g);
 void launch_fft_planes_fast(const float2 *C, int Wpad, const int *plane_start, const int *plane_off,
                             const PlaneGeom &g, float2 *H, int nb);
 struct GatherSeg;
-void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const GatherSeg *segs, const int *plane_start,
-                            int kq, float2 *X, long long xstride, int nb);
+// The sphere points in plane order: points [plane_first[j], plane_first[j + 1])
+// lie in plane j of the second axis; cell is i*N3 + k within the plane, xo the
+// position in the picked-point vector, phase[kq*npts + q] the Bloch phase.
+struct PickList {
+  const int *plane_first = nullptr;
+  int *cell = nullptr, *xo = nullptr;
+  float2 *phase = nullptr;
+  long long npts = 0;
+  int max_plane_pts = 0;
+};
+void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
+                            long long xstride, int nb);
+// fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
+void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).
 void launch_fft_axis(float2 *grid, int nb, int N1, int N2, int N3, int axis, const Radices &r,
                      const float2 *tw);
