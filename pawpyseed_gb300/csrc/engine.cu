@@ -506,7 +506,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   std::vector<SetMaps> maps(sets.size());
   long long xtot = 0;
   int ptot = 0, max_total = 0;
-  const int CHUNK = 512;
+  const int CHUNK = CHUNK_PTS;
   for (size_t i = 0; i < sets.size(); i++) {
     const SphereSet &S = *sets[i];
     for (int q = 0; q < S.nseg; q++) {
@@ -597,19 +597,18 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   pstart_d.upload(pstart.data(), pstart.size());
   DevBuf<ChunkContract> ch_d(std::max<size_t>(1, chunks.size()));
   ch_d.upload(chunks.data(), chunks.size());
-  struct SetMapsDev {
-    DevBuf<int> col_site, col_lm, site_ptr, chunk_off;
-  };
-  std::vector<SetMapsDev> mdev(sets.size());
+  // per output column: first partial, chunk count and chunk stride of its site
+  std::vector<DevBuf<int4>> mdev(sets.size());
   for (size_t i = 0; i < sets.size(); i++) {
-    auto up = [](DevBuf<int> &b, const std::vector<int> &v) {
-      b.alloc(std::max<size_t>(1, v.size()));
-      b.upload(v.data(), v.size());
-    };
-    up(mdev[i].col_site, maps[i].col_site);
-    up(mdev[i].col_lm, maps[i].col_lm);
-    up(mdev[i].site_ptr, maps[i].site_ptr);
-    up(mdev[i].chunk_off, maps[i].chunk_off);
+    const SetMaps &m = maps[i];
+    std::vector<int4> col(std::max<size_t>(1, m.col_site.size()));
+    for (size_t o = 0; o < m.col_site.size(); o++) {
+      const int s = m.col_site[o], e0 = m.site_ptr[s], ne = m.site_ptr[s + 1] - e0;
+      const int stride = ne > 1 ? m.chunk_off[e0 + 1] - m.chunk_off[e0] : 0;
+      col[o] = make_int4(m.chunk_off[e0] + m.col_lm[o], ne, stride, 0);
+    }
+    mdev[i].alloc(col.size());
+    mdev[i].upload(col.data(), col.size());
   }
   int maxn1 = 0;
   for (auto &q : d.kp) maxn1 = std::max(maxn1, q.n1);
@@ -658,8 +657,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       for (size_t i = 0; i < sets.size(); i++) {
         const SphereSet &S = *sets[i];
         if (S.nsites == 0) continue;
-        launch_chunk_reduce(partial.p, ptot, mdev[i].col_site.p, mdev[i].col_lm.p, mdev[i].site_ptr.p,
-                            mdev[i].chunk_off.p, outs[i], S.Ptot, cn, (long long)k * d.nband + c0);
+        launch_chunk_reduce(partial.p, ptot, mdev[i].p, outs[i], S.Ptot, cn, (long long)k * d.nband + c0);
       }
     }
   }

@@ -94,7 +94,8 @@ struct GatherSeg {
   long long x_off;       // position of the segment's first point in the picked-point vector
   int npts;
 };
-// a chunk (<= 512 consecutive points) of one site as the contraction sees it
+// a chunk (<= CHUNK_PTS consecutive points) of one site as the contraction sees it
+constexpr int CHUNK_PTS = 256;
 struct ChunkContract {
   const float2 *tab;     // the site's table [total][site_npts], offset to the chunk's first point
   long long x_off;       // first point of the chunk in the picked-point vector
@@ -116,10 +117,10 @@ void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, c
 // partial[b][part_off + lm] = sum_p X[b][x_off + p] * tab[lm][p] over each chunk, bands b < nb
 void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
                            long long xstride, float2 *partial, int ptot, int nb);
-// P[(band_base + b)*Ptot + o] = sum of partial[b][chunk_off[e] + col_lm[o]] over the chunks e of the
-// site of column o (site_ptr CSR), in chunk order
-void launch_chunk_reduce(const float2 *partial, int ptot, const int *col_site, const int *col_lm,
-                         const int *site_ptr, const int *chunk_off, float2 *P, int Ptot, int nb, long long band_base);
+// P[(band_base + b)*Ptot + o] = sum over c < col[o].y of partial[b][col[o].x + c*col[o].z]: the
+// chunks of column o's site, in chunk order
+void launch_chunk_reduce(const float2 *partial, int ptot, const int4 *col, float2 *P, int Ptot, int nb,
+                         long long band_base);
 
 // ---- overlap GEMM (FP32 complex, SIMT) ----
 // For each batch z < nz: out_z[n][m] = sum_k conj(A_z[m][k]) * B_z[n][k], with the K range split

@@ -255,111 +255,132 @@ void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, c
 }
 
 // ---------------------------------------------------------------------------
-// <p_lm|psi_b> = sum_p X[b][p] tab[lm][p], chunk by chunk.
+// <p_lm|psi_b> = sum_p X[b][p] tab[lm][p], chunk by chunk (the sum over the
+// grid points of one site in onto_projector, projector.c:266-311, for every
+// band at once).
 //
-// One CTA per (chunk, block of 32 bands), 128 threads: thread t owns the band
-// pair (2*(t/8), 2*(t/8)+1) and the channels lm = t%8 + 8q. Points go through
-// shared memory 64 at a time (rows padded against bank conflicts). Each
-// table value read feeds two bands.
+// One CTA per (chunk, block of CT bands), one band per thread. The chunk's
+// table (<= CHUNK_PTS points x its lm channels) is staged in shared memory
+// once and read as warp-wide broadcasts of two points (16 bytes); each thread
+// streams its band's picked values UP points at a time with all UP/2 16-byte
+// loads issued before they are used, so that a warp keeps several memory
+// requests in flight. The table is stored shifted by the parity of the
+// chunk's first point so that both streams stay 16-byte aligned. The channel
+// count is a compile-time bound chosen per chunk (8, 18 or 32).
 namespace {
-constexpr int CB = 32, CP = 64, CPP = CP + 1, CT = 128;
+constexpr int CT = 128;
+constexpr int UP = 16;
+constexpr int TSTRIDE = CHUNK_PTS + 2;
 }
 
-template <int NQ>
+template <int NL>
+__device__ __forceinline__ void chunk_body(const ChunkContract &cc, const float2 *__restrict__ ts, int shift,
+                                           const float2 *__restrict__ x, float2 *__restrict__ o) {
+  float ar[NL], ai[NL];
+#pragma unroll
+  for (int l = 0; l < NL; l++) ar[l] = ai[l] = 0.f;
+  const int n = cc.npts;
+  auto mac = [&](int l, float2 t, float2 v) {
+    ar[l] = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar[l]));
+    ai[l] = fmaf(t.x, v.y, fmaf(t.y, v.x, ai[l]));
+  };
+  int p = 0;
+  if (shift && n > 0) {  // odd first point: one point alone
+    const float2 v = x[0];
+#pragma unroll
+    for (int l = 0; l < NL; l++) mac(l, ts[l * TSTRIDE + shift], v);
+    p = 1;
+  }
+  for (; p + UP <= n; p += UP) {
+    float4 v[UP / 2];
+#pragma unroll
+    for (int i = 0; i < UP / 2; i++) v[i] = *reinterpret_cast<const float4 *>(x + p + 2 * i);
+#pragma unroll
+    for (int i = 0; i < UP / 2; i++)
+#pragma unroll
+      for (int l = 0; l < NL; l++) {
+        const float4 t = *reinterpret_cast<const float4 *>(ts + l * TSTRIDE + shift + p + 2 * i);
+        mac(l, make_float2(t.x, t.y), make_float2(v[i].x, v[i].y));
+        mac(l, make_float2(t.z, t.w), make_float2(v[i].z, v[i].w));
+      }
+  }
+  for (; p < n; p++) {
+    const float2 v = x[p];
+#pragma unroll
+    for (int l = 0; l < NL; l++) mac(l, ts[l * TSTRIDE + shift + p], v);
+  }
+#pragma unroll
+  for (int l = 0; l < NL; l++)
+    if (l < cc.total) o[l] = make_float2(ar[l], ai[l]);
+}
+
 __global__ void __launch_bounds__(CT) k_chunk_contract(const ChunkContract *__restrict__ chunks,
                                                        const float2 *__restrict__ X, long long xstride,
                                                        float2 *__restrict__ partial, int ptot, int nb) {
-  __shared__ float2 xs[CB][CPP];
-  __shared__ float2 ts[8 * NQ][CPP];
+  extern __shared__ float4 ts4[];  // [nl][TSTRIDE] float2
+  float2 *ts = reinterpret_cast<float2 *>(ts4);
   const ChunkContract cc = chunks[blockIdx.x];
-  const int b0 = blockIdx.y * CB;
-  const int tid = threadIdx.x, bp = tid >> 3, lq = tid & 7;
-  float ar[2][NQ], ai[2][NQ];
-#pragma unroll
-  for (int h = 0; h < 2; h++)
-#pragma unroll
-    for (int q = 0; q < NQ; q++) ar[h][q] = ai[h][q] = 0.f;
-  for (int p0 = 0; p0 < cc.npts; p0 += CP) {
-    const int np = min(CP, cc.npts - p0);
-#pragma unroll 4
-    for (int e = tid; e < CB * CP; e += CT) {
-      int bb = e / CP, pp = e - bb * CP;
-      float2 v = make_float2(0.f, 0.f);
-      if (pp < np && b0 + bb < nb) v = X[(long long)(b0 + bb) * xstride + cc.x_off + p0 + pp];
-      xs[bb][pp] = v;
-    }
-    for (int e = tid; e < cc.total * CP; e += CT) {
-      int t = e / CP, pp = e - t * CP;
-      ts[t][pp] = pp < np ? cc.tab[(long long)t * cc.site_npts + p0 + pp] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    for (int pp = 0; pp < np; pp++) {
-      float2 x0 = xs[2 * bp][pp], x1 = xs[2 * bp + 1][pp];
-#pragma unroll
-      for (int q = 0; q < NQ; q++) {
-        if (lq + 8 * q < cc.total) {
-          float2 v = ts[lq + 8 * q][pp];
-          ar[0][q] = fmaf(v.x, x0.x, fmaf(-v.y, x0.y, ar[0][q]));
-          ai[0][q] = fmaf(v.x, x0.y, fmaf(v.y, x0.x, ai[0][q]));
-          ar[1][q] = fmaf(v.x, x1.x, fmaf(-v.y, x1.y, ar[1][q]));
-          ai[1][q] = fmaf(v.x, x1.y, fmaf(v.y, x1.x, ai[1][q]));
-        }
-      }
-    }
-    __syncthreads();
+  const int shift = (int)(cc.x_off & 1);  // X rows are 16-byte aligned (even xstride)
+  const int nl = cc.total <= 8 ? 8 : cc.total <= 18 ? 18 : 32;
+  for (int e = threadIdx.x; e < nl * TSTRIDE; e += blockDim.x) {
+    const int l = e / TSTRIDE, q = e - l * TSTRIDE - shift;
+    ts[e] = l < cc.total && q >= 0 && q < cc.npts ? cc.tab[(long long)l * cc.site_npts + q] : make_float2(0.f, 0.f);
   }
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    int band = b0 + 2 * bp + h;
-    if (band >= nb) continue;
-    float2 *o = partial + (long long)band * ptot + cc.part_off;
-#pragma unroll
-    for (int q = 0; q < NQ; q++) {
-      int t = lq + 8 * q;
-      if (t < cc.total) o[t] = make_float2(ar[h][q], ai[h][q]);
-    }
-  }
+  __syncthreads();
+  const int b = blockIdx.y * CT + threadIdx.x;
+  if (b >= nb) return;
+  const float2 *x = X + (long long)b * xstride + cc.x_off;
+  float2 *o = partial + (long long)b * ptot + cc.part_off;
+  if (nl == 8)
+    chunk_body<8>(cc, ts, shift, x, o);
+  else if (nl == 18)
+    chunk_body<18>(cc, ts, shift, x, o);
+  else
+    chunk_body<32>(cc, ts, shift, x, o);
 }
 
 void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
                            long long xstride, float2 *partial, int ptot, int nb) {
   if (nchunks <= 0 || nb <= 0) return;
-  dim3 grid(nchunks, ceil_div(nb, CB));
-  if (max_total <= 8)
-    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<1><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
-  else if (max_total <= 24)
-    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<3><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
-  else if (max_total <= 32)
-    PAWPY_LAUNCH("sphere_contract", k_chunk_contract<4><<<grid, CT, 0, stream()>>>(chunks, X, xstride, partial, ptot, nb));
-  else
-    throw Error(ERR_UNSUPPORTED, "more than 32 projector channels on one site");
+  if (max_total > 32) throw Error(ERR_UNSUPPORTED, "more than 32 projector channels on one site");
+  PAWPY_REQUIRE(xstride % 2 == 0, "picked-point rows must be 16-byte aligned");
+  const int nl = max_total <= 8 ? 8 : max_total <= 18 ? 18 : 32;
+  const size_t smem = sizeof(float2) * (size_t)nl * TSTRIDE;
+  static size_t conf = 0;
+  if (smem > 48 * 1024 && smem > conf) {
+    PAWPY_CUDA(cudaFuncSetAttribute(k_chunk_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    conf = smem;
+  }
+  dim3 grid(nchunks, ceil_div(nb, CT));
+  PAWPY_LAUNCH("sphere_contract",
+               k_chunk_contract<<<grid, CT, smem, stream()>>>(chunks, X, xstride, partial, ptot, nb));
 }
 
-__global__ void k_chunk_reduce(const float2 *__restrict__ partial, int ptot, const int *__restrict__ col_site,
-                               const int *__restrict__ col_lm, const int *__restrict__ site_ptr,
-                               const int *__restrict__ chunk_off, float2 *__restrict__ P, int Ptot, int nb,
-                               long long band_base) {
-  int o = blockIdx.x * blockDim.x + threadIdx.x;
-  int b = blockIdx.y;
+// P[(band_base + b) * Ptot + o] = sum over the chunks c < n of the column's
+// site of partial[b][first + c * stride] (col = {first, n, stride}), in chunk
+// order. Grid (Ptot / 128, bands).
+__global__ void k_chunk_reduce(const float2 *__restrict__ partial, int ptot, const int4 *__restrict__ col,
+                               float2 *__restrict__ P, int Ptot, int nb, long long band_base) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
   if (o >= Ptot || b >= nb) return;
-  int s = col_site[o], lm = col_lm[o];
-  const float2 *pb = partial + (long long)b * ptot;
+  const int4 c = col[o];
+  const float2 *pb = partial + (long long)b * ptot + c.x;
   float re = 0.f, im = 0.f;
-  for (int e = site_ptr[s]; e < site_ptr[s + 1]; e++) {
-    float2 v = pb[chunk_off[e] + lm];
+  for (int e = 0; e < c.y; e++) {
+    const float2 v = pb[e * c.z];
     re += v.x;
     im += v.y;
   }
   P[(band_base + b) * Ptot + o] = make_float2(re, im);
 }
 
-void launch_chunk_reduce(const float2 *partial, int ptot, const int *col_site, const int *col_lm,
-                         const int *site_ptr, const int *chunk_off, float2 *P, int Ptot, int nb, long long band_base) {
+void launch_chunk_reduce(const float2 *partial, int ptot, const int4 *col, float2 *P, int Ptot, int nb,
+                         long long band_base) {
   if (Ptot <= 0 || nb <= 0) return;
   dim3 grid(ceil_div(Ptot, 128), nb);
-  PAWPY_LAUNCH("sphere_reduce", k_chunk_reduce<<<grid, 128, 0, stream()>>>(partial, ptot, col_site, col_lm,
-                                                                          site_ptr, chunk_off, P, Ptot, nb,
-                                                                          band_base));
+  PAWPY_LAUNCH("sphere_reduce",
+               k_chunk_reduce<<<grid, 128, 0, stream()>>>(partial, ptot, col, P, Ptot, nb, band_base));
 }
 
 }  // namespace pawpy
