@@ -39,6 +39,9 @@ __device__ __forceinline__ bool occupied(int idx, int s, int n, int N) {
   return d < n;
 }
 
+// one lane per line while the line's registers stay moderate
+constexpr int direct_lanes(int n) { return n <= 64 ? 1 : reg::lanes_for(n); }
+
 __device__ __forceinline__ int wrapi(int v, int N) {
   v %= N;
   return v < 0 ? v + N : v;
@@ -154,6 +157,95 @@ __global__ void __launch_bounds__(FT) k_planes_pipe(const float2 *__restrict__ C
   }
 }
 
+// Pass A without the band loop, for occupancy: grid (n1 planes, ceil(nb /
+// BPC) band groups), FT threads split into BPC groups of TPB threads, one band
+// each. A group zeroes the occupied cells of its tile [n2][LD], scatters the
+// plane's coefficients, transforms the occupied rows in place (a lane owns a
+// whole row when T3 = 1, otherwise through a second tile) and then every
+// column straight to H.
+template <int N2, int N3, int T2, int T3>
+__global__ void __launch_bounds__(FT) k_planes_direct(const float2 *__restrict__ C, int Wpad, int nb,
+                                                      const int *__restrict__ pstart, const int *__restrict__ poff,
+                                                      PlaneGeom g, float2 *__restrict__ H) {
+  constexpr int LD = padded(N3), L2 = N2 / T2, L3 = N3 / T3;
+  constexpr int NEED = (N2 * T3 > N3 * T2 ? N2 * T3 : N3 * T2);
+  constexpr int TPB = 32 * ((NEED + 31) / 32) < FT ? 32 * ((NEED + 31) / 32) : FT;
+  constexpr int BPC = FT / TPB;
+  constexpr bool INPLACE = T3 == 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n2 = g.n2;
+  const int grp = threadIdx.x / TPB, gt = threadIdx.x - grp * TPB;
+  float2 *ta = reinterpret_cast<float2 *>(smraw) + grp * (INPLACE ? 1 : 2) * n2 * LD;
+  float2 *tb = INPLACE ? ta : ta + n2 * LD;
+  const int warp = gt >> 5, lane = threadIdx.x & 31, nwg = TPB / 32;
+  const int p = blockIdx.x, b = blockIdx.y * BPC + grp;
+  const bool band_ok = grp < BPC && b < nb;
+  const int s2 = wrapi(g.g2min, N2), s3 = wrapi(g.g3min, N3);
+  const int t0 = pstart[p], cnt = pstart[p + 1] - t0;
+  if (band_ok) {
+    const int occ = n2 * g.n3;
+    for (int e = gt; e < occ; e += TPB) {
+      const int i = e / g.n3, c = e - i * g.n3;
+      ta[i * LD + (s3 + c >= N3 ? s3 + c - N3 : s3 + c)] = make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  if (band_ok) {
+    const float2 *cb = C + (long long)b * Wpad + t0;
+    for (int t = gt; t < cnt; t += TPB) {
+      const int o = poff[t0 + t], row = o / N3, col = o - row * N3;
+      int i = row - s2;
+      i += i < 0 ? N2 : 0;
+      ta[i * LD + col] = cb[t];
+    }
+  }
+  __syncthreads();
+  if (band_ok) {  // third axis, occupied rows
+    constexpr int LPW = 32 / T3;
+    const int h = lane / LPW, c = lane % LPW;
+    for (int g0 = warp * LPW; g0 < n2; g0 += nwg * LPW) {
+      const int i = g0 + c;
+      const bool ok = i < n2;
+      const float2 *rp = ta + (ok ? i : 0) * LD;
+      float2 x[L3];
+#pragma unroll
+      for (int m = 0; m < L3; m++) {
+        const int col = h + T3 * m;
+        x[m] = ok && occupied(col, s3, g.n3, N3) ? rp[col] : make_float2(0.f, 0.f);
+      }
+      reg::line_fft<N3, T3, 1>(x, h);
+      if (ok) {
+        float2 *wp = tb + i * LD + L3 * reg::bitrev(h, T3);
+#pragma unroll
+        for (int k = 0; k < L3; k++) wp[k] = x[k];
+      }
+    }
+  }
+  __syncthreads();
+  if (band_ok) {  // second axis, every column, to H
+    constexpr int LPW = 32 / T2;
+    const int h = lane / LPW, c = lane % LPW;
+    float2 *out = H + ((long long)b * g.n1 + p) * (N2 * N3);
+    for (int g0 = warp * LPW; g0 < N3; g0 += nwg * LPW) {
+      const int col = g0 + c;
+      const bool ok = col < N3;
+      float2 x[L2];
+#pragma unroll
+      for (int m = 0; m < L2; m++) {
+        int i = h + T2 * m - s2;
+        i += i < 0 ? N2 : 0;
+        x[m] = ok && i < n2 ? tb[i * LD + col] : make_float2(0.f, 0.f);
+      }
+      reg::line_fft<N2, T2, 1>(x, h);
+      if (ok) {
+        const int o = L2 * reg::bitrev(h, T2);
+#pragma unroll
+        for (int k = 0; k < L2; k++) out[(o + k) * N3 + col] = x[k];
+      }
+    }
+  }
+}
+
 // Pass B. grid (N2 planes j, G band groups), FT threads: CTA (j, g) transforms
 // the first axis of plane j of bands g, g + G, ... and picks its sphere
 // points. The pick list of plane j is points [plane_first[j],
@@ -244,6 +336,74 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
   }
 }
 
+// Pass B without staging, for occupancy: grid (ceil(nb / BPC) band groups,
+// N2 planes j), FT threads split into BPC groups of TPB = 32 ceil(N3 T1 / 32)
+// threads, one band each; a group loads plane j of its band from H straight
+// into registers (all loads of a lane in flight at once), transforms the
+// first axis into its shared tile [N1][LD] and picks from the flat list
+// through L1 (consecutive CTAs share a plane).
+template <int N1, int N3, int T1>
+__global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ H, int nb, PlaneGeom g,
+                                                     const int *__restrict__ plane_first,
+                                                     const int *__restrict__ cell, const int *__restrict__ xo,
+                                                     const float2 *__restrict__ phase, float2 *__restrict__ X,
+                                                     long long xstride) {
+  constexpr int LD = padded(N3), L1 = N1 / T1;
+  constexpr int TPB = 32 * ((N3 * T1 + 31) / 32) < FT ? 32 * ((N3 * T1 + 31) / 32) : FT;  // threads per band
+  constexpr int BPC = FT / TPB;
+  constexpr int LPW = 32 / T1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int grp = threadIdx.x / TPB, gt = threadIdx.x - grp * TPB;
+  float2 *tile = reinterpret_cast<float2 *>(smraw) + grp * (N1 * LD);
+  const int warp = gt >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * BPC + grp, j = blockIdx.y;
+  const int n1 = g.n1, s1 = wrapi(g.g1min, N1);
+  const int pstride = g.N2 * N3;  // n1 * N2 * N3 < 2^31
+  const bool band_ok = grp < BPC && b < nb;
+  if (band_ok) {
+    const int h = lane / LPW, c = lane % LPW;
+    const float2 *hb = H + ((long long)b * n1 * g.N2 + j) * N3;
+    for (int g0 = warp * LPW; g0 < N3; g0 += (TPB / 32) * LPW) {
+      const int z = g0 + c;
+      const bool ok = z < N3;
+      float2 x[L1];
+#pragma unroll
+      for (int m = 0; m < L1; m++) {
+        int pp = h + T1 * m - s1;
+        pp += pp < 0 ? N1 : 0;
+        x[m] = ok && pp < n1 ? hb[pp * pstride + z] : make_float2(0.f, 0.f);
+      }
+      reg::line_fft<N1, T1, 1>(x, h);
+      if (ok) {
+        float2 *tp = tile + (L1 * reg::bitrev(h, T1)) * LD + z;
+#pragma unroll
+        for (int k = 0; k < L1; k++) tp[k * LD] = x[k];
+      }
+    }
+  }
+  __syncthreads();
+  if (!band_ok) return;
+  const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
+  float2 *xb = X + (long long)b * xstride;
+  for (int q = gt; q < npj; q += TPB) {
+    const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
+    xb[xo[pf + q]] = cmul(tile[xr * LD + z], phase[pf + q]);
+  }
+}
+
+constexpr int direct_bands(int n1, int n3) {
+  return 32 * ((n3 * direct_lanes(n1) + 31) / 32) < FT ? FT / (32 * ((n3 * direct_lanes(n1) + 31) / 32)) : 1;
+}
+constexpr int planes_direct_bands(int n2, int n3) {
+  return 32 * (((n2 * direct_lanes(n3) > n3 * direct_lanes(n2) ? n2 * direct_lanes(n3) : n3 * direct_lanes(n2)) + 31) /
+               32) < FT
+             ? FT / (32 * (((n2 * direct_lanes(n3) > n3 * direct_lanes(n2) ? n2 * direct_lanes(n3)
+                                                                            : n3 * direct_lanes(n2)) +
+                           31) /
+                          32))
+             : 1;
+}
+
 // ------------------------------------------------------------------ host helpers
 
 namespace fftfast {
@@ -252,6 +412,12 @@ constexpr size_t kSmemCap = 200 * 1024;
 
 inline size_t planes_smem(const PlaneGeom &g) {
   return sizeof(float2) * (2 * (size_t)g.n2 * padded(g.N3) + 2 * (size_t)g.maxcnt) + sizeof(int) * (size_t)g.maxcnt;
+}
+inline size_t planes_direct_smem(const PlaneGeom &g, int bpc, bool inplace) {
+  return sizeof(float2) * (size_t)bpc * (inplace ? 1 : 2) * g.n2 * padded(g.N3);
+}
+inline size_t xpick_direct_smem(const PlaneGeom &g, int bpc) {
+  return sizeof(float2) * (size_t)bpc * g.N1 * padded(g.N3);
 }
 inline size_t xpick_smem(const PlaneGeom &g, int pts_cap = 0) {
   return sizeof(float2) * (2 * (size_t)g.n1 * g.N3 + (size_t)g.N1 * padded(g.N3)) + 16 * (size_t)pts_cap;
@@ -302,8 +468,18 @@ inline int tune(const std::tuple<int, int, int, int> &key, const std::vector<int
       best = cands[i];
     }
   }
-  for (auto &e : ev) cudaEventDestroy(e);
   tuned()[key] = best;
+  if (getenv("PAWPY_GPU_TUNE_VERBOSE")) {
+    fprintf(stderr, "pawpy tune pass %d grid %dx%dx%d:", std::get<0>(key), std::get<1>(key), std::get<2>(key),
+            std::get<3>(key));
+    for (size_t i = 0; i < cands.size(); i++) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      fprintf(stderr, " %d:%.4f", cands[i], ms);
+    }
+    fprintf(stderr, " -> %d\n", best);
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
   return best;
 }
 

@@ -8,9 +8,23 @@ namespace {
 using PickFn = void (*)(const float2 *, int, PlaneGeom, const int *, const int *, const int *, const float2 *, int,
                        float2 *, long long);
 
+using DirectFn = void (*)(const float2 *, int, PlaneGeom, const int *, const int *, const int *, const float2 *,
+                         float2 *, long long);
+
 PickFn find_pick(int n1, int n3) {
 #define X(a, b) \
   if (n1 == a && n3 == b) return k_xpick_pipe<a, b>;
+  PAWPY_FFT_PAIRS(X)
+#undef X
+  return nullptr;
+}
+
+DirectFn find_direct(int n1, int n3, int *bpc) {
+#define X(a, b)                     \
+  if (n1 == a && n3 == b) {         \
+    *bpc = direct_bands(a, b);      \
+    return k_xpick_direct<a, b, direct_lanes(a)>; \
+  }
   PAWPY_FFT_PAIRS(X)
 #undef X
   return nullptr;
@@ -37,13 +51,24 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   allow_smem((const void *)fn, smem);
   const int waves = resident_ctas((const void *)fn, smem);
   const float2 *ph = pl.phase + (long long)kq * pl.npts;
+  int bpc = 1;
+  DirectFn dfn = find_direct(g.N1, g.N3, &bpc);
+  const size_t dsmem = xpick_direct_smem(g, bpc);
+  allow_smem((const void *)dfn, dsmem);
+  // candidates: 1, 2, 4 band groups per plane of the pipelined kernel; 0 the direct kernel
   auto run = [&](int mult) {
+    if (mult == 0) {
+      dim3 grid(ceil_div(nb, bpc), g.N2);
+      PAWPY_LAUNCH("fft_x_pick", dfn<<<grid, FT, dsmem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, X,
+                                                                    xstride));
+      return;
+    }
     const int G = std::max(1, std::min(nb, ceil_div((long long)waves * mult, g.N2)));
     dim3 grid(g.N2, G);
     PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, cap, X,
                                                                 xstride));
   };
-  int mult = tune(std::make_tuple(1, g.N1, g.N2, g.N3), {1, 2, 4}, run);
+  int mult = tune(std::make_tuple(1, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
   run(mult);
 }
 
