@@ -479,7 +479,15 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
   DevBuf<SegFill> segs_d(std::max(1, S.nseg));
   segs_d.upload(S.segs.data(), S.nseg);
   double wscale = vol / N[0] / N[1] / N[2] * std::pow(vol, -0.5);
-  launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, Ld.p, Nd.p, wscale, kcd.p, S.nkp, pt, S.idx.p,
+  // half the smallest lattice-plane spacing: a point nearer its site than this has the
+  // unwrapped box displacement as its unique minimum image
+  double hmin = 1e300;
+  for (int a = 0; a < 3; a++) {
+    const double *u = lat + 3 * ((a + 1) % 3), *v = lat + 3 * ((a + 2) % 3);
+    double c[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+    hmin = std::min(hmin, 0.5 * std::fabs(vol) / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+  }
+  launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, Ld.p, Nd.p, wscale, hmin, kcd.p, S.nkp, pt, S.idx.p,
                   S.tab.p, S.phase.p);
   sync();
 }

@@ -107,8 +107,9 @@ struct ChunkContract {
 void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, const double *lattice,
                        const int *fftg, int *counts);
 // pass 2: compact and tabulate every non-empty slab (FP64, stored complex64)
+// hmin: half the smallest lattice-plane spacing (points nearer their site skip the image search)
 void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
-                     const double *lattice, const int *fftg, double wscale, const double *kcart, int nkp,
+                     const double *lattice, const int *fftg, double wscale, double hmin, const double *kcart, int nkp,
                      long long total_pts, int *idx, float2 *tab, float2 *phase);
 // x-axis transform of each plane j of nb bands, then X[b][x_off + p] = u(point p) exp(i k.path_p) for
 // the segments of plane j (segs sorted by plane; plane_start[N2+1])

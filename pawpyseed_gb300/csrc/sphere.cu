@@ -81,7 +81,8 @@ void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, con
 // tabulate them (double precision, rounded to complex64 at the end).
 __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__restrict__ segs,
                            const SpeciesDev *__restrict__ species, const double *__restrict__ Lg,
-                           const int *__restrict__ Ng, double wscale, const double *__restrict__ kcart, int nkp,
+                           const int *__restrict__ Ng, double wscale, double hmin,
+                           const double *__restrict__ kcart, int nkp,
                            long long total_pts, int *__restrict__ idx, float2 *__restrict__ tab,
                            float2 *__restrict__ phase) {
   __shared__ int warp_cnt[32];
@@ -115,23 +116,28 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
       int jj = ((ijk[1] % N[1]) + N[1]) % N[1];
       int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
       idx[sg.pt_off + pos] = ii * N[2] + kk;
-      // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73)
-      double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
-      double t[3] = {0, 0, 0}, r = INFINITY;
-      for (int a = -1; a <= 1; a++)
-        for (int b = -1; b <= 1; b++)
-          for (int c = -1; c <= 1; c++) {
-            double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
-            double v[3];
-            s_to_cart(f, L, v);
-            double dd = s_norm(v);
-            if (dd < r) {
-              r = dd;
-              t[0] = v[0];
-              t[1] = v[1];
-              t[2] = v[2];
+      // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73):
+      // nearer than hmin, the unwrapped box displacement is the unique minimum image;
+      // otherwise search the 27 images
+      double t[3] = {path[0], path[1], path[2]}, r = s_norm(path);
+      if (!(r < hmin)) {
+        double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
+        r = INFINITY;
+        for (int a = -1; a <= 1; a++)
+          for (int b = -1; b <= 1; b++)
+            for (int c = -1; c <= 1; c++) {
+              double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
+              double v[3];
+              s_to_cart(f, L, v);
+              double dd = s_norm(v);
+              if (dd < r) {
+                r = dd;
+                t[0] = v[0];
+                t[1] = v[1];
+                t[2] = v[2];
+              }
             }
-          }
+      }
       // Y_lm(theta, phi) of the displacement t without transcendental calls:
       // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
       // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
@@ -186,11 +192,15 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
         tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] =
             make_float2((float)(y * cs), (float)(-y * sn));
       }
+      // exp(i k.path): the argument in units of pi reduced to [-1, 1] in double precision,
+      // then the single-precision sincospi (the phase is stored in single precision)
       for (int kq = 0; kq < nkp; kq++) {
         double kr = kcart[3 * kq] * path[0] + kcart[3 * kq + 1] * path[1] + kcart[3 * kq + 2] * path[2];
-        double sn, cs;
-        sincos(kr, &sn, &cs);
-        phase[(long long)kq * total_pts + sg.pt_off + pos] = make_float2((float)cs, (float)sn);
+        double u = kr * 0.31830988618379067154;  // 1 / pi
+        u -= 2.0 * rint(0.5 * u);
+        float sn, cs;
+        sincospif((float)u, &sn, &cs);
+        phase[(long long)kq * total_pts + sg.pt_off + pos] = make_float2(cs, sn);
       }
     }
     __syncthreads();
@@ -200,11 +210,11 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
 }
 
 void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
-                     const double *lattice, const int *fftg, double wscale, const double *kcart, int nkp,
+                     const double *lattice, const int *fftg, double wscale, double hmin, const double *kcart, int nkp,
                      long long total_pts, int *idx, float2 *tab, float2 *phase) {
   if (nseg <= 0) return;
   PAWPY_LAUNCH("sphere_fill", k_seg_fill<<<nseg, 128, 0, stream()>>>(sites, segs, species, lattice, fftg, wscale,
-                                                                    kcart, nkp, total_pts, idx, tab, phase));
+                                                                    hmin, kcart, nkp, total_pts, idx, tab, phase));
 }
 
 // ---------------------------------------------------------------------------
