@@ -281,6 +281,9 @@ pswf_t *pawpy_gpu_wavefunction_from_arrays(int nspin, int nwk, int nband, double
                                            const double *energies, const double *occs);
 /* Frees a pswf_t and everything attached to it (also releases its device copy). */
 void pawpy_gpu_free_pswf(pswf_t *wf);
+/* Frees an element array returned by get_projector_list that was not handed
+ * to setup_projections (free_ppot_list, utils.h:248, under a library name). */
+void pawpy_gpu_free_ppot_list(ppot_t *pps, int length);
 /* Releases the device copy of a wavefunction (call before a foreign free). */
 void pawpy_gpu_release(pswf_t *wf);
 /* Makes the device copy of a wavefunction's coefficients resident now. */

@@ -46,6 +46,7 @@ def _declare(L):
                                                     _ip, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                                     _dp, _dp]
     L.pawpy_gpu_free_pswf.argtypes = [_wfp]
+    L.pawpy_gpu_free_ppot_list.argtypes = [_ppp, C.c_int]
     L.pawpy_gpu_release.argtypes = [_wfp]
     L.pawpy_gpu_upload.argtypes = [_wfp]
     L.pawpy_gpu_upload.restype = C.c_int

@@ -146,6 +146,42 @@ static bool fingerprint_ok(const DevWF &d, const pswf_t *wf) {
          d.cs0 == (const void *)wf->kpts[0]->bands[0]->Cs;
 }
 
+// perm = plane-wave indices in (g1, g2, g3) order. The vectors are distinct
+// points of a small box, so one pass over the box's cells orders them (a
+// comparison sort is the fallback for a sparse box).
+static void sort_gvectors(const int *G, int W, std::vector<int> &perm) {
+  perm.resize(W);
+  if (W == 0) return;
+  int lo[3] = {G[0], G[1], G[2]}, hi[3] = {G[0], G[1], G[2]};
+  for (int t = 1; t < W; t++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::min(lo[a], G[3 * t + a]);
+      hi[a] = std::max(hi[a], G[3 * t + a]);
+    }
+  const long long s1 = hi[1] - lo[1] + 1, s2 = hi[2] - lo[2] + 1;
+  const long long cells = (long long)(hi[0] - lo[0] + 1) * s1 * s2;
+  std::vector<int> cell;
+  bool distinct = cells <= 16LL * W + 4096;
+  if (distinct) {
+    cell.assign((size_t)cells, -1);
+    for (int t = 0; t < W && distinct; t++) {
+      long long key = ((long long)(G[3 * t] - lo[0]) * s1 + (G[3 * t + 1] - lo[1])) * s2 + (G[3 * t + 2] - lo[2]);
+      if (cell[key] >= 0) distinct = false;
+      cell[key] = t;
+    }
+  }
+  if (distinct) {
+    int n = 0;
+    for (long long c = 0; c < cells; c++)
+      if (cell[c] >= 0) perm[n++] = cell[c];
+    return;
+  }
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [G](int a, int b) {
+    return std::tie(G[3 * a], G[3 * a + 1], G[3 * a + 2]) < std::tie(G[3 * b], G[3 * b + 1], G[3 * b + 2]);
+  });
+}
+
 static DevWF &mirror(pswf_t *wf) {
   PAWPY_REQUIRE(wf != nullptr, "wavefunction pointer is NULL");
   PAWPY_REQUIRE(!wf->is_ncl, "noncollinear wavefunctions are not supported by the projection path");
@@ -176,11 +212,8 @@ static DevWF &mirror(pswf_t *wf) {
     q.Wpad = (q.W + 15) / 16 * 16;
     for (int a = 0; a < 3; a++) q.kfrac[a] = kp->k[a];
     q.perm.resize(q.W);
-    std::iota(q.perm.begin(), q.perm.end(), 0);
     const int *G = kp->Gs;
-    std::stable_sort(q.perm.begin(), q.perm.end(), [G](int a, int b) {
-      return std::tie(G[3 * a], G[3 * a + 1], G[3 * a + 2]) < std::tie(G[3 * b], G[3 * b + 1], G[3 * b + 2]);
-    });
+    sort_gvectors(G, q.W, q.perm);
     q.invperm.resize(q.W);
     for (int t = 0; t < q.W; t++) q.invperm[q.perm[t]] = t;
     q.gsorted.resize(3 * (size_t)q.W);
@@ -1214,7 +1247,7 @@ int pawpy_gpu_upload(pswf_t *wf) {
 ppot_t *get_projector_list(int num_els, int *labels, int *ls, double *wave_grids, double *projectors,
                            double *aewaves, double *pswaves, double *rmaxs, double grid_encut) {
   PAWPY_API_BEGIN
-  return device_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
+  return cached_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
   PAWPY_API_END(nullptr)
 }
 
@@ -1305,9 +1338,14 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
                ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
   DevBuf<float2> Smat((size_t)nk * S.nband * R.nband);
   overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p);
-  DevBuf<double2> o64(Smat.n);
-  launch_to_host_layout(Smat.p, nk, S.nband, R.nband, o64.p);
-  o64.download(reinterpret_cast<double2 *>(out), o64.n);
+  if (pageable_access()) {
+    // the device writes the caller's (pageable) array through the host page tables
+    launch_to_host_layout(Smat.p, nk, S.nband, R.nband, reinterpret_cast<double2 *>(out));
+  } else {
+    DevBuf<double2> o64(Smat.n);
+    launch_to_host_layout(Smat.p, nk, S.nband, R.nband, o64.p);
+    o64.download(reinterpret_cast<double2 *>(out), o64.n);
+  }
   sync();
   return 0;
   PAWPY_API_END(pawpy_gpu_last_error())

@@ -29,6 +29,11 @@ double spline_integral(const double *x, const double *y, const double *b, const 
 double interp_log(double r, int n, const double *x, const double *f, double *const *s);
 // w with spline_integral(x, y, spline(y)) = sum_i w_i y_i (the integral is linear in y)
 void spline_integral_weights(const double *x, int n, double *w);
+// get_projector_list served from a cache of earlier results with identical
+// inputs (a deep copy the caller owns), computed by device_projector_list otherwise
+ppot_t *cached_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
+                              const double *projectors, const double *aewaves, const double *pswaves,
+                              const double *rmaxs, double grid_encut);
 // get_projector_list on the device (radial.cu)
 ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
                               const double *projectors, const double *aewaves, const double *pswaves,

@@ -302,6 +302,12 @@ void free_ppot_array(ppot_t *pps, int n) {
   std::free(pps);
 }
 
+}  // namespace pawpy
+
+extern "C" void pawpy_gpu_free_ppot_list(ppot_t *pps, int length) { pawpy::free_ppot_array(pps, length); }
+
+namespace pawpy {
+
 void free_pswf_all(pswf_t *wf) {
   if (!wf) return;
   for (int i = 0; wf->kpts && i < wf->nwk * wf->nspin; i++) {

@@ -13,6 +13,9 @@
 // layout and ownership (the ABI returns host structs).
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <mutex>
+
 #include <cmath>
 #include <cstdlib>
 #include <map>
@@ -422,6 +425,142 @@ static double **new_spline3(const double *x, const double *y, int n) {
   }
   spline_coeffs(x, y, n, s[0], s[1], s[2]);
   return s;
+}
+
+// ---- results of get_projector_list by exact input, returned as deep copies
+
+namespace {
+
+template <typename T>
+T *dup_array(const T *src, size_t n) {
+  if (!src) return nullptr;
+  T *d = static_cast<T *>(std::malloc(sizeof(T) * std::max<size_t>(1, n)));
+  if (!d) throw std::bad_alloc();
+  std::memcpy(d, src, sizeof(T) * n);
+  return d;
+}
+
+double **dup_spline(double *const *s, int n) {
+  if (!s) return nullptr;
+  double **d = static_cast<double **>(std::calloc(3, sizeof(double *)));
+  if (!d) throw std::bad_alloc();
+  for (int q = 0; q < 3; q++) d[q] = dup_array(s[q], (size_t)n);
+  return d;
+}
+
+// deep copy of an element array made by device_projector_list (every pointer it sets)
+ppot_t *copy_ppot_array(const ppot_t *src, int n) {
+  ppot_t *pps = static_cast<ppot_t *>(std::calloc(n, sizeof(ppot_t)));
+  if (!pps) throw std::bad_alloc();
+  try {
+    for (int e = 0; e < n; e++) {
+      const ppot_t &a = src[e];
+      ppot_t &b = pps[e];
+      b = a;
+      b.funcs = nullptr;
+      b.pspw_overlap_matrix = b.aepw_overlap_matrix = b.diff_overlap_matrix = nullptr;
+      b.wave_grid = b.kwave_grid = b.proj_grid = b.smooth_grid = b.dense_kgrid = nullptr;
+      const int ng = a.wave_gridsize, nd = a.proj_gridsize, np = a.num_projs;
+      b.wave_grid = dup_array(a.wave_grid, ng);
+      b.kwave_grid = dup_array(a.kwave_grid, ng);
+      b.proj_grid = dup_array(a.proj_grid, nd);
+      b.smooth_grid = dup_array(a.smooth_grid, nd);
+      b.pspw_overlap_matrix = dup_array(a.pspw_overlap_matrix, (size_t)np * np);
+      b.aepw_overlap_matrix = dup_array(a.aepw_overlap_matrix, (size_t)np * np);
+      b.diff_overlap_matrix = dup_array(a.diff_overlap_matrix, (size_t)np * np);
+      b.funcs = static_cast<funcset_t *>(std::calloc(np, sizeof(funcset_t)));
+      if (!b.funcs) throw std::bad_alloc();
+      for (int k = 0; k < np; k++) {
+        const funcset_t &f = a.funcs[k];
+        funcset_t &g = b.funcs[k];
+        g.l = f.l;
+        g.proj = dup_array(f.proj, nd);
+        g.proj_spline = dup_spline(f.proj_spline, nd);
+        g.aewave = dup_array(f.aewave, ng);
+        g.aewave_spline = dup_spline(f.aewave_spline, ng);
+        g.pswave = dup_array(f.pswave, ng);
+        g.pswave_spline = dup_spline(f.pswave_spline, ng);
+        g.diffwave = dup_array(f.diffwave, ng);
+        g.diffwave_spline = dup_spline(f.diffwave_spline, ng);
+        g.kwave = dup_array(f.kwave, ng);
+        g.kwave_spline = dup_spline(f.kwave_spline, ng);
+        g.smooth_diffwave = dup_array(f.smooth_diffwave, nd);
+        g.smooth_diffwave_spline = dup_spline(f.smooth_diffwave_spline, nd);
+      }
+    }
+  } catch (...) {
+    free_ppot_array(pps, n);
+    throw;
+  }
+  return pps;
+}
+
+struct ListCache {
+  std::mutex mu;
+  std::vector<std::pair<std::vector<unsigned char>, ppot_t *>> entries;  // (inputs, master copy)
+  std::vector<int> counts;                                               // elements of each entry
+};
+ListCache &list_cache() {
+  static ListCache c;
+  return c;
+}
+
+void append_bytes(std::vector<unsigned char> &k, const void *p, size_t n) {
+  const unsigned char *c = static_cast<const unsigned char *>(p);
+  k.insert(k.end(), c, c + n);
+}
+
+}  // namespace
+
+ppot_t *cached_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
+                              const double *projectors, const double *aewaves, const double *pswaves,
+                              const double *rmaxs, double grid_encut) {
+  PAWPY_REQUIRE(num_els > 0 && labels && ls && wave_grids && projectors && aewaves && pswaves && rmaxs,
+                "get_projector_list: missing input array");
+  long npt = 0, ngt = 0, ndp = 0, ngp = 0;
+  for (int e = 0; e < num_els; e++) {
+    const long np = labels[4 * e + 1], nd = labels[4 * e + 2], ng = labels[4 * e + 3];
+    PAWPY_REQUIRE(np >= 1 && nd >= 3 && ng >= 3, "get_projector_list: bad element dimensions");
+    npt += np;
+    ngt += ng;
+    ndp += np * nd;
+    ngp += np * ng;
+  }
+  std::vector<unsigned char> key;
+  key.reserve(sizeof(int) * (4 * num_els + npt) + sizeof(double) * (ngt + ndp + 2 * ngp + num_els + 1) + 8);
+  append_bytes(key, &num_els, sizeof(int));
+  append_bytes(key, labels, sizeof(int) * 4 * (size_t)num_els);
+  append_bytes(key, ls, sizeof(int) * (size_t)npt);
+  append_bytes(key, wave_grids, sizeof(double) * (size_t)ngt);
+  append_bytes(key, projectors, sizeof(double) * (size_t)ndp);
+  append_bytes(key, aewaves, sizeof(double) * (size_t)ngp);
+  append_bytes(key, pswaves, sizeof(double) * (size_t)ngp);
+  append_bytes(key, rmaxs, sizeof(double) * (size_t)num_els);
+  append_bytes(key, &grid_encut, sizeof(double));
+  ListCache &c = list_cache();
+  {
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (auto &en : c.entries)
+      if (en.first == key) return copy_ppot_array(en.second, num_els);
+  }
+  ppot_t *master = device_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs,
+                                         grid_encut);
+  ppot_t *out = nullptr;
+  try {
+    out = copy_ppot_array(master, num_els);
+  } catch (...) {
+    free_ppot_array(master, num_els);
+    throw;
+  }
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (c.entries.size() >= 16) {  // oldest first out
+    free_ppot_array(c.entries.front().second, c.counts.front());
+    c.entries.erase(c.entries.begin());
+    c.counts.erase(c.counts.begin());
+  }
+  c.entries.emplace_back(std::move(key), master);
+  c.counts.push_back(num_els);
+  return out;
 }
 
 ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,

@@ -255,3 +255,35 @@ def test_register_fft_matches_shared_memory_fft(name, workload_dirs, monkeypatch
     basis2, wf2 = load(workload_dirs(name))
     slow = Projector(wf2, basis2).project_all()
     assert np.abs(fast - slow).max() <= 1e-6
+
+
+def test_projector_list_cache_returns_independent_copies():
+    """A repeated get_projector_list with identical inputs returns an equal deep copy."""
+    from pawpyseed_gb300 import _lib, synth, vaspio
+    from pawpyseed_gb300.wavefunction import pack_species
+
+    cr = vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
+    L = _lib.lib()
+    args = pack_species(cr)
+    p1 = L.get_projector_list(len(cr.pps), *args, 300.0)
+    _lib.check()
+    p2 = L.get_projector_list(len(cr.pps), *args, 300.0)
+    _lib.check()
+    try:
+        for e in range(len(cr.pps)):
+            a, b = p1[e], p2[e]
+            ng, nd, np_ = a.wave_gridsize, a.proj_gridsize, a.num_projs
+            assert (ng, nd, np_) == (b.wave_gridsize, b.proj_gridsize, b.num_projs)
+            assert C.addressof(a.funcs.contents) != C.addressof(b.funcs.contents)
+            for k in range(np_):
+                for name, n in (("kwave", ng), ("smooth_diffwave", nd), ("proj", nd)):
+                    va = np.ctypeslib.as_array(getattr(a.funcs[k], name), shape=(n,))
+                    vb = np.ctypeslib.as_array(getattr(b.funcs[k], name), shape=(n,))
+                    assert np.array_equal(va, vb)
+                    assert va.ctypes.data != vb.ctypes.data
+            ma = np.ctypeslib.as_array(a.diff_overlap_matrix, shape=(np_ * np_,))
+            mb = np.ctypeslib.as_array(b.diff_overlap_matrix, shape=(np_ * np_,))
+            assert np.array_equal(ma, mb)
+    finally:
+        L.pawpy_gpu_free_ppot_list(p1, len(cr.pps))
+        L.pawpy_gpu_free_ppot_list(p2, len(cr.pps))
