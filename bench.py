@@ -243,7 +243,8 @@ def run_ours(args, rank, world, local, pg):
 
     result = dict(pairs_per_step=pairs, ms=ms_step, value=value, e2e_ms=e2e_step, e2e_value=e2e_value,
                   h2d=h2d, d2h=d2h, launches=launches // args.steps, clocks=clk, roofline=roof,
-                  kernel_ms={k: v[0] for k, v in stats.items()})
+                  kernel_ms={k: v[0] for k, v in stats.items() if not k.startswith("host.")},
+                  host_ms={k[5:]: v[0] for k, v in stats.items() if k.startswith("host.")})
     # correctness spot check of this run against itself being finite
     if not np.all(np.isfinite(out)):
         raise RuntimeError("non-finite overlaps")
@@ -275,6 +276,8 @@ def roofline(stats, w, basis, wf, lists, cr):
         return None
     fams = {}
     for name, (ms, n) in stats.items():
+        if name.startswith("host."):
+            continue
         key = "fft" if name.startswith("fft") else name
         a = fams.setdefault(key, [0.0, 0, []])
         a[0] += ms
@@ -413,7 +416,7 @@ def main():
                     e2e=dict(value=res["e2e_value"], unit="pairs/s", ms_per_step=res["e2e_ms"],
                              h2d_bytes_per_step=res["h2d"], d2h_bytes_per_step=res["d2h"]),
                     gpu_launches=res["launches"], roofline=res["roofline"], cpu_baseline=cpu,
-                    clocks=res["clocks"], kernel_ms=res["kernel_ms"])
+                    clocks=res["clocks"], kernel_ms=res["kernel_ms"], host_ms=res["host_ms"])
         print(json.dumps(line))
 
 

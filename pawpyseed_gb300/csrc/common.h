@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -69,7 +70,13 @@ void clear_error();
 // The single stream every kernel and copy of the library is ordered on.
 cudaStream_t stream();
 int device();
+// Waits for the library stream; throws if a device status word read back
+// since the last sync (status_readback) is nonzero.
 void sync();
+// A zeroed device status word (ordered on the stream) for one kernel, and the
+// asynchronous read-back that the next sync() checks.
+int *device_status();
+void status_readback(int *dev_slot, const char *what);
 
 // Stream-ordered device allocation (cudaMallocAsync from the device's default
 // pool, whose release threshold is raised so that memory is reused between
@@ -121,6 +128,22 @@ void launch_end(const char *family);
 void check_launch(const char *what);
 // Counts launches made outside PAWPY_LAUNCH (no events, no allocation).
 void note_launches(int n);
+
+// Host-side phases: while profiling is on, the wall time of a scope is added
+// to the family "host.<name>" beside the kernel families.
+bool profiling();
+void host_time(const char *name, double ms);
+struct HostPhase {
+  const char *name;
+  bool on;
+  std::chrono::steady_clock::time_point t0;
+  explicit HostPhase(const char *n) : name(n), on(profiling()) {
+    if (on) t0 = std::chrono::steady_clock::now();
+  }
+  ~HostPhase() {
+    if (on) host_time(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
+};
 
 // PAWPY_LAUNCH("family", kernel<<<grid, block, smem, pawpy::stream()>>>(args));
 #define PAWPY_LAUNCH(family, ...)                                                 \

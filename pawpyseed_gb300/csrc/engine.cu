@@ -192,6 +192,7 @@ static DevWF &mirror(pswf_t *wf) {
     it = g_wfs.end();
   }
   if (it != g_wfs.end()) return *it->second;
+  HostPhase hp("mirror");
   auto d = std::make_unique<DevWF>();
   d->wf = wf;
   d->nspin = wf->nspin;
@@ -246,6 +247,7 @@ static int pageable_access() {
 // each band is copied with cudaMemcpyAsync and permuted on the device.
 static void ensure_coeffs(DevWF &d) {
   if (d.c_ready) return;
+  HostPhase hp("upload");
   size_t total = 0;
   for (auto &q : d.kp) total += (size_t)d.nband * q.Wpad;
   d.C.alloc(total);
@@ -264,7 +266,7 @@ static void ensure_coeffs(DevWF &d) {
       inv.upload(q.invperm.data(), q.W);
       launch_load_host_bands(hpd.p + (size_t)k * d.nband, q.W, inv.p, d.C.p + q.c_off, q.Wpad, d.nband);
     }
-    sync();  // the host arrays must stay untouched until the reads are done
+    // the caller's arrays outlive this call, and every entry point synchronises before it returns
     d.c_ready = true;
     return;
   }
@@ -340,6 +342,7 @@ static void ensure_planes(DevWF &d, DevKpt &q) {
 // ============================================================= species / spheres
 
 static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
+  HostPhase hp("species_tables");
   auto t = std::make_unique<SpeciesTables>();
   int nd = pp.proj_gridsize, np = pp.num_projs;
   t->nproj = np;
@@ -413,6 +416,7 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
                           const double *coords, const std::vector<std::unique_ptr<SpeciesTables>> &sp,
                           bool smooth, const double *lat, const int *N, double vol,
                           const std::vector<DevKpt> &kpts, const double *rec) {
+  HostPhase hp("spheres");
   S = SphereSet();
   S.nsites = (int)site_nums.size();
   if (S.nsites == 0) return;
@@ -522,7 +526,6 @@ static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const
   }
   launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, Ld.p, Nd.p, wscale, hmin, kcd.p, S.nkp, pt, S.idx.p,
                   S.tab.p, S.phase.p);
-  sync();
 }
 
 // One FFT pass over every band of wavefunction d, gathering onto several
@@ -536,6 +539,7 @@ static bool generic_fft_forced() {
 
 static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
                           const std::vector<float2 *> &outs) {
+  HostPhase hp("project_bands");
   ensure_coeffs(d);
   // merged point space (X) over the sets; segments sorted by plane for the pick
   std::vector<GatherSeg> segs;
@@ -702,7 +706,6 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       }
     }
   }
-  sync();
 }
 
 // ============================================================= host projection_t output
@@ -866,6 +869,7 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   }
   // N_RS pair matrices (projector.c:682-719): radial integrals on the device, assembly on the host
   ps.Q.assign(nNRS, {});
+  HostPhase hp_pairs("pair_matrices");
   ps.dcoords.assign(3 * (size_t)nNRS, 0.0);
   {
     std::vector<int> eR(nNRS), eS(nNRS);
@@ -965,6 +969,7 @@ static int choose_splits(int M, int N, int nz, int maxK) {
 // S[k][bS][bR] = <C_R,bR,kR | C_S,bS,k> plus, with B32 given, the augmentation
 // columns (A32 of the pair, B32[k][bS][Kcpad]).
 static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out) {
+  HostPhase hp("overlap_gemm");
   DevWF &R = *ps.R, &S = *ps.S;
   ensure_coeffs(R);
   ensure_coeffs(S);
@@ -1006,7 +1011,6 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   DevBuf<float2> ws;
   if (splits > 1) ws.alloc((size_t)splits * nk * S.nband * R.nband);
   launch_zgemm_f32(db.p, nk, R.nband, S.nband, splits, ws.p);
-  sync();
 }
 
 static void ensure_pseudo(PairState &ps, int flip) {
@@ -1034,6 +1038,7 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
   for (int i = 0; i < 6; i++) key.lists[i] = lists[i];
   key.flip = flip ? 1 : 0;
   if (ps.aug_ready && ps.aug_key == key) return;
+  HostPhase hp("aug_setup");
   PAWPY_REQUIRE(ps.ready, "overlap_setup_real has not been called for this basis/defect pair");
   PAWPY_REQUIRE(lists[2] == ps.N_R && lists[3] == ps.N_S && lists[4] == ps.N_RS_R && lists[5] == ps.N_RS_S,
                 "site lists differ from the ones given to overlap_setup_real");
@@ -1134,7 +1139,6 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
                ps.A32.p);
   ps.aug_key = key;
   ps.aug_ready = true;
-  sync();
 }
 
 static void gather_lists(std::vector<int> lists[6], int num_M, int nNR, int nNS, int nNRS, const int *M_R,
@@ -1254,6 +1258,7 @@ ppot_t *get_projector_list(int num_els, int *labels, int *ls, double *wave_grids
 void setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num_sites, int *fftg, int *labels,
                        double *coords) {
   PAWPY_API_BEGIN
+  HostPhase hp_api("setup_projections");
   do_setup_projections(wf, pps, num_elems, num_sites, fftg, labels, coords);
   PAWPY_API_END()
 }
@@ -1262,6 +1267,7 @@ void overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, int *labels_R, int *labels_S
                         double *coords_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S, int num_N_R, int num_N_S,
                         int num_N_RS) {
   PAWPY_API_BEGIN
+  HostPhase hp_api("overlap_setup_real");
   do_overlap_setup_real(wf_R, wf_S, labels_R, labels_S, coords_R, coords_S, N_R, N_S, N_RS_R, N_RS_S, num_N_R,
                         num_N_S, num_N_RS);
   PAWPY_API_END()
@@ -1326,6 +1332,7 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
                           int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S,
                           int flip_spin) {
   PAWPY_API_BEGIN
+  HostPhase hp_api("pawpy_gpu_project_all");
   PAWPY_REQUIRE(out && wf_R && wf_S, "pawpy_gpu_project_all: NULL argument");
   PairState &ps = pair_state(wf_R, wf_S);
   std::vector<int> lists[6];

@@ -138,7 +138,7 @@ void launch_zgemm_f32(const GemmBatch *batches_dev, int nz, int M, int N, int sp
 // The same grouped contraction on the tensor cores (tc_gemm.cu): split-BF16
 // 3-term (tf32 false) or TF32 operands, FP32 accumulation. hb is the host copy
 // of batches_dev. splits_hint <= 0 picks the K split from the SM count.
-// Synchronises and throws if a pipeline wait of the kernel ran out.
+// A pipeline wait of the kernel that ran out makes the next sync() throw.
 struct TcGemmInfo {
   int splits = 0, Kc = 0, ctas = 0;
 };

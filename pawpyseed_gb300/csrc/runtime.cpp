@@ -95,7 +95,59 @@ int device() {
   return rt().dev;
 }
 
-void sync() { PAWPY_CUDA(cudaStreamSynchronize(stream())); }
+// Device status words: a kernel that can fail without a CUDA error (a wait
+// that ran out) writes a slot; the slot is copied to pinned host memory on the
+// stream and checked at the next sync().
+namespace {
+constexpr int kSlots = 256;
+struct Status {
+  int *dev = nullptr, *host = nullptr;
+  int next = 0;
+  std::vector<std::pair<int, std::string>> pending;
+};
+Status &status_state() {
+  static Status s;
+  return s;
+}
+}  // namespace
+
+int *device_status() {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  init_locked(r);
+  Status &st = status_state();
+  if (!st.dev) {
+    PAWPY_CUDA(cudaMalloc(&st.dev, kSlots * sizeof(int)));
+    PAWPY_CUDA(cudaMallocHost(&st.host, kSlots * sizeof(int)));
+  }
+  int slot = st.next;
+  st.next = (st.next + 1) % kSlots;
+  PAWPY_CUDA(cudaMemsetAsync(st.dev + slot, 0, sizeof(int), r.s));
+  return st.dev + slot;
+}
+
+void status_readback(int *dev_slot, const char *what) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  Status &st = status_state();
+  int slot = (int)(dev_slot - st.dev);
+  PAWPY_CUDA(cudaMemcpyAsync(st.host + slot, dev_slot, sizeof(int), cudaMemcpyDeviceToHost, r.s));
+  st.pending.push_back({slot, what});
+}
+
+void sync() {
+  PAWPY_CUDA(cudaStreamSynchronize(stream()));
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  Status &st = status_state();
+  if (st.pending.empty()) return;
+  std::string msg;
+  for (auto &p : st.pending)
+    if (st.host[p.first] != 0 && msg.empty())
+      msg = p.second + " (status " + std::to_string(st.host[p.first]) + ")";
+  st.pending.clear();
+  if (!msg.empty()) throw Error(ERR_DEVICE_FLAG, msg);
+}
 
 void *dmalloc(size_t bytes) {
   cudaStream_t s = stream();
@@ -146,6 +198,20 @@ void launch_end(const char *family) {
   std::lock_guard<std::recursive_mutex> g(r.mu);
   if (r.profile && !r.pending.empty() && r.pending.back().first == family)
     PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, r.s));
+}
+
+bool profiling() {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  return r.profile;
+}
+
+void host_time(const char *name, double ms) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  auto &f = r.fams[std::string("host.") + name];
+  f.ms += ms;
+  f.n += 1;
 }
 
 void note_launches(int n) {

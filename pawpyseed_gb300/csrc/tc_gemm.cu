@@ -468,6 +468,7 @@ template <bool TF32>
 void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, int splits_hint,
             TcGemmInfo *info) {
   using P = Prec<TF32>;
+  HostPhase hp("tc_gemm");
   const int nz = (int)hb.size();
   int maxK = 0, minkb = 1 << 30;
   std::vector<int> kbl(nz);
@@ -498,22 +499,17 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
 
   DevBuf<float2> ws;
   if (splits > 1) ws.alloc((size_t)splits * nz * N * M);
-  DevBuf<int> st(1);
-  st.zero();
+  int *st = device_status();
   PAWPY_CUDA(cudaFuncSetAttribute(k_tc_zgemm<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM));
   dim3 grid(Mpad / TM, Npad / TN, nz * splits);
   PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
                k_tc_zgemm<TF32><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev.p, M, N, Mpad,
-                                                                       Npad, nz, splits, ws.p, st.p));
+                                                                       Npad, nz, splits, ws.p, st));
   if (splits > 1) {
     dim3 g2(ceil_div((long long)M * N, 256 * 4), nz);
     PAWPY_LAUNCH("gemm_reduce", k_split_reduce<<<g2, 256, 0, stream()>>>(batches_dev, ws.p, M, N, splits, nz));
   }
-  int hs = 0;
-  st.download(&hs, 1);
-  sync();
-  if (hs) throw Error(ERR_DEVICE_FLAG, "tensor-core overlap: a pipeline wait timed out (stage " +
-                                           std::to_string(hs) + ")");
+  status_readback(st, "tensor-core overlap: a pipeline wait timed out");
   if (info) {
     info->splits = splits;
     info->Kc = Kc;
