@@ -308,6 +308,59 @@ int pawpy_gpu_upload(pswf_t *wf);
 int pawpy_gpu_overlap_noalloc(const pawpy_c64 *A, long long lda, const pawpy_c64 *B, long long ldb,
                               int M, int N, int K, pawpy_c64 *out, void *stream);
 
+/* Uploads a wavefunction that setup_projections has seen and computes its
+ * projector coefficients, so that it can serve as a shared, read-only basis
+ * for work on several threads. No counterpart in the reference. Returns 0, or
+ * -1 with the status set. */
+int pawpy_gpu_prepare_basis(pswf_t *wf);
+
+/* Projection server: requests (a defect wavefunction against a resident
+ * basis) run on `slots` worker threads, each on its own CUDA stream, and are
+ * admitted first-in first-out when a worker is free and their estimated device
+ * memory fits the budget. A request's work is the sequence setup_projections,
+ * overlap_setup_real, pawpy_gpu_project_all; the server owns the request's
+ * wavefunction and element array from submission (it frees both) and writes
+ * the nband_S x (nband_R nk) result to `out` before the request completes.
+ * No counterpart in the reference. */
+typedef struct pawpy_gpu_request {
+  int basis;                 /* index from pawpy_gpu_server_add_basis */
+  pswf_t *wf;                /* defect wavefunction (owned by the server) */
+  ppot_t *pps;               /* its element array from get_projector_list (owned by the server) */
+  int num_elems, num_sites;
+  const int *fftg;           /* [3] */
+  const int *labels;         /* [num_sites] */
+  const double *coords;      /* [3 num_sites] fractional */
+  int num_M, num_N_R, num_N_S, num_N_RS;
+  const int *M_R, *M_S, *N_R, *N_S, *N_RS_R, *N_RS_S;
+  pawpy_c128 *out;           /* [nband_S][nband_R nk], kept alive by the caller until completion */
+} pawpy_gpu_request_t;
+
+void *pawpy_gpu_server_create(long long hbm_budget_bytes, int slots);
+/* Registers a basis (setup_projections done; labels and coords of its sites);
+ * prepares it. Returns its index or -1. */
+int pawpy_gpu_server_add_basis(void *server, pswf_t *basis, const int *labels, const double *coords,
+                               int num_sites);
+/* Queues a request (arrays copied); returns its id or -1. */
+long long pawpy_gpu_server_submit(void *server, const pawpy_gpu_request_t *request);
+/* Waits for request id; returns 0 on success or its error code (message in
+ * msg, up to msg_len bytes). times_ms (may be NULL) receives queue, run and
+ * total (submission to completion) milliseconds, and est_bytes the admission
+ * estimate. */
+int pawpy_gpu_server_wait(void *server, long long id, double *times_ms, long long *est_bytes, char *msg,
+                          int msg_len);
+/* Requests completed, running, queued; peak estimated bytes in flight. */
+void pawpy_gpu_server_counts(void *server, long long *done, int *running, int *queued, long long *peak_bytes);
+/* Waits for every request, stops the workers and frees the server. */
+void pawpy_gpu_server_destroy(void *server);
+
+/* Orders the calling thread's library work on a CUDA stream of its own (on = 1)
+ * or on the library's shared stream again (on = 0, after waiting for it), so
+ * that several host threads keep independent work in flight on the device
+ * (different wavefunctions per thread; a basis shared by threads must have
+ * been prepared before, pawpy_gpu_prepare_basis). No counterpart in the
+ * reference. Returns 0, or -1 with the status set. */
+int pawpy_gpu_thread_stream(int on);
+
 /* Device-side timing on the library's stream (CUDA events). */
 void pawpy_gpu_timer_start(void);
 float pawpy_gpu_timer_stop_ms(void); /* synchronizes */

@@ -67,6 +67,22 @@ def _declare(L):
     L.pawpy_gpu_set_precision.argtypes = [C.c_int]
     L.pawpy_gpu_get_precision.restype = C.c_int
     L.pawpy_gpu_set_tc_splits.argtypes = [C.c_int]
+    L.pawpy_gpu_prepare_basis.restype = C.c_int
+    L.pawpy_gpu_prepare_basis.argtypes = [_wfp]
+    L.pawpy_gpu_thread_stream.restype = C.c_int
+    L.pawpy_gpu_thread_stream.argtypes = [C.c_int]
+    L.pawpy_gpu_server_create.restype = C.c_void_p
+    L.pawpy_gpu_server_create.argtypes = [C.c_longlong, C.c_int]
+    L.pawpy_gpu_server_add_basis.restype = C.c_int
+    L.pawpy_gpu_server_add_basis.argtypes = [C.c_void_p, _wfp, _ip, _dp, C.c_int]
+    L.pawpy_gpu_server_submit.restype = C.c_longlong
+    L.pawpy_gpu_server_submit.argtypes = [C.c_void_p, C.POINTER(S.pawpy_gpu_request_t)]
+    L.pawpy_gpu_server_wait.restype = C.c_int
+    L.pawpy_gpu_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_longlong), C.c_char_p, C.c_int]
+    L.pawpy_gpu_server_counts.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+    L.pawpy_gpu_server_destroy.argtypes = [C.c_void_p]
     L.pawpy_gpu_overlap_matrix.restype = C.c_int
     L.pawpy_gpu_overlap_matrix.argtypes = [_cp, _cp, C.c_int, C.c_int, C.c_int, _ip, _cp, C.c_int]
     L.pawpy_gpu_set_host_projections.argtypes = [C.c_int]

@@ -156,4 +156,7 @@ struct HostPhase {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Raises a kernel's dynamic shared-memory limit to at least bytes (thread-safe, once per size).
+void allow_dynamic_smem(const void *kernel, size_t bytes);
+
 }  // namespace pawpy

@@ -865,7 +865,7 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
       outs.push_back(wp);
     }
     if (!sets.empty()) project_bands(W, sets, outs);
-    W.p_ready = true;
+    if (!W.p_ready) W.p_ready = true;  // a prepared, shared basis is only read
   }
   // N_RS pair matrices (projector.c:682-719): radial integrals on the device, assembly on the host
   ps.Q.assign(nNRS, {});
@@ -1233,6 +1233,19 @@ int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int 
   PAWPY_API_END(-1)
 }
 void pawpy_gpu_set_host_projections(int on) { g_host_proj = on != 0; }
+
+int pawpy_gpu_prepare_basis(pswf_t *wf) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("prepare_basis");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(d.tables_ready, "pawpy_gpu_prepare_basis: setup_projections has not been called");
+  ensure_coeffs(d);
+  for (auto &q : d.kp) ensure_planes(d, q);
+  ensure_projections(d);
+  sync();
+  return 0;
+  PAWPY_API_END(-1)
+}
 
 void pawpy_gpu_release(pswf_t *wf) {
   PAWPY_API_BEGIN

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -423,8 +424,15 @@ inline size_t xpick_smem(const PlaneGeom &g, int pts_cap = 0) {
   return sizeof(float2) * (2 * (size_t)g.n1 * g.N3 + (size_t)g.N1 * padded(g.N3)) + 16 * (size_t)pts_cap;
 }
 
+// guards the attribute and tuning caches (host threads may launch concurrently)
+inline std::mutex &cache_mutex() {
+  static std::mutex m;
+  return m;
+}
+
 inline void allow_smem(const void *fn, size_t bytes) {
   static std::map<const void *, size_t> done;
+  std::lock_guard<std::mutex> lk(cache_mutex());
   auto &d = done[fn];
   if (bytes > 48 * 1024 && bytes > d) {
     PAWPY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -446,10 +454,26 @@ inline std::map<std::tuple<int, int, int, int>, int> &tuned() {
   return t;
 }
 
+inline std::mutex &tune_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+// The choice for a key is made once per process (concurrent first callers wait
+// for it), so results never depend on which thread tuned.
 template <typename Launch>
 inline int tune(const std::tuple<int, int, int, int> &key, const std::vector<int> &cands, Launch launch) {
-  auto it = tuned().find(key);
-  if (it != tuned().end()) return it->second;
+  {
+    std::lock_guard<std::mutex> lk(cache_mutex());
+    auto it = tuned().find(key);
+    if (it != tuned().end()) return it->second;
+  }
+  std::lock_guard<std::mutex> tlk(tune_mutex());
+  {
+    std::lock_guard<std::mutex> lk(cache_mutex());
+    auto it = tuned().find(key);
+    if (it != tuned().end()) return it->second;
+  }
   std::vector<cudaEvent_t> ev(cands.size() + 1);
   for (auto &e : ev) PAWPY_CUDA(cudaEventCreate(&e));
   PAWPY_CUDA(cudaEventRecord(ev[0], stream()));
@@ -468,7 +492,10 @@ inline int tune(const std::tuple<int, int, int, int> &key, const std::vector<int
       best = cands[i];
     }
   }
-  tuned()[key] = best;
+  {
+    std::lock_guard<std::mutex> lk(cache_mutex());
+    tuned()[key] = best;
+  }
   if (getenv("PAWPY_GPU_TUNE_VERBOSE")) {
     fprintf(stderr, "pawpy tune pass %d grid %dx%dx%d:", std::get<0>(key), std::get<1>(key), std::get<2>(key),
             std::get<3>(key));

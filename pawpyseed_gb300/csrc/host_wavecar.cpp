@@ -419,6 +419,16 @@ int pawpy_gpu_struct_layout(char *buf, int len) {
   PAWPY_MEMBER(real_proj_site_t, gridsize); PAWPY_MEMBER(real_proj_site_t, rmax); PAWPY_MEMBER(real_proj_site_t, coord);
   PAWPY_MEMBER(real_proj_site_t, indices); PAWPY_MEMBER(real_proj_site_t, paths); PAWPY_MEMBER(real_proj_site_t, projs);
   PAWPY_SIZE(real_proj_site_t);
+  PAWPY_MEMBER(pawpy_gpu_request_t, basis); PAWPY_MEMBER(pawpy_gpu_request_t, wf); PAWPY_MEMBER(pawpy_gpu_request_t, pps);
+  PAWPY_MEMBER(pawpy_gpu_request_t, num_elems); PAWPY_MEMBER(pawpy_gpu_request_t, num_sites);
+  PAWPY_MEMBER(pawpy_gpu_request_t, fftg); PAWPY_MEMBER(pawpy_gpu_request_t, labels);
+  PAWPY_MEMBER(pawpy_gpu_request_t, coords); PAWPY_MEMBER(pawpy_gpu_request_t, num_M);
+  PAWPY_MEMBER(pawpy_gpu_request_t, num_N_R); PAWPY_MEMBER(pawpy_gpu_request_t, num_N_S);
+  PAWPY_MEMBER(pawpy_gpu_request_t, num_N_RS); PAWPY_MEMBER(pawpy_gpu_request_t, M_R);
+  PAWPY_MEMBER(pawpy_gpu_request_t, M_S); PAWPY_MEMBER(pawpy_gpu_request_t, N_R); PAWPY_MEMBER(pawpy_gpu_request_t, N_S);
+  PAWPY_MEMBER(pawpy_gpu_request_t, N_RS_R); PAWPY_MEMBER(pawpy_gpu_request_t, N_RS_S);
+  PAWPY_MEMBER(pawpy_gpu_request_t, out);
+  PAWPY_SIZE(pawpy_gpu_request_t);
   if (buf && len > 0) {
     std::strncpy(buf, out.c_str(), (size_t)len - 1);
     buf[len - 1] = 0;

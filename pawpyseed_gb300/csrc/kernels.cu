@@ -79,11 +79,7 @@ void launch_fft_planes(const float2 *C, int Wpad, const int *plane_start, const 
   if (nb <= 0 || g.n1 <= 0) return;
   size_t smem = sizeof(float2) * (2 * (size_t)g.N2 * g.N3 + g.N2 + g.N3);
   PAWPY_REQUIRE(smem <= 227 * 1024, "FFT plane does not fit in shared memory");
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    PAWPY_CUDA(cudaFuncSetAttribute(k_fft_planes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = smem;
-  }
+  allow_dynamic_smem((const void *)k_fft_planes, smem);
   dim3 grid(g.n1, nb);
   PAWPY_LAUNCH("fft_planes", k_fft_planes<<<grid, 256, smem, stream()>>>(C, Wpad, plane_start, plane_off,
                                                                           g, r2, r3, tw2, tw3, H));

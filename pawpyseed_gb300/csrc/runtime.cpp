@@ -83,7 +83,12 @@ void drain_locked(Runtime &r) {
 }
 }  // namespace
 
+// A thread may order its work on a stream of its own (pawpy_gpu_thread_stream),
+// so that several host threads keep independent work in flight on the device.
+static thread_local cudaStream_t t_stream = nullptr;
+
 cudaStream_t stream() {
+  if (t_stream) return t_stream;
   Runtime &r = rt();
   std::lock_guard<std::recursive_mutex> g(r.mu);
   init_locked(r);
@@ -103,8 +108,8 @@ constexpr int kSlots = 256;
 struct Status {
   int *dev = nullptr, *host = nullptr;
   int next = 0;
-  std::vector<std::pair<int, std::string>> pending;
 };
+thread_local std::vector<std::pair<int, std::string>> t_pending;  // slots read back on this thread's stream
 Status &status_state() {
   static Status s;
   return s;
@@ -122,7 +127,7 @@ int *device_status() {
   }
   int slot = st.next;
   st.next = (st.next + 1) % kSlots;
-  PAWPY_CUDA(cudaMemsetAsync(st.dev + slot, 0, sizeof(int), r.s));
+  PAWPY_CUDA(cudaMemsetAsync(st.dev + slot, 0, sizeof(int), stream()));
   return st.dev + slot;
 }
 
@@ -131,21 +136,19 @@ void status_readback(int *dev_slot, const char *what) {
   std::lock_guard<std::recursive_mutex> g(r.mu);
   Status &st = status_state();
   int slot = (int)(dev_slot - st.dev);
-  PAWPY_CUDA(cudaMemcpyAsync(st.host + slot, dev_slot, sizeof(int), cudaMemcpyDeviceToHost, r.s));
-  st.pending.push_back({slot, what});
+  PAWPY_CUDA(cudaMemcpyAsync(st.host + slot, dev_slot, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  t_pending.push_back({slot, what});
 }
 
 void sync() {
   PAWPY_CUDA(cudaStreamSynchronize(stream()));
-  Runtime &r = rt();
-  std::lock_guard<std::recursive_mutex> g(r.mu);
+  if (t_pending.empty()) return;
   Status &st = status_state();
-  if (st.pending.empty()) return;
   std::string msg;
-  for (auto &p : st.pending)
+  for (auto &p : t_pending)
     if (st.host[p.first] != 0 && msg.empty())
       msg = p.second + " (status " + std::to_string(st.host[p.first]) + ")";
-  st.pending.clear();
+  t_pending.clear();
   if (!msg.empty()) throw Error(ERR_DEVICE_FLAG, msg);
 }
 
@@ -188,7 +191,7 @@ void launch_begin(const char *family) {
   r.launches++;
   if (r.profile) {
     cudaEvent_t a = take_event(r), b = take_event(r);
-    PAWPY_CUDA(cudaEventRecord(a, r.s));
+    PAWPY_CUDA(cudaEventRecord(a, t_stream ? t_stream : r.s));
     r.pending.push_back({family, {a, b}});
   }
 }
@@ -197,7 +200,19 @@ void launch_end(const char *family) {
   Runtime &r = rt();
   std::lock_guard<std::recursive_mutex> g(r.mu);
   if (r.profile && !r.pending.empty() && r.pending.back().first == family)
-    PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, r.s));
+    PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, t_stream ? t_stream : r.s));
+}
+
+void allow_dynamic_smem(const void *kernel, size_t bytes) {
+  static std::mutex m;
+  static std::map<const void *, size_t> done;
+  if (bytes <= 48 * 1024) return;
+  std::lock_guard<std::mutex> lk(m);
+  size_t &d = done[kernel];
+  if (bytes > d) {
+    PAWPY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    d = bytes;
+  }
 }
 
 bool profiling() {
@@ -239,9 +254,23 @@ void pawpy_gpu_clear_error(void) { clear_error(); }
 void pawpy_gpu_timer_start(void) {
   PAWPY_API_BEGIN
   Runtime &r = rt();
-  stream();
-  PAWPY_CUDA(cudaEventRecord(r.t0, r.s));
+  PAWPY_CUDA(cudaEventRecord(r.t0, stream()));
   PAWPY_API_END()
+}
+
+int pawpy_gpu_thread_stream(int on) {
+  PAWPY_API_BEGIN
+  stream();  // the device context and the shared stream exist first
+  if (on && !t_stream) {
+    PAWPY_CUDA(cudaStreamCreateWithFlags(&t_stream, cudaStreamNonBlocking));
+  } else if (!on && t_stream) {
+    cudaStream_t s = t_stream;
+    PAWPY_CUDA(cudaStreamSynchronize(s));
+    t_stream = nullptr;
+    PAWPY_CUDA(cudaStreamDestroy(s));
+  }
+  return 0;
+  PAWPY_API_END(-1)
 }
 
 float pawpy_gpu_timer_stop_ms(void) {

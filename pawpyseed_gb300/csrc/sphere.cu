@@ -254,11 +254,7 @@ void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, c
   if (nb <= 0) return;
   size_t smem = sizeof(float2) * (2 * (size_t)g.N1 * g.N3 + g.N1);
   PAWPY_REQUIRE(smem <= 227 * 1024, "FFT tile does not fit in shared memory");
-  static size_t conf = 0;
-  if (smem > 48 * 1024 && smem > conf) {
-    PAWPY_CUDA(cudaFuncSetAttribute(k_fft_x_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    conf = smem;
-  }
+  allow_dynamic_smem((const void *)k_fft_x_pick, smem);
   dim3 grid(g.N2, nb);
   PAWPY_LAUNCH("fft_x_pick", k_fft_x_pick<<<grid, 256, smem, stream()>>>(H, g, r1, tw1, segs, plane_start, kq, X,
                                                                         xstride));
@@ -356,11 +352,7 @@ void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_tot
   PAWPY_REQUIRE(xstride % 2 == 0, "picked-point rows must be 16-byte aligned");
   const int nl = max_total <= 8 ? 8 : max_total <= 18 ? 18 : 32;
   const size_t smem = sizeof(float2) * (size_t)nl * TSTRIDE;
-  static size_t conf = 0;
-  if (smem > 48 * 1024 && smem > conf) {
-    PAWPY_CUDA(cudaFuncSetAttribute(k_chunk_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    conf = smem;
-  }
+  allow_dynamic_smem((const void *)k_chunk_contract, smem);
   dim3 grid(nchunks, ceil_div(nb, CT));
   PAWPY_LAUNCH("sphere_contract",
                k_chunk_contract<<<grid, CT, smem, stream()>>>(chunks, X, xstride, partial, ptot, nb));

@@ -500,7 +500,7 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
   DevBuf<float2> ws;
   if (splits > 1) ws.alloc((size_t)splits * nz * N * M);
   int *st = device_status();
-  PAWPY_CUDA(cudaFuncSetAttribute(k_tc_zgemm<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM));
+  allow_dynamic_smem((const void *)k_tc_zgemm<TF32>, P::SMEM);
   dim3 grid(Mpad / TM, Npad / TN, nz * splits);
   PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
                k_tc_zgemm<TF32><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev.p, M, N, Mpad,

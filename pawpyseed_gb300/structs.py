@@ -103,8 +103,34 @@ class real_proj_site_t(C.Structure):
     ]
 
 
+class pawpy_gpu_request_t(C.Structure):
+    """A projection request of the library's server (include/pawpy_gpu.h)."""
+
+    _fields_ = [
+        ("basis", C.c_int),
+        ("wf", C.POINTER(pswf_t)),
+        ("pps", C.POINTER(ppot_t)),
+        ("num_elems", C.c_int),
+        ("num_sites", C.c_int),
+        ("fftg", C.c_void_p),
+        ("labels", C.c_void_p),
+        ("coords", C.c_void_p),
+        ("num_M", C.c_int),
+        ("num_N_R", C.c_int),
+        ("num_N_S", C.c_int),
+        ("num_N_RS", C.c_int),
+        ("M_R", C.c_void_p),
+        ("M_S", C.c_void_p),
+        ("N_R", C.c_void_p),
+        ("N_S", C.c_void_p),
+        ("N_RS_R", C.c_void_p),
+        ("N_RS_S", C.c_void_p),
+        ("out", C.c_void_p),
+    ]
+
+
 STRUCTS = [funcset_t, ppot_t, projection_t, band_t, rayleigh_set_t, kpoint_t, pswf_t,
-           real_proj_t, real_proj_site_t]
+           real_proj_t, real_proj_site_t, pawpy_gpu_request_t]
 
 
 def layout_table():

@@ -153,6 +153,10 @@ class Wavefunction:
         _lib.check()
         return Wavefunction(struct, ptr, cr, dim, data["kpts"], kws, 1e-4, setup_projectors)
 
+    def detach(self):
+        """Give up the pswf_t without freeing it (its new owner frees it)."""
+        self._ptr = None
+
     def __del__(self):
         if getattr(self, "_ptr", None):
             try:
