@@ -38,9 +38,17 @@ def parse():
     ap.add_argument("--workload", type=int, default=1)
     ap.add_argument("--bands", type=int, default=None, help="reduced band count (testing only)")
     ap.add_argument("--nk", type=int, default=None, help="reduced k-point count (testing only)")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3", "tf32"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16x3", "tf32"])
     ap.add_argument("--cpu-sample-bands", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", action="store_true",
+                    help="replay the serving stream (Poisson requests against resident bases) instead")
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=200.0, help="mean request arrival rate (1/s)")
+    ap.add_argument("--slots", type=int, default=4, help="requests in flight at once")
+    ap.add_argument("--budget-gb", type=float, default=100.0, help="device-memory admission budget")
+    ap.add_argument("--precision-report", action="store_true",
+                    help="overlap matrix of the workload in every precision against FP64 (error and time)")
     return ap.parse_args()
 
 
@@ -299,7 +307,14 @@ def roofline(stats, w, basis, wf, lists, cr):
     elif fam == "fft":
         nbytes = 16.0 * N3 * wf.nband * nk
         ach = nbytes / secs / 1e9
-        out.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm)
+        out.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm,
+                   algorithmic_bytes_per_band_fft=16.0 * N3)
+        if tuple(w["dim"]) == (60, 60, 60):
+            # DRAM bytes of both passes per band-FFT from one ncu capture of this workload's
+            # launches (profiles/fft_planes_pipe_60cubed.md, launches of 99 bands):
+            # pass A 59.4 MB + pass B 121 MB per 99 bands
+            out.update(traffic=(59.4e6 + 121.4e6) / 99.0,
+                       traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")
     else:
         out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)
     return out
@@ -393,11 +408,90 @@ def config(args, w):
             "precision": args.precision, "l2": "inputs larger than L2 (defect 190 MB, basis 190 MB)"}
 
 
+def run_serve(args, rank, world, local):
+    """Serving form: a seeded Poisson stream against resident 8-, 64- and 216-atom bases.
+
+    Every rank replays its own stream (replicas; seeds differ by rank); rank 0 prints."""
+    import torch
+
+    torch.cuda.set_device(local)
+    from pawpyseed_gb300 import serve
+
+    bases, reqs = serve.poisson_workload(n_requests=args.requests, rate=args.rate, seed=4 + rank)
+    res = serve.run_stream(bases, reqs, slots=args.slots, budget=int(args.budget_gb * (1 << 30)),
+                           precision=args.precision)
+    per_basis = {}
+    for r in res["records"]:
+        per_basis.setdefault(r["basis"], []).append(r["latency_ms"])
+    if rank == 0:
+        line = dict(metric="band-pair projections/sec (served stream)", value=res["pairs_per_s"], unit="pairs/s",
+                    higher_is_better=True, n_gpus=world, p50_ms=res["p50_ms"], p99_ms=res["p99_ms"],
+                    mean_ms=res["mean_ms"], requests=len(reqs), wall_s=res["wall_s"], pairs=res["pairs"],
+                    dtype="c64 (fp32 accumulate) / f64 setup", precision=args.precision,
+                    data="synthetic (seeded VASP-format content)",
+                    config=dict(workload="Poisson %.0f req/s against resident 8-, 64- and 216-atom bases; "
+                                         "1-3 point defects, log-uniform 16-512 bands, the basis k-points"
+                                % args.rate, slots=args.slots, budget_gb=args.budget_gb,
+                                peak_admitted_gb=res["peak_est_bytes"] / (1 << 30)),
+                    p50_ms_by_basis={str(k): float(np.percentile(v, 50)) for k, v in per_basis.items()},
+                    p99_ms_by_basis={str(k): float(np.percentile(v, 99)) for k, v in per_basis.items()})
+        print(json.dumps(line))
+
+
+def run_precision_report(args, local):
+    """Pseudo-overlap matrix <C_R|C_S> of the workload (every k-point) in FP32 (CUDA cores), TF32 and
+    split-BF16 (tensor cores) through pawpy_gpu_overlap_matrix, each against an FP64 evaluation of the
+    same complex64 coefficients (torch complex128 matmul on the device, the checker only)."""
+    import torch
+
+    torch.cuda.set_device(local)
+    from pawpyseed_gb300 import _lib
+
+    w, basis_s, defect_s, cr, bd, dd = make_workload(args.workload, args.bands, args.nk)
+    nk = len(bd["coeffs"])
+    As = [np.ascontiguousarray(c) for c in bd["coeffs"]]
+    Bs = [np.ascontiguousarray(c) for c in dd["coeffs"]]
+    truth = []
+    for a, b in zip(As, Bs):
+        ta = torch.from_numpy(a).to("cuda", torch.complex128)
+        tb = torch.from_numpy(b).to("cuda", torch.complex128)
+        truth.append((tb @ ta.conj().T).cpu().numpy())
+    truth = np.stack(truth)
+    L = _lib.lib()
+    out = {}
+    for prec in ("fp32", "tf32", "bf16x3"):
+        _lib.overlap_matrix(As, Bs, prec)  # warm-up (tuning, allocations)
+        t0 = time.perf_counter()
+        L.pawpy_gpu_timer_start()
+        s = _lib.overlap_matrix(As, Bs, prec)
+        ms = L.pawpy_gpu_timer_stop_ms()
+        err = np.abs(s - truth)
+        out[prec] = dict(max_abs_err=float(err.max()), rms_abs_err=float(np.sqrt((err ** 2).mean())),
+                         call_ms=ms, wall_ms=(time.perf_counter() - t0) * 1e3)
+    # worst case for accumulation bias: the basis against itself (diagonal = 1)
+    self_truth = np.stack([np.ones(a.shape[0]) for a in As])
+    for prec in ("fp32", "tf32", "bf16x3"):
+        s = _lib.overlap_matrix(As, As, prec)
+        d = np.abs(np.stack([np.diag(x) for x in s]) - self_truth)
+        out[prec]["self_diag_max_err"] = float(d.max())
+    W = [a.shape[1] for a in As]
+    print(json.dumps(dict(metric="pseudo-overlap error vs FP64 per precision", workload=args.workload,
+                          nband_R=As[0].shape[0], nband_S=Bs[0].shape[0], nk=nk, W=W, max_abs_overlap=float(
+                              np.abs(truth).max()), variants=out,
+                          note="call_ms includes the host-to-device copy of both coefficient sets")))
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init(args.gpus)
+    if args.precision_report:
+        run_precision_report(args, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
+        return
+    if args.serve:
+        run_serve(args, rank, world, local)
         return
     res, work = run_ours(args, rank, world, local, pg)
     w = work[0]

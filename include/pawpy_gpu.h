@@ -310,9 +310,13 @@ int pawpy_gpu_overlap_noalloc(const pawpy_c64 *A, long long lda, const pawpy_c64
 
 /* Uploads a wavefunction that setup_projections has seen and computes its
  * projector coefficients, so that it can serve as a shared, read-only basis
- * for work on several threads. No counterpart in the reference. Returns 0, or
- * -1 with the status set. */
-int pawpy_gpu_prepare_basis(pswf_t *wf);
+ * for work on several threads. With keep_real_space, its real-space
+ * wavefunctions stay on the device too (nk nband N1 N2 N3 complex64) and
+ * later projections of it onto new sites gather from them instead of
+ * transforming again. No counterpart in the reference. Returns 1 when the
+ * real-space wavefunctions are resident, 0 when not, -1 with the status set on
+ * failure. */
+int pawpy_gpu_prepare_basis(pswf_t *wf, int keep_real_space);
 
 /* Projection server: requests (a defect wavefunction against a resident
  * basis) run on `slots` worker threads, each on its own CUDA stream, and are
@@ -337,15 +341,17 @@ typedef struct pawpy_gpu_request {
 
 void *pawpy_gpu_server_create(long long hbm_budget_bytes, int slots);
 /* Registers a basis (setup_projections done; labels and coords of its sites);
- * prepares it. Returns its index or -1. */
+ * prepares it (pawpy_gpu_prepare_basis with keep_real_space). Returns its
+ * index or -1. */
 int pawpy_gpu_server_add_basis(void *server, pswf_t *basis, const int *labels, const double *coords,
-                               int num_sites);
+                               int num_sites, int keep_real_space);
 /* Queues a request (arrays copied); returns its id or -1. */
 long long pawpy_gpu_server_submit(void *server, const pawpy_gpu_request_t *request);
 /* Waits for request id; returns 0 on success or its error code (message in
- * msg, up to msg_len bytes). times_ms (may be NULL) receives queue, run and
- * total (submission to completion) milliseconds, and est_bytes the admission
- * estimate. */
+ * msg, up to msg_len bytes). times_ms (may be NULL, else 7 values) receives
+ * queue, run and total (submission to completion) milliseconds, then the run's
+ * setup_projections, overlap_setup_real, pawpy_gpu_project_all and release
+ * parts; est_bytes the admission estimate. */
 int pawpy_gpu_server_wait(void *server, long long id, double *times_ms, long long *est_bytes, char *msg,
                           int msg_len);
 /* Requests completed, running, queued; peak estimated bytes in flight. */

@@ -68,13 +68,13 @@ def _declare(L):
     L.pawpy_gpu_get_precision.restype = C.c_int
     L.pawpy_gpu_set_tc_splits.argtypes = [C.c_int]
     L.pawpy_gpu_prepare_basis.restype = C.c_int
-    L.pawpy_gpu_prepare_basis.argtypes = [_wfp]
+    L.pawpy_gpu_prepare_basis.argtypes = [_wfp, C.c_int]
     L.pawpy_gpu_thread_stream.restype = C.c_int
     L.pawpy_gpu_thread_stream.argtypes = [C.c_int]
     L.pawpy_gpu_server_create.restype = C.c_void_p
     L.pawpy_gpu_server_create.argtypes = [C.c_longlong, C.c_int]
     L.pawpy_gpu_server_add_basis.restype = C.c_int
-    L.pawpy_gpu_server_add_basis.argtypes = [C.c_void_p, _wfp, _ip, _dp, C.c_int]
+    L.pawpy_gpu_server_add_basis.argtypes = [C.c_void_p, _wfp, _ip, _dp, C.c_int, C.c_int]
     L.pawpy_gpu_server_submit.restype = C.c_longlong
     L.pawpy_gpu_server_submit.argtypes = [C.c_void_p, C.POINTER(S.pawpy_gpu_request_t)]
     L.pawpy_gpu_server_wait.restype = C.c_int

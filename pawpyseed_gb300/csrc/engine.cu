@@ -74,6 +74,9 @@ struct DevWF {
   std::vector<DevKpt> kp;
   DevBuf<float2> C;
   bool c_ready = false;
+  // resident real-space wavefunctions [k][band][N1][N2][N3] (a prepared basis)
+  DevBuf<float2> grid;
+  bool grid_ready = false;
   // projectors
   int N[3] = {0, 0, 0};
   std::vector<std::unique_ptr<SpeciesTables>> species;
@@ -253,7 +256,7 @@ static void ensure_coeffs(DevWF &d) {
   d.C.alloc(total);
   int maxW = 0;
   for (auto &q : d.kp) maxW = std::max(maxW, q.W);
-  if (pageable_access()) {
+  if (pageable_access() && !getenv("PAWPY_GPU_NO_HOST_READ")) {
     std::vector<const float2 *> hp((size_t)d.nk * d.nband);
     for (int k = 0; k < d.nk; k++)
       for (int b = 0; b < d.nband; b++)
@@ -669,7 +672,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   int cbatch = (int)std::max<long long>(fbatch, std::min<long long>(d.nband, (2LL << 30) / std::max(1LL, per_band)));
   cbatch = std::max(1, cbatch / fbatch) * fbatch;
   cbatch = std::min(cbatch, d.nband);
-  DevBuf<float2> H((size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
+  DevBuf<float2> H(d.grid_ready ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
   DevBuf<float2> X((size_t)cbatch * std::max(1LL, xstride));
   DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
   for (int k = 0; k < d.nk; k++) {
@@ -687,7 +690,12 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       int cn = std::min(cbatch, d.nband - c0);
       for (int b0 = c0; b0 < c0 + cn; b0 += fbatch) {
         int nb = std::min(fbatch, c0 + cn - b0);
-        if (fast) {
+        if (d.grid_ready) {
+          // resident real-space wavefunctions: a gather instead of the transform
+          const size_t n3d = (size_t)d.N[0] * d.N[1] * d.N[2];
+          launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k,
+                           X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
+        } else if (fast) {
           launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p,
                                  g, H.p, nb);
           launch_fft_x_pick_fast(H.p, g, plist, k, X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
@@ -706,6 +714,44 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       }
     }
   }
+}
+
+// Real-space wavefunctions of every band, kept on the device (grid sizes with
+// register kernels only); returns whether they were built.
+static bool build_grids(DevWF &d) {
+  HostPhase hp("build_grids");
+  ensure_coeffs(d);
+  const size_t n3d = (size_t)d.N[0] * d.N[1] * d.N[2];
+  std::vector<PlaneGeom> geo(d.nk);
+  int maxn1 = 0;
+  for (int k = 0; k < d.nk; k++) {
+    DevKpt &q = d.kp[k];
+    ensure_planes(d, q);
+    PlaneGeom g{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
+    g.g2min = q.g2min;
+    g.n2 = q.n2;
+    g.g3min = q.g3min;
+    g.n3 = q.n3;
+    g.maxcnt = q.maxcnt;
+    if (!(q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g)) || generic_fft_forced()) return false;
+    geo[k] = g;
+    maxn1 = std::max(maxn1, q.n1);
+  }
+  d.grid.alloc((size_t)d.nk * d.nband * n3d);
+  const long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
+  const int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, (96LL << 20) / std::max(1LL, hband)));
+  DevBuf<float2> H((size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
+  for (int k = 0; k < d.nk; k++) {
+    DevKpt &q = d.kp[k];
+    for (int b0 = 0; b0 < d.nband; b0 += fbatch) {
+      const int nb = std::min(fbatch, d.nband - b0);
+      launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
+                             H.p, nb);
+      launch_fft_x_grid(H.p, geo[k], d.grid.p + ((size_t)k * d.nband + b0) * n3d, nb);
+    }
+  }
+  d.grid_ready = true;
+  return true;
 }
 
 // ============================================================= host projection_t output
@@ -1234,7 +1280,7 @@ int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int 
 }
 void pawpy_gpu_set_host_projections(int on) { g_host_proj = on != 0; }
 
-int pawpy_gpu_prepare_basis(pswf_t *wf) {
+int pawpy_gpu_prepare_basis(pswf_t *wf, int keep_real_space) {
   PAWPY_API_BEGIN
   HostPhase hp_api("prepare_basis");
   DevWF &d = mirror(wf);
@@ -1242,8 +1288,10 @@ int pawpy_gpu_prepare_basis(pswf_t *wf) {
   ensure_coeffs(d);
   for (auto &q : d.kp) ensure_planes(d, q);
   ensure_projections(d);
+  int kept = 0;
+  if (keep_real_space && !d.grid_ready) kept = build_grids(d) ? 1 : 0;
   sync();
-  return 0;
+  return d.grid_ready ? 1 : kept;
   PAWPY_API_END(-1)
 }
 

@@ -392,6 +392,45 @@ __global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ 
   }
 }
 
+// Pass B writing whole grids (resident real-space wavefunctions): grid
+// (ceil(nb / BPC) band groups, N2 planes j), FT threads in BPC groups of TPB,
+// one band each; the first-axis transform of plane j goes straight from
+// registers to grid[b][(x N2 + j) N3 + z].
+template <int N1, int N3, int T1>
+__global__ void __launch_bounds__(FT) k_xgrid(const float2 *__restrict__ H, int nb, PlaneGeom g,
+                                              float2 *__restrict__ grid) {
+  constexpr int L1 = N1 / T1;
+  constexpr int TPB = 32 * ((N3 * T1 + 31) / 32) < FT ? 32 * ((N3 * T1 + 31) / 32) : FT;
+  constexpr int BPC = FT / TPB;
+  constexpr int LPW = 32 / T1;
+  const int grp = threadIdx.x / TPB, gt = threadIdx.x - grp * TPB;
+  const int warp = gt >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * BPC + grp, j = blockIdx.y;
+  if (grp >= BPC || b >= nb) return;
+  const int n1 = g.n1, s1 = wrapi(g.g1min, N1);
+  const int pstride = g.N2 * N3;
+  const int h = lane / LPW, c = lane % LPW;
+  const float2 *hb = H + ((long long)b * n1 * g.N2 + j) * N3;
+  float2 *gb = grid + (long long)b * N1 * g.N2 * N3 + (long long)j * N3;
+  for (int g0 = warp * LPW; g0 < N3; g0 += (TPB / 32) * LPW) {
+    const int z = g0 + c;
+    const bool ok = z < N3;
+    float2 x[L1];
+#pragma unroll
+    for (int m = 0; m < L1; m++) {
+      int pp = h + T1 * m - s1;
+      pp += pp < 0 ? N1 : 0;
+      x[m] = ok && pp < n1 ? hb[pp * pstride + z] : make_float2(0.f, 0.f);
+    }
+    reg::line_fft<N1, T1, 1>(x, h);
+    if (ok) {
+      const int o = L1 * reg::bitrev(h, T1);
+#pragma unroll
+      for (int k = 0; k < L1; k++) gb[(long long)(o + k) * pstride + z] = x[k];
+    }
+  }
+}
+
 constexpr int direct_bands(int n1, int n3) {
   return 32 * ((n3 * direct_lanes(n1) + 31) / 32) < FT ? FT / (32 * ((n3 * direct_lanes(n1) + 31) / 32)) : 1;
 }

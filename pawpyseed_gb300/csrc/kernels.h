@@ -47,6 +47,11 @@ struct PickList {
 };
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
                             long long xstride, int nb);
+// pass B writing whole grids: grid[b] = [N1][N2][N3] real-space values of band b (register sizes only)
+void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb);
+// the pick of launch_fft_x_pick_fast from resident grids [b][N1][N2][N3]
+void launch_grid_pick(const float2 *grid, int N1, int N2, int N3, const PickList &pl, int kq, float2 *X,
+                      long long xstride, int nb);
 // fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
 void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).

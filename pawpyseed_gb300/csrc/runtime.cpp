@@ -86,6 +86,10 @@ void drain_locked(Runtime &r) {
 // A thread may order its work on a stream of its own (pawpy_gpu_thread_stream),
 // so that several host threads keep independent work in flight on the device.
 static thread_local cudaStream_t t_stream = nullptr;
+// ...and a memory pool of its own: blocks freed on one thread's stream are never
+// handed to another thread's stream, so the pool inserts no dependencies
+// between the threads' streams (which would order their work).
+static thread_local cudaMemPool_t t_pool = nullptr;
 
 cudaStream_t stream() {
   if (t_stream) return t_stream;
@@ -155,7 +159,7 @@ void sync() {
 void *dmalloc(size_t bytes) {
   cudaStream_t s = stream();
   void *p = nullptr;
-  cudaError_t e = cudaMallocAsync(&p, bytes, s);
+  cudaError_t e = t_pool ? cudaMallocFromPoolAsync(&p, bytes, t_pool, s) : cudaMallocAsync(&p, bytes, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
     throw Error(ERR_ALLOC, std::string("device allocation of ") + std::to_string(bytes) +
@@ -263,11 +267,27 @@ int pawpy_gpu_thread_stream(int on) {
   stream();  // the device context and the shared stream exist first
   if (on && !t_stream) {
     PAWPY_CUDA(cudaStreamCreateWithFlags(&t_stream, cudaStreamNonBlocking));
+    if (!t_pool) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = device();
+      PAWPY_CUDA(cudaMemPoolCreate(&t_pool, &props));
+      uint64_t thr = ~0ull;
+      PAWPY_CUDA(cudaMemPoolSetAttribute(t_pool, cudaMemPoolAttrReleaseThreshold, &thr));
+      int no = 0;
+      PAWPY_CUDA(cudaMemPoolSetAttribute(t_pool, cudaMemPoolReuseAllowInternalDependencies, &no));
+    }
   } else if (!on && t_stream) {
     cudaStream_t s = t_stream;
     PAWPY_CUDA(cudaStreamSynchronize(s));
     t_stream = nullptr;
     PAWPY_CUDA(cudaStreamDestroy(s));
+    if (t_pool) {
+      // the pool stays (blocks may still be owned by longer-lived objects); its unused memory goes back
+      PAWPY_CUDA(cudaMemPoolTrimTo(t_pool, 0));
+      t_pool = nullptr;
+    }
   }
   return 0;
   PAWPY_API_END(-1)

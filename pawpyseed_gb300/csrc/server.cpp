@@ -31,6 +31,7 @@ struct Request {
   std::vector<double> coords;
   long long est = 0;
   Clock::time_point t_submit, t_start, t_end;
+  double phase_ms[4] = {0, 0, 0, 0};  // setup_projections, overlap_setup_real, project_all, release
   int status = 0;
   std::string msg;
   bool done = false;
@@ -93,18 +94,27 @@ void run_request(Server &s, Request &q) {
   const int *L[6];
   for (int i = 0; i < 6; i++) L[i] = q.lists[i].empty() ? nullptr : q.lists[i].data();
   auto mut = [](const int *p) { return const_cast<int *>(p); };
+  Clock::time_point t = Clock::now();
+  auto lap = [&](int i) {
+    Clock::time_point n = Clock::now();
+    q.phase_ms[i] = std::chrono::duration<double, std::milli>(n - t).count();
+    t = n;
+  };
   setup_projections(r.wf, r.pps, r.num_elems, r.num_sites, q.fftg, q.labels.data(), q.coords.data());
+  lap(0);
   if (pawpy_gpu_last_error()) {
     fail("setup_projections");
   } else {
     overlap_setup_real(B.wf, r.wf, const_cast<int *>(B.labels.data()), q.labels.data(),
                        const_cast<double *>(B.coords.data()), q.coords.data(), mut(L[2]), mut(L[3]), mut(L[4]),
                        mut(L[5]), r.num_N_R, r.num_N_S, r.num_N_RS);
+    lap(1);
     if (pawpy_gpu_last_error()) {
       fail("overlap_setup_real");
     } else {
       pawpy_gpu_project_all(r.out, B.wf, r.wf, r.num_M, r.num_N_R, r.num_N_S, r.num_N_RS, mut(L[0]), mut(L[1]),
                             mut(L[2]), mut(L[3]), mut(L[4]), mut(L[5]), 0);
+      lap(2);
       if (pawpy_gpu_last_error()) fail("pawpy_gpu_project_all");
     }
   }
@@ -112,6 +122,7 @@ void run_request(Server &s, Request &q) {
   const bool attached = r.wf->pps == r.pps;
   pawpy_gpu_release(r.wf);
   pawpy_gpu_free_pswf(r.wf);
+  lap(3);
   if (!attached && r.pps) free_ppot_array(r.pps, r.num_elems);
   r.wf = nullptr;
   r.pps = nullptr;
@@ -170,11 +181,12 @@ void *pawpy_gpu_server_create(long long hbm_budget_bytes, int slots) {
 }
 
 int pawpy_gpu_server_add_basis(void *server, pswf_t *basis, const int *labels, const double *coords,
-                               int num_sites) {
+                               int num_sites, int keep_real_space) {
   PAWPY_API_BEGIN
   auto *s = static_cast<Server *>(server);
   PAWPY_REQUIRE(s && basis && labels && coords && num_sites > 0, "pawpy_gpu_server_add_basis: bad argument");
-  if (pawpy_gpu_prepare_basis(basis) != 0) throw Error(pawpy_gpu_last_error(), pawpy_gpu_error_string());
+  if (pawpy_gpu_prepare_basis(basis, keep_real_space) < 0)
+    throw Error(pawpy_gpu_last_error(), pawpy_gpu_error_string());
   Basis b;
   b.wf = basis;
   b.labels.assign(labels, labels + num_sites);
@@ -238,6 +250,7 @@ int pawpy_gpu_server_wait(void *server, long long id, double *times_ms, long lon
     times_ms[0] = ms_between(q->t_submit, q->t_start);
     times_ms[1] = ms_between(q->t_start, q->t_end);
     times_ms[2] = ms_between(q->t_submit, q->t_end);
+    for (int i = 0; i < 4; i++) times_ms[3 + i] = q->phase_ms[i];
   }
   if (est_bytes) *est_bytes = q->est;
   if (msg && msg_len > 0) {

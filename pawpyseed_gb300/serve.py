@@ -49,7 +49,8 @@ def site_lists(basis, defect):
 class ProjectionServer:
     """Continuous-batching server over the library (see the module docstring)."""
 
-    def __init__(self, hbm_budget_bytes=100 << 30, slots=4):
+    def __init__(self, hbm_budget_bytes=100 << 30, slots=4, keep_real_space=True):
+        self._keep = 1 if keep_real_space else 0
         self._L = _lib.lib()
         self._h = self._L.pawpy_gpu_server_create(int(hbm_budget_bytes), int(slots))
         _lib.check()
@@ -60,7 +61,7 @@ class ProjectionServer:
         """Make a basis Wavefunction resident; returns its index."""
         basis.check_c_projectors()
         idx = self._L.pawpy_gpu_server_add_basis(self._h, basis.wf_ptr, basis.nums, basis.coords,
-                                                 len(basis.structure))
+                                                 len(basis.structure), self._keep)
         _lib.check()
         self._bases.append(basis)
         return idx
@@ -98,14 +99,15 @@ class ProjectionServer:
 
     def wait(self, rid):
         """(result nband_S x (nband_R nk), dict of queue/run/latency ms, estimate bytes, pairs)."""
-        times = (C.c_double * 3)()
+        times = (C.c_double * 7)()
         est = C.c_longlong(0)
         msg = C.create_string_buffer(1024)
         st = self._L.pawpy_gpu_server_wait(self._h, int(rid), times, C.byref(est), msg, len(msg))
         keep = self._pending.pop(rid)
         if st:
             raise _lib.PAWpyGPUError(st, msg.value.decode(errors="replace"))
-        return keep["out"], dict(queue_ms=times[0], run_ms=times[1], latency_ms=times[2], est_bytes=est.value,
+        return keep["out"], dict(queue_ms=times[0], run_ms=times[1], latency_ms=times[2], setup_ms=times[3],
+                                 overlap_ms=times[4], project_ms=times[5], release_ms=times[6], est_bytes=est.value,
                                  pairs=keep["pairs"])
 
     def counts(self):
@@ -191,13 +193,13 @@ def core_region():
     return vaspio.CoreRegion(synth.potcar_text(["A", "B"]))
 
 
-def run_stream(bases, reqs, slots=4, budget=100 << 30, precision="bf16x3"):
+def run_stream(bases, reqs, slots=4, budget=100 << 30, precision="bf16x3", keep_real_space=True):
     """Replays the request stream in real time; returns per-request records and totals."""
     _lib.set_precision(precision)
     L = _lib.lib()
     L.pawpy_gpu_set_host_projections(0)
     cr = core_region()
-    srv = ProjectionServer(budget, slots)
+    srv = ProjectionServer(budget, slots, keep_real_space)
     try:
         bwf = []
         for bs, w, data in bases:
