@@ -223,6 +223,21 @@ def run_ours(args, rank, world, local, pg):
     ms_step = max_over_ranks(pg, ms / args.steps)
     value = sum_over_ranks(pg, pairs) / (ms_step / 1e3)
 
+    # ---- the plain FP32 form (CUDA-core contraction) on the same resident inputs, for comparison
+    plain = None
+    if args.precision != "fp32":
+        _lib.set_precision("fp32")
+        step()
+        L.pawpy_gpu_synchronize()
+        barrier(pg)
+        L.pawpy_gpu_timer_start()
+        for _ in range(args.steps):
+            step()
+        ms_fp32 = max_over_ranks(pg, L.pawpy_gpu_timer_stop_ms() / args.steps)
+        plain = dict(value=sum_over_ranks(pg, pairs) / (ms_fp32 / 1e3), ms_per_step=ms_fp32)
+        _lib.set_precision(args.precision)
+        step()
+
     # ---- end to end: host pswf_t, H2D of the defect's coefficients and D2H of the matrix every step
     h2d = sum(c.nbytes for c in dd["coeffs"])
     d2h = out.nbytes
@@ -249,7 +264,7 @@ def run_ours(args, rank, world, local, pg):
     stats = _lib.kernel_stats(reset=True)
     roof = roofline(stats, w, basis, wf, lists, cr)
 
-    result = dict(pairs_per_step=pairs, ms=ms_step, value=value, e2e_ms=e2e_step, e2e_value=e2e_value,
+    result = dict(pairs_per_step=pairs, ms=ms_step, value=value, e2e_ms=e2e_step, e2e_value=e2e_value, plain=plain,
                   h2d=h2d, d2h=d2h, launches=launches // args.steps, clocks=clk, roofline=roof,
                   kernel_ms={k: v[0] for k, v in stats.items() if not k.startswith("host.")},
                   host_ms={k[5:]: v[0] for k, v in stats.items() if k.startswith("host.")})
@@ -510,7 +525,8 @@ def main():
                     e2e=dict(value=res["e2e_value"], unit="pairs/s", ms_per_step=res["e2e_ms"],
                              h2d_bytes_per_step=res["h2d"], d2h_bytes_per_step=res["d2h"]),
                     gpu_launches=res["launches"], roofline=res["roofline"], cpu_baseline=cpu,
-                    clocks=res["clocks"], kernel_ms=res["kernel_ms"], host_ms=res["host_ms"])
+                    clocks=res["clocks"], kernel_ms=res["kernel_ms"], host_ms=res["host_ms"],
+                    plain_fp32_form=res["plain"])
         print(json.dumps(line))
 
 

@@ -273,12 +273,14 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
  * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf. */
 pswf_t *pawpy_gpu_read_wavefunctions(const char *filename, const double *kpt_weights);
 /* Builds a pswf_t from in-memory arrays: Gs[iwk] int32[3*nplane[iwk]] and
- * Cs[iwk] complex64[nband*nplane[iwk]] for iwk = spin*nwk + k. Copies them. */
+ * Cs[iwk] complex64[nband*nplane[iwk]] for iwk = spin*nwk + k. Copies them.
+ * is_ncl: noncollinear (spinor) coefficients; nplane counts both halves (up
+ * then down) and Gs holds the nplane/2 vectors of one half. */
 pswf_t *pawpy_gpu_wavefunction_from_arrays(int nspin, int nwk, int nband, double encut,
                                            const double *lattice, const double *kpts,
                                            const double *weights, const int *nplane,
                                            const int *const *Gs, const pawpy_c64 *const *Cs,
-                                           const double *energies, const double *occs);
+                                           const double *energies, const double *occs, int is_ncl);
 /* Frees a pswf_t and everything attached to it (also releases its device copy). */
 void pawpy_gpu_free_pswf(pswf_t *wf);
 /* Frees an element array returned by get_projector_list that was not handed

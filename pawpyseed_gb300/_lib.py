@@ -44,7 +44,7 @@ def _declare(L):
     L.pawpy_gpu_wavefunction_from_arrays.restype = _wfp
     L.pawpy_gpu_wavefunction_from_arrays.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
                                                     _ip, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
-                                                    _dp, _dp]
+                                                    _dp, _dp, C.c_int]
     L.pawpy_gpu_free_pswf.argtypes = [_wfp]
     L.pawpy_gpu_free_ppot_list.argtypes = [_ppp, C.c_int]
     L.pawpy_gpu_release.argtypes = [_wfp]

@@ -67,7 +67,12 @@ struct DevKpt {
 
 struct DevWF {
   pswf_t *wf = nullptr;
+  // nband counts device bands: a noncollinear wavefunction's band b is the two
+  // device bands 2b (spin-up half) and 2b+1 (spin-down half), which share the
+  // G list as in onto_projector_ncl (projector.c:359-392)
   int nspin = 0, nwk = 0, nband = 0, nk = 0;
+  bool ncl = false;
+  int nband_host = 0;
   kpoint_t **kpts_ptr = nullptr;
   const void *cs0 = nullptr;
   double lattice[9], rec[9], vol = 0;
@@ -144,7 +149,8 @@ void release_device(pswf_t *wf) {
 }
 
 static bool fingerprint_ok(const DevWF &d, const pswf_t *wf) {
-  return d.nspin == wf->nspin && d.nwk == wf->nwk && d.nband == wf->nband && d.kpts_ptr == wf->kpts &&
+  return d.nspin == wf->nspin && d.nwk == wf->nwk && d.nband_host == wf->nband && d.kpts_ptr == wf->kpts &&
+         d.ncl == (wf->is_ncl != 0) &&
          wf->kpts && wf->kpts[0] && wf->kpts[0]->bands && wf->kpts[0]->bands[0] &&
          d.cs0 == (const void *)wf->kpts[0]->bands[0]->Cs;
 }
@@ -187,7 +193,6 @@ static void sort_gvectors(const int *G, int W, std::vector<int> &perm) {
 
 static DevWF &mirror(pswf_t *wf) {
   PAWPY_REQUIRE(wf != nullptr, "wavefunction pointer is NULL");
-  PAWPY_REQUIRE(!wf->is_ncl, "noncollinear wavefunctions are not supported by the projection path");
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   auto it = g_wfs.find(wf);
   if (it != g_wfs.end() && !fingerprint_ok(*it->second, wf)) {
@@ -200,7 +205,9 @@ static DevWF &mirror(pswf_t *wf) {
   d->wf = wf;
   d->nspin = wf->nspin;
   d->nwk = wf->nwk;
-  d->nband = wf->nband;
+  d->ncl = wf->is_ncl != 0;
+  d->nband_host = wf->nband;
+  d->nband = d->ncl ? 2 * wf->nband : wf->nband;
   d->nk = wf->nspin * wf->nwk;
   d->kpts_ptr = wf->kpts;
   d->cs0 = wf->kpts[0]->bands[0]->Cs;
@@ -212,7 +219,8 @@ static DevWF &mirror(pswf_t *wf) {
   for (int k = 0; k < d->nk; k++) {
     kpoint_t *kp = wf->kpts[k];
     DevKpt &q = d->kp[k];
-    q.W = kp->num_waves;
+    q.W = d->ncl ? kp->num_waves / 2 : kp->num_waves;
+    PAWPY_REQUIRE(!d->ncl || kp->num_waves % 2 == 0, "noncollinear k-point with an odd plane-wave count");
     q.Wpad = (q.W + 15) / 16 * 16;
     for (int a = 0; a < 3; a++) q.kfrac[a] = kp->k[a];
     q.perm.resize(q.W);
@@ -231,6 +239,13 @@ static DevWF &mirror(pswf_t *wf) {
   DevWF &ref = *d;
   g_wfs[wf] = std::move(d);
   return ref;
+}
+
+// host coefficients of device band b at k-point k (a spinor half for noncollinear wavefunctions)
+static const float2 *host_band(const DevWF &d, int k, int b) {
+  const kpoint_t *kp = d.wf->kpts[k];
+  if (!d.ncl) return reinterpret_cast<const float2 *>(kp->bands[b]->Cs);
+  return reinterpret_cast<const float2 *>(kp->bands[b / 2]->Cs) + (size_t)(b & 1) * d.kp[k].W;
 }
 
 static int pageable_access() {
@@ -260,7 +275,7 @@ static void ensure_coeffs(DevWF &d) {
     std::vector<const float2 *> hp((size_t)d.nk * d.nband);
     for (int k = 0; k < d.nk; k++)
       for (int b = 0; b < d.nband; b++)
-        hp[(size_t)k * d.nband + b] = reinterpret_cast<const float2 *>(d.wf->kpts[k]->bands[b]->Cs);
+        hp[(size_t)k * d.nband + b] = host_band(d, k, b);
     DevBuf<const float2 *> hpd(hp.size());
     hpd.upload(hp.data(), hp.size());
     for (int k = 0; k < d.nk; k++) {
@@ -277,8 +292,9 @@ static void ensure_coeffs(DevWF &d) {
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
     kpoint_t *kp = d.wf->kpts[k];
+    (void)kp;
     for (int b = 0; b < d.nband; b++)
-      PAWPY_CUDA(cudaMemcpyAsync(raw.p + (size_t)b * q.W, kp->bands[b]->Cs, sizeof(float2) * q.W,
+      PAWPY_CUDA(cudaMemcpyAsync(raw.p + (size_t)b * q.W, host_band(d, k, b), sizeof(float2) * q.W,
                                  cudaMemcpyHostToDevice, stream()));
     q.perm_d.alloc(q.W);
     q.perm_d.upload(q.perm.data(), q.W);
@@ -839,19 +855,21 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
     }
     for (int k = 0; k < d.nk; k++)
       for (int b = 0; b < d.nband; b++) {
-        band_t *bd = wf->kpts[k]->bands[b];
-        if (bd->projections) {
+        // noncollinear: device band 2b -> up_projections, 2b+1 -> down_projections of band b
+        band_t *bd = wf->kpts[k]->bands[d.ncl ? b / 2 : b];
+        projection_t *&slot = !d.ncl ? bd->projections : (b & 1) ? bd->down_projections : bd->up_projections;
+        if (slot) {
           for (int s = 0; s < num_sites; s++) {
-            std::free(bd->projections[s].ns);
-            std::free(bd->projections[s].ls);
-            std::free(bd->projections[s].ms);
-            std::free(bd->projections[s].overlaps);
+            std::free(slot[s].ns);
+            std::free(slot[s].ls);
+            std::free(slot[s].ms);
+            std::free(slot[s].overlaps);
           }
-          std::free(bd->projections);
+          std::free(slot);
         }
-        bd->projections = static_cast<projection_t *>(std::calloc(num_sites, sizeof(projection_t)));
-        if (!bd->projections) throw std::bad_alloc();
-        fill_projection_list(bd->projections, tot, off, sp.data(),
+        slot = static_cast<projection_t *>(std::calloc(num_sites, sizeof(projection_t)));
+        if (!slot) throw std::bad_alloc();
+        fill_projection_list(slot, tot, off, sp.data(),
                              h.data() + ((size_t)k * d.nband + b) * d.proj.Ptot);
       }
   }
@@ -865,9 +883,15 @@ static PairState &pair_state(pswf_t *R, pswf_t *S) {
   auto key = std::make_pair((const pswf_t *)R, (const pswf_t *)S);
   auto &ptr = g_pairs[key];
   if (!ptr) {
+    DevWF &r = mirror(R), &s = mirror(S);
+    // the reference computes no overlaps of noncollinear wavefunctions (projector.py:74-75)
+    if (r.ncl || s.ncl) {
+      g_pairs.erase(key);
+      throw Error(ERR_UNSUPPORTED, "overlaps of noncollinear wavefunctions are not part of the projection path");
+    }
     ptr = std::make_unique<PairState>();
-    ptr->R = &mirror(R);
-    ptr->S = &mirror(S);
+    ptr->R = &r;
+    ptr->S = &s;
   }
   return *ptr;
 }

@@ -15,7 +15,7 @@ pswf_t *read_wavecar(const char *path, const double *kws);
 pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const double *lattice,
                          const double *kpts, const double *weights, const int *nplane,
                          const int *const *Gs, const pawpy_c64 *const *Cs, const double *energies,
-                         const double *occs);
+                         const double *occs, int is_ncl);
 void free_pswf_all(pswf_t *wf);
 void free_ppot_array(ppot_t *pps, int n);
 void free_wave_projections(pswf_t *wf);

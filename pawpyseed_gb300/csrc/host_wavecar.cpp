@@ -216,9 +216,10 @@ pswf_t *read_wavecar(const char *path, const double *kws) {
 pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const double *lattice,
                          const double *kpts, const double *weights, const int *nplane,
                          const int *const *Gs, const pawpy_c64 *const *Cs, const double *energies,
-                         const double *occs) {
+                         const double *occs, int is_ncl) {
   PAWPY_REQUIRE(nspin >= 1 && nspin <= 2 && nwk >= 1 && nband >= 1, "bad wavefunction dimensions");
   pswf_t *wf = new_pswf(nspin, nwk, nband, encut, lattice);
+  wf->is_ncl = is_ncl ? 1 : 0;
   try {
     for (int iwk = 0; iwk < nwk * nspin; iwk++) {
       int np = nplane[iwk];
@@ -226,8 +227,13 @@ pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const doub
       kp->up = (short)(iwk / nwk);
       wf->kpts[iwk] = kp;
       kp->Gs = xmalloc<int>((size_t)3 * np);
-      std::memcpy(kp->Gs, Gs[iwk], sizeof(int) * 3 * np);
-      update_bounds(wf, kp->Gs, np);
+      // noncollinear (reader.c:275-284): np counts both spinor halves; the G list of
+      // one half is given, and stored twice as the WAVECAR reader stores it
+      const int ng = is_ncl ? np / 2 : np;
+      PAWPY_REQUIRE(!is_ncl || np % 2 == 0, "noncollinear plane-wave count must be even");
+      std::memcpy(kp->Gs, Gs[iwk], sizeof(int) * 3 * ng);
+      if (is_ncl) std::memcpy(kp->Gs + 3 * ng, Gs[iwk], sizeof(int) * 3 * ng);
+      update_bounds(wf, kp->Gs, ng);
       for (int b = 0; b < nband; b++) {
         band_t *bd = kp->bands[b];
         bd->Cs = xmalloc<pawpy_c64>(np);
@@ -362,10 +368,10 @@ pswf_t *pawpy_gpu_wavefunction_from_arrays(int nspin, int nwk, int nband, double
                                            const double *lattice, const double *kpts,
                                            const double *weights, const int *nplane,
                                            const int *const *Gs, const pawpy_c64 *const *Cs,
-                                           const double *energies, const double *occs) {
+                                           const double *energies, const double *occs, int is_ncl) {
   PAWPY_API_BEGIN
   return pswf_from_arrays(nspin, nwk, nband, encut, lattice, kpts, weights, nplane, Gs, Cs,
-                          energies, occs);
+                          energies, occs, is_ncl);
   PAWPY_API_END(nullptr)
 }
 

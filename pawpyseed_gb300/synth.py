@@ -205,8 +205,11 @@ def band_coefficients(rng, lattice, kpt, gs, nband):
     return (c / nrm[:, None].astype(np.float32)).astype(np.complex64)
 
 
-def wavefunction_data(struct, w, seed):
-    """In-memory WAVECAR content for one structure of a workload."""
+def wavefunction_data(struct, w, seed, ncl=False):
+    """In-memory WAVECAR content for one structure of a workload.
+
+    ncl: noncollinear content; each band is a spinor (up half, then down half,
+    each on the k-point's G list) normalised as a whole."""
     rng = np.random.default_rng(seed)
     lattice = struct.lattice
     kpts = np.asarray(w["kpts"], dtype=np.float64).reshape(-1, 3)
@@ -220,12 +223,19 @@ def wavefunction_data(struct, w, seed):
         k = kpts[iwk % nwk]
         g = vaspio.gvectors(lattice, k, w["encut"])
         gs.append(g)
-        coeffs.append(band_coefficients(rng, lattice, k, g, nband))
+        if ncl:
+            up = band_coefficients(rng, lattice, k, g, nband)
+            dn = band_coefficients(rng, lattice, k, g, nband)
+            sp = np.concatenate([up, dn], axis=1).astype(np.complex128)
+            sp /= np.sqrt((np.abs(sp) ** 2).sum(1))[:, None]
+            coeffs.append(sp.astype(np.complex64))
+        else:
+            coeffs.append(band_coefficients(rng, lattice, k, g, nband))
         energies.append(np.linspace(-5.0, 5.0, nband))
         occs.append((np.arange(nband) < nband // 2).astype(np.float64))
     return dict(lattice=lattice, encut=w["encut"], kpts=kpts, nspin=nspin, nwk=nwk,
                 nband=nband, gs=gs, coeffs=coeffs, energies=np.array(energies),
-                occs=np.array(occs), weights=np.full(nwk, 1.0 / nwk))
+                occs=np.array(occs), weights=np.full(nwk, 1.0 / nwk), ncl=bool(ncl))
 
 
 def write_structure_dir(path, struct, data, dim, symbols=None):

@@ -70,6 +70,8 @@ class Wavefunction:
     kpts, kws, ncl, symprec.
     """
 
+    _NCL = False  # the collinear class refuses spinor wavefunctions, as the reference does
+
     def __init__(self, struct, pwf, cr, dim, kpts=None, kws=None, symprec=1e-4, setup_projectors=False):
         self._ptr = None
         if not pwf:
@@ -78,8 +80,10 @@ class Wavefunction:
         w = pwf.contents
         self.nband, self.nwk, self.nspin, self.encut = w.nband, w.nwk, w.nspin, w.encut
         self.ncl = bool(w.is_ncl)
-        if self.ncl:
+        if self.ncl and not self._NCL:
             raise PAWpyError("Pseudowavefunction is noncollinear! Call NCLWavefunction(...) instead")
+        if self._NCL and not self.ncl:
+            raise PAWpyError("Pseudowavefunction is collinear! Call Wavefunction(...) instead")
         self.structure = struct
         self.cr = cr
         self.symprec = symprec
@@ -101,8 +105,8 @@ class Wavefunction:
 
     # -- construction ------------------------------------------------------
 
-    @staticmethod
-    def from_files(struct="CONTCAR", wavecar="WAVECAR", cr="POTCAR", vr="vasprun.xml",
+    @classmethod
+    def from_files(cls, struct="CONTCAR", wavecar="WAVECAR", cr="POTCAR", vr="vasprun.xml",
                    setup_projectors=False):
         """Wavefunction.from_files (wavefunction.py:281-322)."""
         for fname in [struct, wavecar, cr, vr]:
@@ -125,19 +129,21 @@ class Wavefunction:
         finally:
             if tmp is not None:
                 os.unlink(tmp.name)
-        return Wavefunction(read_poscar(struct), ptr, CoreRegion(cr), dim, vr.actual_kpoints, kws,
+        return cls(read_poscar(struct), ptr, CoreRegion(cr), dim, vr.actual_kpoints, kws,
                             vr.parameters["SYMPREC"], setup_projectors)
 
-    @staticmethod
-    def from_directory(path, setup_projectors=False):
+    @classmethod
+    def from_directory(cls, path, setup_projectors=False):
         files = [os.path.join(path, d) for d in ["CONTCAR", "WAVECAR", "POTCAR", "vasprun.xml"]]
-        return Wavefunction.from_files(*files, setup_projectors)
+        return cls.from_files(*files, setup_projectors)
 
-    @staticmethod
-    def from_arrays(struct, cr, dim, data, setup_projectors=False):
-        """Build from in-memory WAVECAR content (dict of synth.wavefunction_data)."""
+    @classmethod
+    def from_arrays(cls, struct, cr, dim, data, setup_projectors=False):
+        """Build from in-memory WAVECAR content (dict of synth.wavefunction_data; a
+        noncollinear dict has ``ncl`` set, spinor coefficients of twice the G count)."""
         nk = data["nspin"] * data["nwk"]
-        nplane = np.array([g.shape[0] for g in data["gs"]], dtype=np.int32)
+        ncl = bool(data.get("ncl", False))
+        nplane = np.array([(2 if ncl else 1) * g.shape[0] for g in data["gs"]], dtype=np.int32)
         gs = [np.ascontiguousarray(g, dtype=np.int32) for g in data["gs"]]
         cs = [np.ascontiguousarray(c, dtype=np.complex64) for c in data["coeffs"]]
         gp = (C.c_void_p * nk)(*[g.ctypes.data for g in gs])
@@ -149,9 +155,9 @@ class Wavefunction:
         oc = np.ascontiguousarray(np.asarray(data["occs"]).reshape(-1), dtype=np.float64)
         ptr = _lib.lib().pawpy_gpu_wavefunction_from_arrays(data["nspin"], data["nwk"], data["nband"],
                                                            float(data["encut"]), lat, kp, kws, nplane,
-                                                           gp, cp, en, oc)
+                                                           gp, cp, en, oc, 1 if ncl else 0)
         _lib.check()
-        return Wavefunction(struct, ptr, cr, dim, data["kpts"], kws, 1e-4, setup_projectors)
+        return cls(struct, ptr, cr, dim, data["kpts"], kws, 1e-4, setup_projectors)
 
     def detach(self):
         """Give up the pswf_t without freeing it (its new owner frees it)."""
@@ -233,3 +239,31 @@ class Wavefunction:
         _lib.lib().pseudoprojection(res, basis._ptr, self._ptr, int(band_num), int(flip_spin))
         _lib.check()
         return res
+
+
+class NCLWavefunction(Wavefunction):
+    """Noncollinear (spinor) wavefunction (noncollinear.py:4-32).
+
+    setup_projections fills every band's ``up_projections`` and
+    ``down_projections`` (onto_projector_ncl, projector.c:359-392): the two
+    spinor halves share the G list and are transformed and projected as two
+    bands on the device. Overlaps of noncollinear wavefunctions are not part of
+    the reference's projection path (``Projector`` refuses them)."""
+
+    _NCL = True
+
+    def spinor_projections(self, band, k):
+        """(<p|psi_up>, <p|psi_down>) of one band at k-point index k (spin-major), complex128
+        over every site's lm channels in site order."""
+        self.check_c_projectors()
+        kp = self.wf_ptr.contents.kpts[k].contents
+        bd = kp.bands[band].contents
+        out = []
+        for lst in (bd.up_projections, bd.down_projections):
+            vals = []
+            for s in range(len(self.structure)):
+                p = lst[s]
+                v = np.ctypeslib.as_array(p.overlaps, shape=(2 * p.total_projs,))
+                vals.append(v[0::2] + 1j * v[1::2])
+            out.append(np.concatenate(vals))
+        return out[0], out[1]

@@ -176,3 +176,23 @@ def test_synthetic_inputs_are_reproducible(workload_dirs, golden):
     g = golden("cfg0")
     if fingerprint(d["basis"]) != str(g["fp_basis"]):
         pytest.skip("this platform's numpy regenerates different bytes; tolerance tests still apply")
+
+
+def test_collinear_and_noncollinear_classes_refuse_each_other():
+    from pawpyseed_gb300 import synth, vaspio
+    from pawpyseed_gb300.wavefunction import NCLWavefunction, PAWpyError, Wavefunction
+
+    w = synth.small_workload(0, nband=2, nk=1)
+    bs, _ = synth.structures(0)
+    cr = vaspio.CoreRegion(synth.potcar_text(["A"]))
+    ncl = synth.wavefunction_data(bs, w, 5, ncl=True)
+    col = synth.wavefunction_data(bs, w, 5)
+    wf = NCLWavefunction.from_arrays(bs, cr, w["dim"], ncl)
+    kp = wf.wf_ptr.contents.kpts[0].contents
+    assert wf.ncl and kp.num_waves == 2 * ncl["gs"][0].shape[0]
+    g = np.ctypeslib.as_array(kp.Gs, shape=(3 * kp.num_waves,)).reshape(-1, 3)
+    assert np.array_equal(g[: kp.num_waves // 2], g[kp.num_waves // 2:])
+    with pytest.raises(PAWpyError):
+        Wavefunction.from_arrays(bs, cr, w["dim"], ncl)
+    with pytest.raises(PAWpyError):
+        NCLWavefunction.from_arrays(bs, cr, w["dim"], col)
