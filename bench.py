@@ -67,29 +67,7 @@ def dist_init(n):
     return rank, world, local, pg
 
 
-def barrier(pg):
-    if pg is not None:
-        pg.barrier()
-
-
-def max_over_ranks(pg, v):
-    if pg is None:
-        return v
-    import torch
-
-    t = torch.tensor([float(v)])
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
-
-
-def sum_over_ranks(pg, v):
-    if pg is None:
-        return v
-    import torch
-
-    t = torch.tensor([float(v)])
-    pg.all_reduce(t, op=pg.ReduceOp.SUM)
-    return float(t.item())
+from pawpyseed_gb300.replicas import barrier, max_over_ranks, sum_over_ranks  # noqa: E402
 
 
 # ---------------------------------------------------------------- clocks
