@@ -139,6 +139,8 @@ static bool g_host_proj = true;
 
 void release_device(pswf_t *wf) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
+  // work still queued may read the wavefunction's host arrays, which the caller frees next
+  if (g_wfs.count(wf)) sync();
   for (auto it = g_pairs.begin(); it != g_pairs.end();) {
     if (it->first.first == wf || it->first.second == wf)
       it = g_pairs.erase(it);
@@ -873,7 +875,10 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
                              h.data() + ((size_t)k * d.nband + b) * d.proj.Ptot);
       }
   }
-  sync();
+  // Without host outputs the results stay on the device and the call returns with
+  // its work queued: the next call's host preparation overlaps it (a kernel error
+  // surfaces at that call's synchronisation).
+  if (g_host_proj) sync();
 }
 
 // ============================================================= overlap_setup_real
@@ -1018,7 +1023,7 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
     }
   }
   ps.ready = true;
-  sync();
+  if (g_host_proj) sync();  // without host outputs the work stays queued (see do_setup_projections)
 }
 
 // ============================================================= overlap matrices
