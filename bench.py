@@ -387,18 +387,22 @@ def run_reference(args, rank, world, pg):
                 steps=args.steps, warmup=args.warmup, ms_per_step=float(np.median(ts)) * 1e3,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="c64/f64", data="synthetic",
                 impl="reference",
-                config=config(args, w),
+                config=config(args, w, work),
                 cpu_baseline=dict(value=value, unit="pairs/s", cores=cores(), kind="port", sample=sample),
                 e2e=dict(value=value, unit="pairs/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line))
 
 
-def config(args, w):
+def config(args, w, work=None):
+    l2 = "inputs larger than L2"
+    if work is not None:
+        mb = [sum(c.nbytes for c in d["coeffs"]) / 1e6 for d in (work[4], work[5])]
+        l2 += " (basis coefficients %.0f MB, defect coefficients %.0f MB)" % tuple(mb)
     return {"workload": "64-atom cubic 10.86 A A/B cell minus one A, 8 k-points (2x2x2 MP), %d bands, "
                         "ENCUT %g eV, FFT %dx%dx%d, aug_real" % (w["nband"], w["encut"], *w["dim"])
             if args.workload == 1 else "workload %d" % args.workload,
             "nband": w["nband"], "nk": len(w["kpts"]) * w["nspin"], "fft_grid": list(w["dim"]),
-            "precision": args.precision, "l2": "inputs larger than L2 (defect 190 MB, basis 190 MB)"}
+            "precision": args.precision, "l2": l2}
 
 
 def run_serve(args, rank, world, local):
@@ -499,7 +503,7 @@ def main():
         line = dict(metric="band-pair projections/sec", value=res["value"], unit="pairs/s", n_gpus=world,
                     steps=args.steps, warmup=args.warmup, ms_per_step=res["ms"], higher_is_better=True,
                     scaling="weak", vs_baseline=None, dtype="c64 (fp32 accumulate) / f64 setup",
-                    data="synthetic (seeded VASP-format WAVECAR/POTCAR content)", config=config(args, w),
+                    data="synthetic (seeded VASP-format WAVECAR/POTCAR content)", config=config(args, w, work),
                     e2e=dict(value=res["e2e_value"], unit="pairs/s", ms_per_step=res["e2e_ms"],
                              h2d_bytes_per_step=res["h2d"], d2h_bytes_per_step=res["d2h"]),
                     gpu_launches=res["launches"], roofline=res["roofline"], cpu_baseline=cpu,

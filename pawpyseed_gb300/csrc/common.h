@@ -70,6 +70,17 @@ void clear_error();
 // The single stream every kernel and copy of the library is ordered on.
 cudaStream_t stream();
 int device();
+// The calling thread's upload stream, and a scope in which stream() (and so
+// every launch and copy of the library) is another stream. Nothing may be
+// allocated inside such a scope.
+cudaStream_t side_stream();
+struct OnStream {
+  cudaStream_t prev;
+  explicit OnStream(cudaStream_t s);
+  ~OnStream();
+  OnStream(const OnStream &) = delete;
+  OnStream &operator=(const OnStream &) = delete;
+};
 // Waits for the library stream; throws if a device status word read back
 // since the last sync (status_readback) is nonzero.
 void sync();
@@ -82,6 +93,11 @@ void status_readback(int *dev_slot, const char *what);
 // pool, whose release threshold is raised so that memory is reused between
 // calls instead of returned to the driver).
 void *dmalloc(size_t bytes);
+// Host-to-device copy ordered on stream(); h may be reused when it returns.
+// Copies of up to 1 MiB go through a pinned staging ring of the calling thread
+// and never wait for the stream (a copy from pageable memory may wait for the
+// stream's earlier work, which would keep the host from queueing ahead).
+void upload_bytes(void *dev, const void *h, size_t bytes);
 void dfree(void *p);
 long long device_bytes();
 
@@ -113,7 +129,7 @@ struct DevBuf {
     if (n) PAWPY_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), stream()));
   }
   void upload(const T *h, size_t count, size_t off = 0) {
-    if (count) PAWPY_CUDA(cudaMemcpyAsync(p + off, h, count * sizeof(T), cudaMemcpyHostToDevice, stream()));
+    if (count) upload_bytes(p + off, h, count * sizeof(T));
   }
   void download(T *h, size_t count, size_t off = 0) const {
     if (count) PAWPY_CUDA(cudaMemcpyAsync(h, p + off, count * sizeof(T), cudaMemcpyDeviceToHost, stream()));

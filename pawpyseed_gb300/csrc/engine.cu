@@ -14,11 +14,13 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <numeric>
 #include <tuple>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -60,6 +62,7 @@ struct DevKpt {
   std::vector<int> invperm;  // original plane-wave index -> sorted position
   std::vector<int> gsorted;  // [W][3] in sorted order
   DevBuf<int> perm_d, plane_start, plane_off;
+  DevBuf<int> inv_d;  // invperm on the device (host-read upload)
   int off_N2 = 0, off_N3 = 0;
   size_t c_off = 0;
   double kfrac[3] = {0, 0, 0};
@@ -79,6 +82,10 @@ struct DevWF {
   std::vector<DevKpt> kp;
   DevBuf<float2> C;
   bool c_ready = false;
+  // per k-point: the upload of its coefficients on the side stream (empty when
+  // the upload was ordered on the library stream); band pointers of the upload
+  std::vector<cudaEvent_t> c_ev;
+  DevBuf<const float2 *> host_ptrs;
   // resident real-space wavefunctions [k][band][N1][N2][N3] (a prepared basis)
   DevBuf<float2> grid;
   bool grid_ready = false;
@@ -94,7 +101,28 @@ struct DevWF {
   bool p_ready = false;       // P holds <p|psi> of every band
   Radices r[3];
   DevBuf<float2> tw[3];
+  DevWF() = default;
+  DevWF(const DevWF &) = delete;
+  DevWF &operator=(const DevWF &) = delete;
+  // the buffers are freed on the library stream: it waits for the uploads first
+  ~DevWF() {
+    for (cudaEvent_t e : c_ev) {
+      cudaStreamWaitEvent(stream(), e, 0);
+      cudaEventDestroy(e);
+    }
+  }
 };
+
+// Makes the library stream wait for the upload of k-point k's coefficients;
+// their device address.
+static const float2 *coeffs(DevWF &d, int k) {
+  if (!d.c_ev.empty()) PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.c_ev[k], 0));
+  return d.C.p + d.kp[k].c_off;
+}
+
+static void join_uploads(DevWF &d) {
+  for (cudaEvent_t e : d.c_ev) PAWPY_CUDA(cudaStreamWaitEvent(stream(), e, 0));
+}
 
 struct AugKey {
   std::vector<int> lists[6];
@@ -140,7 +168,11 @@ static bool g_host_proj = true;
 void release_device(pswf_t *wf) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   // work still queued may read the wavefunction's host arrays, which the caller frees next
-  if (g_wfs.count(wf)) sync();
+  auto f = g_wfs.find(wf);
+  if (f != g_wfs.end()) {
+    join_uploads(*f->second);
+    sync();
+  }
   for (auto it = g_pairs.begin(); it != g_pairs.end();) {
     if (it->first.first == wf || it->first.second == wf)
       it = g_pairs.erase(it);
@@ -155,6 +187,32 @@ static bool fingerprint_ok(const DevWF &d, const pswf_t *wf) {
          d.ncl == (wf->is_ncl != 0) &&
          wf->kpts && wf->kpts[0] && wf->kpts[0]->bands && wf->kpts[0]->bands[0] &&
          d.cs0 == (const void *)wf->kpts[0]->bands[0]->Cs;
+}
+
+// Runs f(0..n-1) on up to n host threads (the calling thread takes index 0).
+template <typename F>
+static void parallel_for(int n, F f) {
+  const int hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min(n, std::min(hw, 16));
+  if (nt <= 1) {
+    for (int i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::vector<std::exception_ptr> err(nt);
+  auto run = [&](int t) {
+    try {
+      for (int i = t; i < n; i += nt) f(i);
+    } catch (...) {
+      err[t] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (int t = 1; t < nt; t++) th.emplace_back(run, t);
+  run(0);
+  for (auto &x : th) x.join();
+  for (auto &e : err)
+    if (e) std::rethrow_exception(e);
 }
 
 // perm = plane-wave indices in (g1, g2, g3) order. The vectors are distinct
@@ -225,8 +283,13 @@ static DevWF &mirror(pswf_t *wf) {
     PAWPY_REQUIRE(!d->ncl || kp->num_waves % 2 == 0, "noncollinear k-point with an odd plane-wave count");
     q.Wpad = (q.W + 15) / 16 * 16;
     for (int a = 0; a < 3; a++) q.kfrac[a] = kp->k[a];
-    q.perm.resize(q.W);
-    const int *G = kp->Gs;
+    q.c_off = off;
+    off += (size_t)d->nband * q.Wpad;
+  }
+  // the plane-wave orderings of the k-points are independent: one host thread each
+  parallel_for(d->nk, [&](int k) {
+    DevKpt &q = d->kp[k];
+    const int *G = wf->kpts[k]->Gs;
     sort_gvectors(G, q.W, q.perm);
     q.invperm.resize(q.W);
     for (int t = 0; t < q.W; t++) q.invperm[q.perm[t]] = t;
@@ -235,9 +298,7 @@ static DevWF &mirror(pswf_t *wf) {
       for (int a = 0; a < 3; a++) q.gsorted[3 * t + a] = G[3 * q.perm[t] + a];
     q.g1min = q.W ? q.gsorted[0] : 0;
     q.n1 = q.W ? q.gsorted[3 * (q.W - 1)] - q.g1min + 1 : 0;
-    q.c_off = off;
-    off += (size_t)d->nband * q.Wpad;
-  }
+  });
   DevWF &ref = *d;
   g_wfs[wf] = std::move(d);
   return ref;
@@ -274,19 +335,37 @@ static void ensure_coeffs(DevWF &d) {
   int maxW = 0;
   for (auto &q : d.kp) maxW = std::max(maxW, q.W);
   if (pageable_access() && !getenv("PAWPY_GPU_NO_HOST_READ")) {
+    // The uploads run on the side stream, one k-point after another, while the
+    // library stream goes on with the transforms of the k-points already
+    // uploaded (coeffs() orders each use after its k-point's upload). The
+    // caller's arrays outlive the upload: release_device waits for it.
     std::vector<const float2 *> hp((size_t)d.nk * d.nband);
     for (int k = 0; k < d.nk; k++)
       for (int b = 0; b < d.nband; b++)
         hp[(size_t)k * d.nband + b] = host_band(d, k, b);
-    DevBuf<const float2 *> hpd(hp.size());
-    hpd.upload(hp.data(), hp.size());
-    for (int k = 0; k < d.nk; k++) {
-      DevKpt &q = d.kp[k];
-      DevBuf<int> inv(std::max(1, q.W));
-      inv.upload(q.invperm.data(), q.W);
-      launch_load_host_bands(hpd.p + (size_t)k * d.nband, q.W, inv.p, d.C.p + q.c_off, q.Wpad, d.nband);
+    d.host_ptrs.alloc(hp.size());
+    d.host_ptrs.upload(hp.data(), hp.size());
+    for (auto &q : d.kp) {
+      q.inv_d.alloc(std::max(1, q.W));
+      q.inv_d.upload(q.invperm.data(), q.W);
     }
-    // the caller's arrays outlive this call, and every entry point synchronises before it returns
+    cudaEvent_t ready;
+    PAWPY_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    PAWPY_CUDA(cudaEventRecord(ready, stream()));
+    const cudaStream_t up = side_stream();
+    PAWPY_CUDA(cudaStreamWaitEvent(up, ready, 0));
+    PAWPY_CUDA(cudaEventDestroy(ready));
+    d.c_ev.assign(d.nk, nullptr);
+    for (auto &e : d.c_ev) PAWPY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    {
+      OnStream on(up);
+      for (int k = 0; k < d.nk; k++) {
+        DevKpt &q = d.kp[k];
+        launch_load_host_bands(d.host_ptrs.p + (size_t)k * d.nband, q.W, q.inv_d.p, d.C.p + q.c_off, q.Wpad,
+                               d.nband);
+        PAWPY_CUDA(cudaEventRecord(d.c_ev[k], up));
+      }
+    }
     d.c_ready = true;
     return;
   }
@@ -714,11 +793,11 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
           launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k,
                            X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
         } else if (fast) {
-          launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p,
-                                 g, H.p, nb);
+          launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
+                                 H.p, nb);
           launch_fft_x_pick_fast(H.p, g, plist, k, X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
         } else {
-          launch_fft_planes(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
+          launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
           launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k,
                             X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
@@ -763,7 +842,7 @@ static bool build_grids(DevWF &d) {
     DevKpt &q = d.kp[k];
     for (int b0 = 0; b0 < d.nband; b0 += fbatch) {
       const int nb = std::min(fbatch, d.nband - b0);
-      launch_fft_planes_fast(d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
+      launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
                              H.p, nb);
       launch_fft_x_grid(H.p, geo[k], d.grid.p + ((size_t)k * d.nband + b0) * n3d, nb);
     }
@@ -803,6 +882,9 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   PAWPY_REQUIRE(wf && pps && fftg && labels && coords, "setup_projections: NULL argument");
   PAWPY_REQUIRE(num_elems > 0 && num_sites > 0, "setup_projections: empty structure");
   DevWF &d = mirror(wf);
+  // the coefficient upload (on the side stream, where the device reads host memory) runs during the
+  // host's table and sphere work below
+  ensure_coeffs(d);
   // attach as the reference does (projector.c:563-571); the wavefunction owns pps from now on
   if (wf->pps && wf->pps != pps) free_ppot_array(wf->pps, wf->num_elems);
   if (!wf->fftg) {
@@ -1058,8 +1140,8 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
     PAWPY_REQUIRE(qR.W == qS.W && qR.gsorted == qS.gsorted,
                   "basis and defect plane-wave sets differ at a k-point (lattice, ENCUT or k mismatch)");
     GemmBatch &g = hb[k];
-    g.A1 = R.C.p + qR.c_off;
-    g.B1 = S.C.p + qS.c_off;
+    g.A1 = coeffs(R, kR);
+    g.B1 = coeffs(S, k);
     g.lda1 = qR.Wpad;
     g.ldb1 = qS.Wpad;
     g.K1 = qR.Wpad;
@@ -1319,6 +1401,7 @@ int pawpy_gpu_prepare_basis(pswf_t *wf, int keep_real_space) {
   ensure_projections(d);
   int kept = 0;
   if (keep_real_space && !d.grid_ready) kept = build_grids(d) ? 1 : 0;
+  join_uploads(d);
   sync();
   return d.grid_ready ? 1 : kept;
   PAWPY_API_END(-1)
@@ -1332,7 +1415,9 @@ void pawpy_gpu_release(pswf_t *wf) {
 
 int pawpy_gpu_upload(pswf_t *wf) {
   PAWPY_API_BEGIN
-  ensure_coeffs(mirror(wf));
+  DevWF &d = mirror(wf);
+  ensure_coeffs(d);
+  join_uploads(d);
   sync();
   return 0;
   PAWPY_API_END(pawpy_gpu_last_error())

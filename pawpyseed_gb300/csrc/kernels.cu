@@ -2,6 +2,8 @@
 // backward 3D FFT (fft3d, linalg.c:14-45; the last pass, fused with the sphere
 // gather, is in sphere.cu), and the double-precision GEMV of the per-band
 // compensation terms (compensation_terms, projector.c:850-963).
+#include <algorithm>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "fft_tmpl.cuh"
@@ -25,25 +27,56 @@ void launch_permute(const float2 *Cu, int W, const int *perm, float2 *C, int Wpa
 }
 
 // Reads each band's coefficients in order (coalesced) from its host array and
-// scatters them to their sorted positions.
-__global__ void k_load_host_bands(const float2 *const *__restrict__ hb, int W, const int *__restrict__ inv,
-                                  float2 *__restrict__ C, int Wpad) {
-  int b = blockIdx.y;
-  const float2 *src = hb[b];
-  float2 *dst = C + (long long)b * Wpad;
-  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < Wpad; w += gridDim.x * blockDim.x) {
-    if (w < W)
-      dst[inv[w]] = src[w];
-    else
-      dst[w] = make_float2(0.f, 0.f);
+// scatters them to their sorted positions. Host reads cross the CPU-GPU link
+// with a latency of microseconds, so a thread issues LH independent loads
+// before its first store. The kernel is persistent over (band, tile of
+// LH x LH_THREADS coefficients) pairs with a few blocks: it runs beside the
+// transforms of the k-points already uploaded and leaves them most SM slots.
+namespace {
+constexpr int LH = 8;
+constexpr int LH_THREADS = 128;
+constexpr int LH_TILE = LH * LH_THREADS;
+}
+
+__global__ void __launch_bounds__(LH_THREADS) k_load_host_bands(const float2 *const *__restrict__ hb, int W,
+                                                                const int *__restrict__ inv,
+                                                                float2 *__restrict__ C, int Wpad, int nb) {
+  const int tiles = (Wpad + LH_TILE - 1) / LH_TILE;
+  for (long long t = blockIdx.x; t < (long long)tiles * nb; t += gridDim.x) {
+    const int b = (int)(t / tiles), w0 = (int)(t - (long long)b * tiles) * LH_TILE + threadIdx.x;
+    const float2 *__restrict__ src = hb[b];
+    float2 *__restrict__ dst = C + (long long)b * Wpad;
+    float2 v[LH];
+#pragma unroll
+    for (int i = 0; i < LH; i++) {
+      const int w = w0 + i * LH_THREADS;
+      v[i] = w < W ? src[w] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < LH; i++) {
+      const int w = w0 + i * LH_THREADS;
+      if (w < W)
+        dst[inv[w]] = v[i];
+      else if (w < Wpad)
+        dst[w] = v[i];
+    }
   }
 }
 
 void launch_load_host_bands(const float2 *const *host_bands, int W, const int *invperm, float2 *C, int Wpad,
                             int nb) {
   if (nb <= 0) return;
-  dim3 grid(ceil_div(Wpad, 256 * 4), nb);
-  PAWPY_LAUNCH("load_host", k_load_host_bands<<<grid, 256, 0, stream()>>>(host_bands, W, invperm, C, Wpad));
+  static int blocks = [] {
+    int sms = 0;
+    PAWPY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device()));
+    int per_sm = 1;
+    if (const char *e = getenv("PAWPY_GPU_LOAD_BLOCKS_PER_SM")) per_sm = std::max(1, atoi(e));
+    return sms * per_sm;
+  }();
+  const long long work = (long long)ceil_div(Wpad, LH_TILE) * nb;
+  const int grid = (int)std::min<long long>(blocks, work);
+  PAWPY_LAUNCH("load_host",
+               k_load_host_bands<<<grid, LH_THREADS, 0, stream()>>>(host_bands, W, invperm, C, Wpad, nb));
 }
 
 // ===================================================================== FFT

@@ -1,5 +1,6 @@
 // Error status, the library stream, stream-ordered allocation, launch
 // accounting and timers of libpawpy_gpu.
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -91,6 +92,24 @@ static thread_local cudaStream_t t_stream = nullptr;
 // between the threads' streams (which would order their work).
 static thread_local cudaMemPool_t t_pool = nullptr;
 
+// A second stream per thread for host-to-device uploads that overlap the work
+// on the thread's main stream (created on first use, at the highest priority
+// so that its blocks are scheduled as soon as SM slots free up).
+static thread_local cudaStream_t t_side = nullptr;
+
+cudaStream_t side_stream() {
+  if (!t_side) {
+    stream();
+    int lo = 0, hi = 0;
+    PAWPY_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PAWPY_CUDA(cudaStreamCreateWithPriority(&t_side, cudaStreamNonBlocking, hi));
+  }
+  return t_side;
+}
+
+OnStream::OnStream(cudaStream_t s) : prev(t_stream) { t_stream = s; }
+OnStream::~OnStream() { t_stream = prev; }
+
 cudaStream_t stream() {
   if (t_stream) return t_stream;
   Runtime &r = rt();
@@ -154,6 +173,67 @@ void sync() {
       msg = p.second + " (status " + std::to_string(st.host[p.first]) + ")";
   t_pending.clear();
   if (!msg.empty()) throw Error(ERR_DEVICE_FLAG, msg);
+}
+
+namespace {
+// Two halves; a half is reused once the copies out of it have completed (an
+// event on each stream that copied from it, recorded when the ring left it).
+constexpr size_t kRingHalf = 4u << 20;
+constexpr size_t kRingMax = 1u << 20;
+struct Ring {
+  char *buf = nullptr;
+  size_t off = 0;
+  int half = 0;
+  std::vector<cudaStream_t> used[2];
+  std::vector<cudaEvent_t> done[2];
+};
+thread_local Ring t_ring;
+
+void ring_wait(Ring &r, int h) {
+  for (cudaEvent_t e : r.done[h]) {
+    PAWPY_CUDA(cudaEventSynchronize(e));
+    PAWPY_CUDA(cudaEventDestroy(e));
+  }
+  r.done[h].clear();
+  r.used[h].clear();
+}
+
+void ring_free(Ring &r) {
+  if (!r.buf) return;
+  ring_wait(r, 0);
+  ring_wait(r, 1);
+  PAWPY_CUDA(cudaFreeHost(r.buf));
+  r = Ring();
+}
+}  // namespace
+
+void upload_bytes(void *dev, const void *h, size_t bytes) {
+  cudaStream_t s = stream();
+  if (bytes > kRingMax) {
+    PAWPY_CUDA(cudaMemcpyAsync(dev, h, bytes, cudaMemcpyHostToDevice, s));
+    return;
+  }
+  Ring &r = t_ring;
+  if (!r.buf) PAWPY_CUDA(cudaMallocHost(reinterpret_cast<void **>(&r.buf), 2 * kRingHalf));
+  const size_t need = (bytes + 255) & ~size_t(255);
+  if (r.off + need > kRingHalf) {
+    for (cudaStream_t u : r.used[r.half]) {
+      cudaEvent_t e;
+      PAWPY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      PAWPY_CUDA(cudaEventRecord(e, u));
+      r.done[r.half].push_back(e);
+    }
+    r.used[r.half].clear();
+    r.half ^= 1;
+    r.off = 0;
+    ring_wait(r, r.half);
+  }
+  char *p = r.buf + (size_t)r.half * kRingHalf + r.off;
+  std::memcpy(p, h, bytes);
+  PAWPY_CUDA(cudaMemcpyAsync(dev, p, bytes, cudaMemcpyHostToDevice, s));
+  auto &u = r.used[r.half];
+  if (std::find(u.begin(), u.end(), s) == u.end()) u.push_back(s);
+  r.off += need;
 }
 
 void *dmalloc(size_t bytes) {
@@ -279,6 +359,21 @@ int pawpy_gpu_thread_stream(int on) {
       PAWPY_CUDA(cudaMemPoolSetAttribute(t_pool, cudaMemPoolReuseAllowInternalDependencies, &no));
     }
   } else if (!on && t_stream) {
+    // the staging ring's copies were ordered on this thread's streams
+    {
+      Ring &r = t_ring;
+      for (int h = 0; h < 2; h++) {
+        for (cudaStream_t u : r.used[h]) PAWPY_CUDA(cudaStreamSynchronize(u));
+        r.used[h].clear();
+      }
+      ring_free(r);
+    }
+    if (t_side) {
+      cudaStream_t u = t_side;
+      t_side = nullptr;
+      PAWPY_CUDA(cudaStreamSynchronize(u));
+      PAWPY_CUDA(cudaStreamDestroy(u));
+    }
     cudaStream_t s = t_stream;
     PAWPY_CUDA(cudaStreamSynchronize(s));
     t_stream = nullptr;
@@ -306,6 +401,8 @@ float pawpy_gpu_timer_stop_ms(void) {
 
 void pawpy_gpu_synchronize(void) {
   PAWPY_API_BEGIN
+  // uploads still running on the thread's side stream count as the library's work
+  if (t_side) PAWPY_CUDA(cudaStreamSynchronize(t_side));
   sync();
   PAWPY_API_END()
 }
