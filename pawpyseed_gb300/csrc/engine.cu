@@ -763,52 +763,64 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   long long hcap = 96LL << 20;
   if (const char *e = getenv("PAWPY_GPU_FFT_BATCH_MB")) hcap = std::max(1LL, atoll(e)) << 20;
   int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, hcap / std::max(1LL, hband)));
-  // contraction batch: picked points and partial sums of up to 2 GiB
-  long long xstride = (xtot + 3) / 4 * 4;
-  long long per_band = (xstride + ptot) * (long long)sizeof(float2);
-  int cbatch = (int)std::max<long long>(fbatch, std::min<long long>(d.nband, (2LL << 30) / std::max(1LL, per_band)));
-  cbatch = std::max(1, cbatch / fbatch) * fbatch;
-  cbatch = std::min(cbatch, d.nband);
+  // Contraction batch: rows are (k-point, band) pairs, k-major, so that one
+  // launch covers several k-points (the tables do not depend on k; the Bloch
+  // phase is applied at the pick); picked points and partial sums of up to 2 GiB.
+  const long long xstride = (xtot + 3) / 4 * 4;
+  const long long per_row = (xstride + ptot) * (long long)sizeof(float2);
+  const long long rows = (long long)d.nk * d.nband;
+  const long long cbatch =
+      std::min({rows, 32768LL, std::max<long long>(fbatch, (2LL << 30) / std::max(1LL, per_row))});
   DevBuf<float2> H(d.grid_ready ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
   DevBuf<float2> X((size_t)cbatch * std::max(1LL, xstride));
   DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
+  std::vector<PlaneGeom> geo(d.nk);
+  std::vector<char> fast(d.nk);
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
     ensure_planes(d, q);
-    PlaneGeom g{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
+    PlaneGeom &g = geo[k];
+    g = PlaneGeom{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
     g.g2min = q.g2min;
     g.n2 = q.n2;
     g.g3min = q.g3min;
     g.n3 = q.n3;
     g.maxcnt = q.maxcnt;
-    const bool fast = q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
-    if (xtot == 0) continue;
-    for (int c0 = 0; c0 < d.nband; c0 += cbatch) {
-      int cn = std::min(cbatch, d.nband - c0);
-      for (int b0 = c0; b0 < c0 + cn; b0 += fbatch) {
-        int nb = std::min(fbatch, c0 + cn - b0);
+    fast[k] = q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
+  }
+  if (xtot == 0) return;
+  for (long long r0 = 0; r0 < rows; r0 += cbatch) {
+    const long long r1 = std::min(rows, r0 + cbatch);
+    for (int k = (int)(r0 / d.nband); (long long)k * d.nband < r1; k++) {
+      DevKpt &q = d.kp[k];
+      const PlaneGeom &g = geo[k];
+      const int blo = (int)(std::max(r0, (long long)k * d.nband) - (long long)k * d.nband);
+      const int bhi = (int)(std::min(r1, (long long)(k + 1) * d.nband) - (long long)k * d.nband);
+      for (int b0 = blo; b0 < bhi; b0 += fbatch) {
+        const int nb = std::min(fbatch, bhi - b0);
+        float2 *xb = X.p + ((long long)k * d.nband + b0 - r0) * xstride;
         if (d.grid_ready) {
           // resident real-space wavefunctions: a gather instead of the transform
           const size_t n3d = (size_t)d.N[0] * d.N[1] * d.N[2];
-          launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k,
-                           X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
-        } else if (fast) {
+          launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k, xb,
+                           xstride, nb);
+        } else if (fast[k]) {
           launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                                  H.p, nb);
-          launch_fft_x_pick_fast(H.p, g, plist, k, X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
+          launch_fft_x_pick_fast(H.p, g, plist, k, xb, xstride, nb);
         } else {
           launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k,
-                            X.p + (size_t)(b0 - c0) * xstride, xstride, nb);
+          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, xstride, nb);
         }
       }
-      launch_chunk_contract(ch_d.p, (int)chunks.size(), max_total, X.p, xstride, partial.p, ptot, cn);
-      for (size_t i = 0; i < sets.size(); i++) {
-        const SphereSet &S = *sets[i];
-        if (S.nsites == 0) continue;
-        launch_chunk_reduce(partial.p, ptot, mdev[i].p, outs[i], S.Ptot, cn, (long long)k * d.nband + c0);
-      }
+    }
+    const int cn = (int)(r1 - r0);
+    launch_chunk_contract(ch_d.p, (int)chunks.size(), max_total, X.p, xstride, partial.p, ptot, cn);
+    for (size_t i = 0; i < sets.size(); i++) {
+      const SphereSet &S = *sets[i];
+      if (S.nsites == 0) continue;
+      launch_chunk_reduce(partial.p, ptot, mdev[i].p, outs[i], S.Ptot, cn, r0);
     }
   }
 }
