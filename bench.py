@@ -304,9 +304,10 @@ def roofline(stats, w, basis, wf, lists, cr):
                    algorithmic_bytes_per_band_fft=16.0 * N3)
         if tuple(w["dim"]) == (60, 60, 60):
             # DRAM bytes of both passes per band-FFT from one ncu capture of this workload's
-            # launches (profiles/fft_planes_pipe_60cubed.md, launches of 99 bands):
-            # pass A 59.4 MB + pass B 121 MB per 99 bands
-            out.update(traffic=(59.4e6 + 121.4e6) / 99.0,
+            # launches (profiles/fft_passes_traffic_60cubed.md, launches of 256 bands, one
+            # k-point): pass A 47.9 MB read + 195.0 MB written, pass B 261.2 MB read + 99.1 MB
+            # written
+            out.update(traffic=(47.9e6 + 195.0e6 + 261.2e6 + 99.1e6) / 256.0,
                        traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")
     else:
         out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)

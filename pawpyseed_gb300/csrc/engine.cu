@@ -189,6 +189,13 @@ static bool fingerprint_ok(const DevWF &d, const pswf_t *wf) {
          d.cs0 == (const void *)wf->kpts[0]->bands[0]->Cs;
 }
 
+// Size of the plane-FFT intermediate H of one FFT sub-batch. Measured per
+// 64-atom step on the 60^3 grid (1 MiB of H per band): 64 MiB 3.97 ms, 96 MiB
+// 3.84 ms, 192 MiB 3.72 ms, 288 MiB (all 256 bands of a k-point) 3.57 ms,
+// 384 MiB 3.61 ms; fewer, longer launches of the persistent kernels outweigh
+// H leaving L2 between the passes.
+constexpr long long kFftBatchBytes = 288LL << 20;
+
 // Runs f(0..n-1) on up to n host threads (the calling thread takes index 0).
 template <typename F>
 static void parallel_for(int n, F f) {
@@ -409,34 +416,86 @@ static void set_grid(DevWF &d, const int *fftg) {
 }
 
 // Plane offsets (j*N3 + k) of the sorted plane waves for the current grid.
-static void ensure_planes(DevWF &d, DevKpt &q) {
-  if (q.off_N2 == d.N[1] && q.off_N3 == d.N[2] && q.plane_off.p) return;
+// Plane lists of one k-point for the plane FFT: start[p] = first sorted
+// coefficient of g1 plane p, off[t] = cell j * N3 + k of coefficient t within its
+// plane, and the occupied ranges of the other two axes.
+struct PlaneLists {
+  std::vector<int> start, off;
+  int g2min = 0, n2 = 0, g3min = 0, n3 = 0, maxcnt = 0;
+};
+
+static void plane_lists(const DevWF &d, const DevKpt &q, PlaneLists &pl) {
   PAWPY_REQUIRE(q.n1 <= d.N[0], "FFT grid smaller than the plane-wave sphere along the first axis");
-  std::vector<int> start(q.n1 + 1, 0), off(q.W);
+  const int N2 = d.N[1], N3 = d.N[2];
+  pl.start.assign(q.n1 + 1, 0);
+  pl.off.resize(q.W);
   int lo2 = 1 << 30, hi2 = -(1 << 30), lo3 = 1 << 30, hi3 = -(1 << 30);
   for (int t = 0; t < q.W; t++) {
-    int g1 = q.gsorted[3 * t], g2 = q.gsorted[3 * t + 1], g3 = q.gsorted[3 * t + 2];
-    start[g1 - q.g1min + 1]++;
-    int j = ((g2 % d.N[1]) + d.N[1]) % d.N[1], kk = ((g3 % d.N[2]) + d.N[2]) % d.N[2];
-    off[t] = j * d.N[2] + kk;
+    const int g2 = q.gsorted[3 * t + 1], g3 = q.gsorted[3 * t + 2];
     lo2 = std::min(lo2, g2);
     hi2 = std::max(hi2, g2);
     lo3 = std::min(lo3, g3);
     hi3 = std::max(hi3, g3);
   }
-  q.g2min = q.W ? lo2 : 0;
-  q.n2 = q.W ? hi2 - lo2 + 1 : 0;
-  q.g3min = q.W ? lo3 : 0;
-  q.n3 = q.W ? hi3 - lo3 + 1 : 0;
-  q.maxcnt = 0;
-  for (int p = 0; p < q.n1; p++) q.maxcnt = std::max(q.maxcnt, start[p + 1]);
-  for (int p = 0; p < q.n1; p++) start[p + 1] += start[p];
+  // indices inside (-N, N) wrap with one compare; others take the modulus
+  const bool near = q.W == 0 || (lo2 > -N2 && hi2 < N2 && lo3 > -N3 && hi3 < N3);
+  for (int t = 0; t < q.W; t++) {
+    const int g1 = q.gsorted[3 * t], g2 = q.gsorted[3 * t + 1], g3 = q.gsorted[3 * t + 2];
+    pl.start[g1 - q.g1min + 1]++;
+    int j, kk;
+    if (near) {
+      j = g2 < 0 ? g2 + N2 : g2;
+      kk = g3 < 0 ? g3 + N3 : g3;
+    } else {
+      j = ((g2 % N2) + N2) % N2;
+      kk = ((g3 % N3) + N3) % N3;
+    }
+    pl.off[t] = j * N3 + kk;
+  }
+  pl.g2min = q.W ? lo2 : 0;
+  pl.n2 = q.W ? hi2 - lo2 + 1 : 0;
+  pl.g3min = q.W ? lo3 : 0;
+  pl.n3 = q.W ? hi3 - lo3 + 1 : 0;
+  for (int p = 0; p < q.n1; p++) pl.maxcnt = std::max(pl.maxcnt, pl.start[p + 1]);
+  for (int p = 0; p < q.n1; p++) pl.start[p + 1] += pl.start[p];
+}
+
+static void install_planes(DevWF &d, DevKpt &q, const PlaneLists &pl) {
+  q.g2min = pl.g2min;
+  q.n2 = pl.n2;
+  q.g3min = pl.g3min;
+  q.n3 = pl.n3;
+  q.maxcnt = pl.maxcnt;
   q.plane_start.alloc(q.n1 + 1);
-  q.plane_start.upload(start.data(), q.n1 + 1);
+  q.plane_start.upload(pl.start.data(), q.n1 + 1);
   q.plane_off.alloc(std::max(q.W, 1));
-  q.plane_off.upload(off.data(), q.W);
+  q.plane_off.upload(pl.off.data(), q.W);
   q.off_N2 = d.N[1];
   q.off_N3 = d.N[2];
+}
+
+static bool planes_current(const DevWF &d, const DevKpt &q) {
+  return q.off_N2 == d.N[1] && q.off_N3 == d.N[2] && q.plane_off.p;
+}
+
+static void ensure_planes(DevWF &d, DevKpt &q) {
+  if (planes_current(d, q)) return;
+  PlaneLists pl;
+  plane_lists(d, q, pl);
+  install_planes(d, q, pl);
+}
+
+// The plane lists of every k-point, computed on host threads (the device
+// copies are made on the calling thread's stream).
+static void ensure_all_planes(DevWF &d) {
+  std::vector<int> todo;
+  for (int k = 0; k < d.nk; k++)
+    if (!planes_current(d, d.kp[k])) todo.push_back(k);
+  if (todo.empty()) return;
+  HostPhase hp("plane_lists");
+  std::vector<PlaneLists> pl(todo.size());
+  parallel_for((int)todo.size(), [&](int i) { plane_lists(d, d.kp[todo[i]], pl[i]); });
+  for (size_t i = 0; i < todo.size(); i++) install_planes(d, d.kp[todo[i]], pl[i]);
 }
 
 // ============================================================= species / spheres
@@ -760,7 +819,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   // FFT sub-batch: the plane-FFT intermediate H of a sub-batch stays within L2
   // between the two passes (PAWPY_GPU_FFT_BATCH_MB overrides the size)
   long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
-  long long hcap = 96LL << 20;
+  long long hcap = kFftBatchBytes;
   if (const char *e = getenv("PAWPY_GPU_FFT_BATCH_MB")) hcap = std::max(1LL, atoll(e)) << 20;
   int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, hcap / std::max(1LL, hband)));
   // Contraction batch: rows are (k-point, band) pairs, k-major, so that one
@@ -848,7 +907,7 @@ static bool build_grids(DevWF &d) {
   }
   d.grid.alloc((size_t)d.nk * d.nband * n3d);
   const long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
-  const int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, (96LL << 20) / std::max(1LL, hband)));
+  const int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, kFftBatchBytes / std::max(1LL, hband)));
   DevBuf<float2> H((size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
@@ -909,6 +968,7 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   wf->pps = pps;
   for (int e = 0; e < num_elems; e++) pps[e].num_cart_gridpts = cart_gridpts_bound(pps[e], wf->lattice, fftg);
   set_grid(d, fftg);
+  ensure_all_planes(d);
   d.species.clear();
   for (int e = 0; e < num_elems; e++) d.species.push_back(species_tables(pps[e]));
   d.labels.assign(labels, labels + num_sites);

@@ -75,7 +75,7 @@ long long estimate_bytes(const pswf_t *R, const pswf_t *S, int num_sites) {
   // H of one FFT sub-batch; picked points and per-chunk partial sums (<= 32 channels per chunk of
   // 256 points) of every (k, band) row, at most 2 GiB
   const long long fft =
-      (96LL << 20) + std::min(2LL << 30, nk * (8 * nbS * pts + 8 * nbS * 32 * (pts / 256 + num_sites)));
+      (288LL << 20) + std::min(2LL << 30, nk * (8 * nbS * pts + 8 * nbS * 32 * (pts / 256 + num_sites)));
   const long long tables = pts * (8 * 32 + 8 * nk + 8);
   const long long Kc = round_up(maxW + 32LL * std::max(1, num_sites), 32);
   const long long gemm = 8 * (round_up(nbR, 128) + round_up(nbS, 128)) * Kc * nk + 3 * 8 * nk * nbS * nbR * 4;
