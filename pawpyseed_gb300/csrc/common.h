@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -171,6 +172,12 @@ struct HostPhase {
   } while (0)
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Runs f(0..n-1) on the library's host worker threads and the calling thread;
+// returns when every index is done and rethrows the first exception. A call
+// made while another thread's call is running runs its indices on the calling
+// thread alone.
+void host_parallel_for(int n, const std::function<void(int)> &f);
 
 // Raises a kernel's dynamic shared-memory limit to at least bytes (thread-safe, once per size).
 void allow_dynamic_smem(const void *kernel, size_t bytes);

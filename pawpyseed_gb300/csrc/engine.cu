@@ -196,30 +196,10 @@ static bool fingerprint_ok(const DevWF &d, const pswf_t *wf) {
 // H leaving L2 between the passes.
 constexpr long long kFftBatchBytes = 288LL << 20;
 
-// Runs f(0..n-1) on up to n host threads (the calling thread takes index 0).
+// Runs f(0..n-1) on the library's host worker threads (see host_parallel_for).
 template <typename F>
 static void parallel_for(int n, F f) {
-  const int hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nt = std::min(n, std::min(hw, 16));
-  if (nt <= 1) {
-    for (int i = 0; i < n; i++) f(i);
-    return;
-  }
-  std::vector<std::exception_ptr> err(nt);
-  auto run = [&](int t) {
-    try {
-      for (int i = t; i < n; i += nt) f(i);
-    } catch (...) {
-      err[t] = std::current_exception();
-    }
-  };
-  std::vector<std::thread> th;
-  th.reserve(nt - 1);
-  for (int t = 1; t < nt; t++) th.emplace_back(run, t);
-  run(0);
-  for (auto &x : th) x.join();
-  for (auto &e : err)
-    if (e) std::rethrow_exception(e);
+  host_parallel_for(n, std::function<void(int)>(f));
 }
 
 // perm = plane-wave indices in (g1, g2, g3) order. The vectors are distinct

@@ -1,9 +1,14 @@
 // Error status, the library stream, stream-ordered allocation, launch
 // accounting and timers of libpawpy_gpu.
+#include <unistd.h>
+
 #include <algorithm>
+#include <condition_variable>
+#include <exception>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 
 #include "common.h"
 
@@ -287,6 +292,97 @@ void launch_end(const char *family) {
     PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, t_stream ? t_stream : r.s));
 }
 
+namespace {
+// Host worker pool: threads started once (detached; the pool is never
+// destroyed) that wait for jobs, so that short host loops over k-points cost
+// no thread creation. A process forked from one that used the pool starts a
+// pool of its own.
+struct HostPool {
+  pid_t pid = 0;
+  int nthreads = 0;
+  std::mutex submit;  // one job at a time
+  std::mutex m;
+  std::condition_variable cv_work, cv_done;
+  const std::function<void(int)> *job = nullptr;
+  int n = 0, next = 0, busy = 0;
+  long gen = 0;
+  std::exception_ptr err;
+
+  void run_items() {
+    for (;;) {
+      int i;
+      {
+        std::lock_guard<std::mutex> lk(m);
+        if (next >= n) return;
+        i = next++;
+      }
+      try {
+        (*job)(i);
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(m);
+        if (!err) err = std::current_exception();
+      }
+    }
+  }
+  void worker() {
+    long seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv_work.wait(lk, [&] { return gen != seen; });
+        seen = gen;
+      }
+      run_items();
+      std::lock_guard<std::mutex> lk(m);
+      if (--busy == 0) cv_done.notify_all();
+    }
+  }
+};
+
+HostPool *host_pool() {
+  static std::mutex init;
+  static HostPool *pool = nullptr;
+  std::lock_guard<std::mutex> lk(init);
+  if (!pool || pool->pid != getpid()) {
+    pool = new HostPool();  // never destroyed: its threads outlive every caller
+    pool->pid = getpid();
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    pool->nthreads = std::min(hw, 16) - 1;
+    for (int t = 0; t < pool->nthreads; t++) std::thread([p = pool] { p->worker(); }).detach();
+  }
+  return pool;
+}
+}  // namespace
+
+void host_parallel_for(int n, const std::function<void(int)> &f) {
+  HostPool *p = n > 1 ? host_pool() : nullptr;
+  std::unique_lock<std::mutex> own;
+  if (p && p->nthreads > 0) own = std::unique_lock<std::mutex>(p->submit, std::try_to_lock);
+  if (!own.owns_lock()) {
+    for (int i = 0; i < n; i++) f(i);
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> lk(p->m);
+    p->job = &f;
+    p->n = n;
+    p->next = 0;
+    p->busy = p->nthreads;
+    p->err = nullptr;
+    p->gen++;
+  }
+  p->cv_work.notify_all();
+  p->run_items();
+  std::exception_ptr e;
+  {
+    std::unique_lock<std::mutex> lk(p->m);
+    p->cv_done.wait(lk, [&] { return p->busy == 0; });
+    e = p->err;
+    p->job = nullptr;
+  }
+  if (e) std::rethrow_exception(e);
+}
+
 void allow_dynamic_smem(const void *kernel, size_t bytes) {
   static std::mutex m;
   static std::map<const void *, size_t> done;
@@ -403,7 +499,7 @@ void pawpy_gpu_synchronize(void) {
   PAWPY_API_BEGIN
   // uploads still running on the thread's side stream count as the library's work
   if (t_side) PAWPY_CUDA(cudaStreamSynchronize(t_side));
-  sync();
+  pawpy::sync();
   PAWPY_API_END()
 }
 
