@@ -524,6 +524,8 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
     s.rmax = which == 0 ? pp.rmax : pp.wave_rmax;
     s.grid_rmax = s.rmax;
     s.r0_size = nd;
+    s.h = s.grid_rmax / nd;
+    s.inv_h = nd / s.grid_rmax;
     for (int i = 0; i < t->total; i++) {
       s.lm_l[i] = t->lm_l[i];
       s.lm_m[i] = t->lm_m[i];
@@ -532,7 +534,15 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
       double f1 = 1, f2 = 1;
       for (int q = 2; q <= l - m; q++) f1 *= q;
       for (int q = 2; q <= l + m; q++) f2 *= q;
-      s.lm_norm[i] = std::sqrt((2 * l + 1) / (4 * M_PI) * f1 / f2);
+      double c = std::sqrt((2 * l + 1) / (4 * M_PI) * f1 / f2);
+      if (m < 0) {
+        // P_l^{-a} = (-1)^a (l-a)!/(l+a)! P_l^a (utils.c:379-380)
+        const int a = -m;
+        double ratio = 1.0;
+        for (int q = l - a + 1; q <= l + a; q++) ratio *= q;
+        c = c / ratio * ((a & 1) ? -1.0 : 1.0);
+      }
+      s.lm_coef[i] = c;
     }
   }
   t->D.assign((size_t)t->total * t->total, 0.0);

@@ -72,7 +72,10 @@ struct SpeciesDev {      // radial data of one element, device pointers
   double grid_rmax;      // the linear grid's rmax
   int r0_size;           // proj_gridsize used for the cutoff denominator
   int lm_l[32], lm_m[32], lm_f[32];
-  double lm_norm[32];    // sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) of each channel
+  // sqrt((2l+1)/(4 pi) (l-|m|)!/(l+|m|)!) of each channel, times (-1)^|m| (l-|m|)!/(l+|m|)!
+  // for m < 0 (P_l^-|m| from P_l^|m|): Y_lm = lm_coef P_l^|m|(cos theta) e^{i m phi}
+  double lm_coef[32];
+  double h, inv_h;       // grid_rmax / size and its inverse (spline interval)
 };
 struct SiteDesc {
   double coord[3];

@@ -121,53 +121,61 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
       // otherwise search the 27 images
       double t[3] = {path[0], path[1], path[2]}, r = s_norm(path);
       if (!(r < hmin)) {
+        // the image of least squared distance is the image of least distance (the square root
+        // is monotone and correctly rounded), so one square root at the end gives the same r
         double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
-        r = INFINITY;
+        double r2 = INFINITY;
         for (int a = -1; a <= 1; a++)
           for (int b = -1; b <= 1; b++)
             for (int c = -1; c <= 1; c++) {
               double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
               double v[3];
               s_to_cart(f, L, v);
-              double dd = s_norm(v);
-              if (dd < r) {
-                r = dd;
+              double dd = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+              if (dd < r2) {
+                r2 = dd;
                 t[0] = v[0];
                 t[1] = v[1];
                 t[2] = v[2];
               }
             }
+        r = sqrt(r2);
       }
       // Y_lm(theta, phi) of the displacement t without transcendental calls:
       // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
       // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
+      // (FP64 division is slow on this part: one reciprocal each for r and rho, and the
+      // recurrence divisors as constant multipliers; the table is rounded to FP32 after)
       double ct = 1.0, cp = 1.0, sp_ = 0.0;
       if (r != 0) {
-        ct = t[2] / r;
+        ct = t[2] * (1.0 / r);
         double rho = sqrt(t[0] * t[0] + t[1] * t[1]);
         if (rho != 0 && r - fabs(t[2]) != 0) {
-          cp = t[0] / rho;
-          sp_ = t[1] / rho;
+          const double irho = 1.0 / rho;
+          cp = t[0] * irho;
+          sp_ = t[1] * irho;
         }
       }
       double st = sqrt(fmax(0.0, 1.0 - ct * ct));
-      // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence
+      // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence:
+      // P_l^m = ((2l-1) ct P_{l-1}^m - (l+m-1) P_{l-2}^m) / (l-m)
       double P[4][4];
       P[0][0] = 1.0;
       for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * st * P[m - 1][m - 1];
       for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ct * P[m][m];
-      for (int m = 0; m <= 1; m++)
-        for (int l = m + 2; l <= 3; l++) P[l][m] = ((2 * l - 1) * ct * P[l - 1][m] - (l + m - 1) * P[l - 2][m]) / (l - m);
+      P[2][0] = (3.0 * ct * P[1][0] - 1.0 * P[0][0]) * 0.5;
+      P[3][0] = (5.0 * ct * P[2][0] - 2.0 * P[1][0]) * (1.0 / 3.0);
+      P[3][1] = (5.0 * ct * P[2][1] - 3.0 * P[1][1]) * 0.5;
       double er[4] = {1.0, cp, 0, 0}, ei[4] = {0.0, sp_, 0, 0};
       for (int m = 2; m <= 3; m++) {
         er[m] = er[m - 1] * cp - ei[m - 1] * sp_;
         ei[m] = er[m - 1] * sp_ + ei[m - 1] * cp;
       }
       // linear-grid spline interpolation (proj_interpolate, utils.c:461-475); x_j = rmax/size*j
-      double xlast = sp.grid_rmax / sp.size * (sp.size - 1);
-      int ind = (int)(r / sp.grid_rmax * sp.size);
+      double xlast = sp.h * (sp.size - 1);
+      int ind = (int)(r * sp.inv_h);
       if (ind > sp.size - 2) ind = sp.size - 2;
-      double dd = r - sp.grid_rmax / sp.size * ind;
+      double dd = r - sp.h * ind;
       double rad = 0.0;
       int last_f = -1;
       for (int lm = 0; lm < sp.total; lm++) {
@@ -180,13 +188,8 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
         }
         int am = mm < 0 ? -mm : mm;
         double plm = l <= 3 ? P[l][am] : 0.0;
-        // m = -a < 0: P_l^{-a} = (-1)^a (l-a)!/(l+a)! P_l^a (utils.c:379-380)
-        double y = sp.lm_norm[lm] * plm * rad * wscale;
-        if (mm < 0) {
-          double ratio = 1.0;
-          for (int q = l - am + 1; q <= l + am; q++) ratio *= q;  // (l+|m|)!/(l-|m|)!
-          y = y / ratio * ((am & 1) ? -1.0 : 1.0);
-        }
+        // lm_coef carries the m < 0 factor of P_l^{-|m|} (utils.c:379-380)
+        double y = sp.lm_coef[lm] * plm * rad * wscale;
         double cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
         // conj(radial * Y_lm) * dV * V^-1/2
         tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] =
