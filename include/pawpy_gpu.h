@@ -376,7 +376,9 @@ void pawpy_gpu_synchronize(void);
 /* Kernels launched by this library since the counter was last reset. */
 long long pawpy_gpu_launch_count(int reset);
 /* Per-kernel-family device time: enables CUDA-event bracketing of launches;
- * pawpy_gpu_kernel_stats writes "name ms launches\n" lines into buf. */
+ * pawpy_gpu_kernel_stats writes "name ms launches first last\n" lines into buf
+ * (first start and last end of the family's launches, or of the host phase
+ * "host.<name>", in ms after profiling was switched on). */
 void pawpy_gpu_profile(int on);
 int pawpy_gpu_kernel_stats(char *buf, int len, int reset);
 /* Bytes of device memory the library holds. */

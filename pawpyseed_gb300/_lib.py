@@ -152,7 +152,10 @@ def overlap_matrix(As, Bs, precision="fp32"):
     return out
 
 
-def kernel_stats(reset=True):
+def kernel_stats(reset=True, spans=False):
+    """{family: (ms, launches)} of the launches profiled since the last reset; with spans,
+    {family: (ms, launches, first start, last end)}, the times in ms after profiling was
+    switched on (host phases "host.<name>" on the host clock from the same moment)."""
     L = lib()
     n = L.pawpy_gpu_kernel_stats(None, 0, 0)
     buf = C.create_string_buffer(max(n, 1))
@@ -160,8 +163,8 @@ def kernel_stats(reset=True):
     check()
     out = {}
     for line in buf.value.decode().splitlines():
-        name, ms, cnt = line.split()
-        out[name] = (float(ms), int(cnt))
+        name, ms, cnt, t0, t1 = line.split()
+        out[name] = (float(ms), int(cnt), float(t0), float(t1)) if spans else (float(ms), int(cnt))
     return out
 
 

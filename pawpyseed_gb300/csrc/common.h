@@ -75,6 +75,8 @@ int device();
 // every launch and copy of the library) is another stream. Nothing may be
 // allocated inside such a scope.
 cudaStream_t side_stream();
+// The calling thread's stream for work issued ahead of the library stream's queue.
+cudaStream_t aux_stream();
 struct OnStream {
   cudaStream_t prev;
   explicit OnStream(cudaStream_t s);

@@ -89,6 +89,13 @@ struct DevWF {
   // resident real-space wavefunctions [k][band][N1][N2][N3] (a prepared basis)
   DevBuf<float2> grid;
   bool grid_ready = false;
+  // the first FFT pass of every band, issued on the auxiliary stream ahead of the sphere
+  // setup when the projections are computed later: H of k-point k at hoff[k],
+  // [band][n1 of k][N2][N3], complete at event h_ev[k]
+  DevBuf<float2> Hall;
+  std::vector<size_t> hoff;
+  std::vector<cudaEvent_t> h_ev;
+  bool h_ready = false;
   // projectors
   int N[3] = {0, 0, 0};
   std::vector<std::unique_ptr<SpeciesTables>> species;
@@ -110,6 +117,10 @@ struct DevWF {
       cudaStreamWaitEvent(stream(), e, 0);
       cudaEventDestroy(e);
     }
+    for (cudaEvent_t e : h_ev) {
+      cudaStreamWaitEvent(stream(), e, 0);
+      cudaEventDestroy(e);
+    }
   }
 };
 
@@ -120,8 +131,10 @@ static const float2 *coeffs(DevWF &d, int k) {
   return d.C.p + d.kp[k].c_off;
 }
 
+// The library stream waits for the uploads and the early transforms of d.
 static void join_uploads(DevWF &d) {
   for (cudaEvent_t e : d.c_ev) PAWPY_CUDA(cudaStreamWaitEvent(stream(), e, 0));
+  for (cudaEvent_t e : d.h_ev) PAWPY_CUDA(cudaStreamWaitEvent(stream(), e, 0));
 }
 
 struct AugKey {
@@ -393,9 +406,13 @@ static void set_grid(DevWF &d, const int *fftg) {
   for (auto &q : d.kp) q.off_N2 = q.off_N3 = 0;
   d.p_ready = false;
   d.tables_ready = false;
+  if (d.h_ready) {
+    join_uploads(d);
+    d.Hall.reset();
+    d.h_ready = false;
+  }
 }
 
-// Plane offsets (j*N3 + k) of the sorted plane waves for the current grid.
 // Plane lists of one k-point for the plane FFT: start[p] = first sorted
 // coefficient of g1 plane p, off[t] = cell j * N3 + k of coefficient t within its
 // plane, and the occupied ranges of the other two axes.
@@ -686,6 +703,64 @@ static bool generic_fft_forced() {
   return e && strcmp(e, "generic") == 0;
 }
 
+// Geometry of k-point k for the plane FFT; true when the register kernels cover it.
+static bool plane_geom(DevWF &d, int k, PlaneGeom &g) {
+  DevKpt &q = d.kp[k];
+  ensure_planes(d, q);
+  g = PlaneGeom{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
+  g.g2min = q.g2min;
+  g.n2 = q.n2;
+  g.g3min = q.g3min;
+  g.n3 = q.n3;
+  g.maxcnt = q.maxcnt;
+  return q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
+}
+
+// Largest H of all k-points that the early first FFT pass may hold.
+constexpr long long kEarlyPlanesBytes = 8LL << 30;
+
+// Issues the first FFT pass of every band and k-point on the auxiliary stream
+// (each k-point after its coefficient upload), so that it runs while the host
+// builds the sphere tables; project_bands then runs the second pass from Hall.
+// Only for grids of the register kernels and an H of at most kEarlyPlanesBytes.
+static void transform_planes_early(DevWF &d) {
+  if (d.h_ready || d.grid_ready || d.nk == 0) return;
+  std::vector<PlaneGeom> geo(d.nk);
+  std::vector<size_t> off(d.nk);
+  size_t total = 0;
+  for (int k = 0; k < d.nk; k++) {
+    if (!plane_geom(d, k, geo[k])) return;
+    off[k] = total;
+    total += (size_t)d.nband * d.kp[k].n1 * d.N[1] * d.N[2];
+  }
+  if ((long long)(total * sizeof(float2)) > kEarlyPlanesBytes) return;
+  HostPhase hp("early_planes");
+  d.Hall.alloc(std::max<size_t>(total, 1));
+  d.hoff = off;
+  if ((int)d.h_ev.size() != d.nk) {
+    for (cudaEvent_t e : d.h_ev) PAWPY_CUDA(cudaEventDestroy(e));
+    d.h_ev.assign(d.nk, nullptr);
+    for (auto &e : d.h_ev) PAWPY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // the auxiliary stream starts after the allocation and the plane lists
+  cudaEvent_t ready;
+  PAWPY_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  PAWPY_CUDA(cudaEventRecord(ready, stream()));
+  const cudaStream_t xs = aux_stream();
+  PAWPY_CUDA(cudaStreamWaitEvent(xs, ready, 0));
+  PAWPY_CUDA(cudaEventDestroy(ready));
+  {
+    OnStream on(xs);
+    for (int k = 0; k < d.nk; k++) {
+      DevKpt &q = d.kp[k];
+      launch_fft_planes_fast(coeffs(d, k), q.Wpad, q.plane_start.p, q.plane_off.p, geo[k], d.Hall.p + off[k],
+                             d.nband);
+      PAWPY_CUDA(cudaEventRecord(d.h_ev[k], xs));
+    }
+  }
+  d.h_ready = true;
+}
+
 static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
                           const std::vector<float2 *> &outs) {
   HostPhase hp("project_bands");
@@ -820,23 +895,13 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   const long long rows = (long long)d.nk * d.nband;
   const long long cbatch =
       std::min({rows, 32768LL, std::max<long long>(fbatch, (2LL << 30) / std::max(1LL, per_row))});
-  DevBuf<float2> H(d.grid_ready ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
+  const bool early = d.h_ready && !d.grid_ready;
+  DevBuf<float2> H(d.grid_ready || early ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
   DevBuf<float2> X((size_t)cbatch * std::max(1LL, xstride));
   DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<char> fast(d.nk);
-  for (int k = 0; k < d.nk; k++) {
-    DevKpt &q = d.kp[k];
-    ensure_planes(d, q);
-    PlaneGeom &g = geo[k];
-    g = PlaneGeom{d.N[0], d.N[1], d.N[2], q.g1min, q.n1};
-    g.g2min = q.g2min;
-    g.n2 = q.n2;
-    g.g3min = q.g3min;
-    g.n3 = q.n3;
-    g.maxcnt = q.maxcnt;
-    fast[k] = q.n2 <= d.N[1] && q.n3 <= d.N[2] && fft_fast_supported(g) && !generic_fft_forced();
-  }
+  for (int k = 0; k < d.nk; k++) fast[k] = plane_geom(d, k, geo[k]);
   if (xtot == 0) return;
   for (long long r0 = 0; r0 < rows; r0 += cbatch) {
     const long long r1 = std::min(rows, r0 + cbatch);
@@ -845,10 +910,16 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       const PlaneGeom &g = geo[k];
       const int blo = (int)(std::max(r0, (long long)k * d.nband) - (long long)k * d.nband);
       const int bhi = (int)(std::min(r1, (long long)(k + 1) * d.nband) - (long long)k * d.nband);
-      for (int b0 = blo; b0 < bhi; b0 += fbatch) {
-        const int nb = std::min(fbatch, bhi - b0);
+      // with the first pass done early, one second-pass launch per k-point
+      const int step = early ? std::max(1, bhi - blo) : fbatch;
+      for (int b0 = blo; b0 < bhi; b0 += step) {
+        const int nb = std::min(step, bhi - b0);
         float2 *xb = X.p + ((long long)k * d.nband + b0 - r0) * xstride;
-        if (d.grid_ready) {
+        if (early) {
+          PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
+          launch_fft_x_pick_fast(d.Hall.p + d.hoff[k] + (size_t)b0 * q.n1 * d.N[1] * d.N[2], g, plist, k, xb,
+                                 xstride, nb);
+        } else if (d.grid_ready) {
           // resident real-space wavefunctions: a gather instead of the transform
           const size_t n3d = (size_t)d.N[0] * d.N[1] * d.N[2];
           launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k, xb,
@@ -871,6 +942,11 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       if (S.nsites == 0) continue;
       launch_chunk_reduce(partial.p, ptot, mdev[i].p, outs[i], S.Ptot, cn, r0);
     }
+  }
+  if (early) {
+    // consumed: the planes go back to the pool (freed in stream order after the second pass)
+    d.Hall.reset();
+    d.h_ready = false;
   }
 }
 
@@ -959,6 +1035,9 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   for (int e = 0; e < num_elems; e++) pps[e].num_cart_gridpts = cart_gridpts_bound(pps[e], wf->lattice, fftg);
   set_grid(d, fftg);
   ensure_all_planes(d);
+  // with the projections deferred to overlap_setup_real, the first FFT pass runs now, beside the
+  // table and sphere work below
+  if (!g_host_proj) transform_planes_early(d);
   d.species.clear();
   for (int e = 0; e < num_elems; e++) d.species.push_back(species_tables(pps[e]));
   d.labels.assign(labels, labels + num_sites);

@@ -36,9 +36,15 @@ struct Runtime {
   long long bytes = 0;
   std::map<void *, size_t> sizes;
   bool profile = false;
+  // timeline origin: recorded when profiling is switched on; every launch's
+  // start and end are also taken relative to it (first start, last end per family)
+  cudaEvent_t origin = nullptr;
+  bool has_origin = false;
+  std::chrono::steady_clock::time_point host_origin;
   struct Fam {
     double ms = 0;
     long long n = 0;
+    double first = -1, last = -1;
   };
   std::map<std::string, Fam> fams;
   std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -82,6 +88,13 @@ void drain_locked(Runtime &r) {
     auto &f = r.fams[p.first];
     f.ms += ms;
     f.n += 1;
+    if (r.has_origin) {
+      float t0 = 0, t1 = 0;
+      PAWPY_CUDA(cudaEventElapsedTime(&t0, r.origin, p.second.first));
+      PAWPY_CUDA(cudaEventElapsedTime(&t1, r.origin, p.second.second));
+      if (f.first < 0 || t0 < f.first) f.first = t0;
+      if (t1 > f.last) f.last = t1;
+    }
     r.event_pool.push_back(p.second.first);
     r.event_pool.push_back(p.second.second);
   }
@@ -101,6 +114,9 @@ static thread_local cudaMemPool_t t_pool = nullptr;
 // on the thread's main stream (created on first use, at the highest priority
 // so that its blocks are scheduled as soon as SM slots free up).
 static thread_local cudaStream_t t_side = nullptr;
+// ...and a third for work issued ahead of the main stream's queue (the first FFT
+// pass of a wavefunction whose projections come later), at normal priority.
+static thread_local cudaStream_t t_aux = nullptr;
 
 cudaStream_t side_stream() {
   if (!t_side) {
@@ -110,6 +126,14 @@ cudaStream_t side_stream() {
     PAWPY_CUDA(cudaStreamCreateWithPriority(&t_side, cudaStreamNonBlocking, hi));
   }
   return t_side;
+}
+
+cudaStream_t aux_stream() {
+  if (!t_aux) {
+    stream();
+    PAWPY_CUDA(cudaStreamCreateWithFlags(&t_aux, cudaStreamNonBlocking));
+  }
+  return t_aux;
 }
 
 OnStream::OnStream(cudaStream_t s) : prev(t_stream) { t_stream = s; }
@@ -403,10 +427,16 @@ bool profiling() {
 
 void host_time(const char *name, double ms) {
   Runtime &r = rt();
+  const auto now = std::chrono::steady_clock::now();
   std::lock_guard<std::recursive_mutex> g(r.mu);
   auto &f = r.fams[std::string("host.") + name];
   f.ms += ms;
   f.n += 1;
+  // host phases on the same timeline (the host clock when profiling was switched on stands
+  // for the origin event, which the device records moments later)
+  const double t1 = std::chrono::duration<double, std::milli>(now - r.host_origin).count(), t0 = t1 - ms;
+  if (f.first < 0 || t0 < f.first) f.first = t0;
+  if (t1 > f.last) f.last = t1;
 }
 
 void note_launches(int n) {
@@ -464,12 +494,13 @@ int pawpy_gpu_thread_stream(int on) {
       }
       ring_free(r);
     }
-    if (t_side) {
-      cudaStream_t u = t_side;
-      t_side = nullptr;
-      PAWPY_CUDA(cudaStreamSynchronize(u));
-      PAWPY_CUDA(cudaStreamDestroy(u));
-    }
+    for (cudaStream_t *ps : {&t_side, &t_aux})
+      if (*ps) {
+        cudaStream_t u = *ps;
+        *ps = nullptr;
+        PAWPY_CUDA(cudaStreamSynchronize(u));
+        PAWPY_CUDA(cudaStreamDestroy(u));
+      }
     cudaStream_t s = t_stream;
     PAWPY_CUDA(cudaStreamSynchronize(s));
     t_stream = nullptr;
@@ -497,8 +528,9 @@ float pawpy_gpu_timer_stop_ms(void) {
 
 void pawpy_gpu_synchronize(void) {
   PAWPY_API_BEGIN
-  // uploads still running on the thread's side stream count as the library's work
+  // uploads and early transforms on the thread's other streams count as the library's work
   if (t_side) PAWPY_CUDA(cudaStreamSynchronize(t_side));
+  if (t_aux) PAWPY_CUDA(cudaStreamSynchronize(t_aux));
   pawpy::sync();
   PAWPY_API_END()
 }
@@ -514,6 +546,11 @@ long long pawpy_gpu_launch_count(int reset) {
 void pawpy_gpu_profile(int on) {
   Runtime &r = rt();
   std::lock_guard<std::recursive_mutex> g(r.mu);
+  if (on && !r.profile) {
+    if (!r.origin && cudaEventCreate(&r.origin) != cudaSuccess) r.origin = nullptr;
+    r.has_origin = r.origin && cudaEventRecord(r.origin, stream()) == cudaSuccess;
+    r.host_origin = std::chrono::steady_clock::now();
+  }
   r.profile = on != 0;
 }
 
@@ -525,7 +562,8 @@ int pawpy_gpu_kernel_stats(char *buf, int len, int reset) {
   std::string out;
   for (auto &f : r.fams) {
     char line[256];
-    snprintf(line, sizeof line, "%s %.6f %lld\n", f.first.c_str(), f.second.ms, f.second.n);
+    snprintf(line, sizeof line, "%s %.6f %lld %.6f %.6f\n", f.first.c_str(), f.second.ms, f.second.n,
+             f.second.first, f.second.last);
     out += line;
   }
   if (reset) r.fams.clear();
