@@ -373,6 +373,11 @@ int pawpy_gpu_thread_stream(int on);
 void pawpy_gpu_timer_start(void);
 float pawpy_gpu_timer_stop_ms(void); /* synchronizes */
 void pawpy_gpu_synchronize(void);
+/* Host-side check of the library's worker pool (no device work): `callers`
+ * threads each run a loop of n items through it at once, then a loop whose item
+ * 1 throws. Returns the number of items not run exactly once plus the loops
+ * whose exception was not passed back (0 = correct), or -1 on a bad argument. */
+int pawpy_gpu_host_pool_check(int callers, int n);
 /* Kernels launched by this library since the counter was last reset. */
 long long pawpy_gpu_launch_count(int reset);
 /* Per-kernel-family device time: enables CUDA-event bracketing of launches;

@@ -94,6 +94,8 @@ def _declare(L):
     L.pawpy_gpu_kernel_stats.argtypes = [C.c_char_p, C.c_int, C.c_int]
     L.pawpy_gpu_device_bytes.restype = C.c_longlong
     L.pawpy_gpu_pageable_memory_access.restype = C.c_int
+    L.pawpy_gpu_host_pool_check.restype = C.c_int
+    L.pawpy_gpu_host_pool_check.argtypes = [C.c_int, C.c_int]
     L.pawpy_gpu_struct_layout.restype = C.c_int
     L.pawpy_gpu_struct_layout.argtypes = [C.c_char_p, C.c_int]
 

@@ -77,6 +77,8 @@ int device();
 cudaStream_t side_stream();
 // The calling thread's stream for work issued ahead of the library stream's queue.
 cudaStream_t aux_stream();
+// Whether the calling thread orders its work on a stream of its own (pawpy_gpu_thread_stream).
+bool thread_has_stream();
 struct OnStream {
   cudaStream_t prev;
   explicit OnStream(cudaStream_t s);
@@ -176,9 +178,8 @@ struct HostPhase {
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // Runs f(0..n-1) on the library's host worker threads and the calling thread;
-// returns when every index is done and rethrows the first exception. A call
-// made while another thread's call is running runs its indices on the calling
-// thread alone.
+// returns when every index is done and rethrows the first exception. Calls of
+// several threads share the workers.
 void host_parallel_for(int n, const std::function<void(int)> &f);
 
 // Raises a kernel's dynamic shared-memory limit to at least bytes (thread-safe, once per size).

@@ -719,21 +719,40 @@ static bool plane_geom(DevWF &d, int k, PlaneGeom &g) {
 // Largest H of all k-points that the early first FFT pass may hold.
 constexpr long long kEarlyPlanesBytes = 8LL << 30;
 
+static long long l2_bytes() {
+  static long long v = -1;
+  if (v < 0) {
+    int b = 0;
+    PAWPY_CUDA(cudaDeviceGetAttribute(&b, cudaDevAttrL2CacheSize, device()));
+    v = b;
+  }
+  return v;
+}
+
 // Issues the first FFT pass of every band and k-point on the auxiliary stream
 // (each k-point after its coefficient upload), so that it runs while the host
 // builds the sphere tables; project_bands then runs the second pass from Hall.
-// Only for grids of the register kernels and an H of at most kEarlyPlanesBytes.
+// Only for grids of the register kernels, an H of at most kEarlyPlanesBytes,
+// and k-points whose H exceeds the L2 cache anyway (measured: at 36x45x50 a
+// k-point's 77 MB of H stays in L2 between the passes of the interleaved form,
+// and the early form made the second pass 2.4 times slower). Threads on a
+// stream of their own (the serving form) interleave requests instead: with
+// several requests in flight the device has work, and the early form only added
+// memory (measured: 9.7 -> 8.4 M pairs/s with 4 slots).
 static void transform_planes_early(DevWF &d) {
-  if (d.h_ready || d.grid_ready || d.nk == 0) return;
+  if (d.h_ready || d.grid_ready || d.nk == 0 || thread_has_stream()) return;
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<size_t> off(d.nk);
-  size_t total = 0;
+  size_t total = 0, kmax = 0;
   for (int k = 0; k < d.nk; k++) {
     if (!plane_geom(d, k, geo[k])) return;
     off[k] = total;
-    total += (size_t)d.nband * d.kp[k].n1 * d.N[1] * d.N[2];
+    const size_t hk = (size_t)d.nband * d.kp[k].n1 * d.N[1] * d.N[2];
+    total += hk;
+    kmax = std::max(kmax, hk);
   }
   if ((long long)(total * sizeof(float2)) > kEarlyPlanesBytes) return;
+  if ((long long)(kmax * sizeof(float2)) <= l2_bytes()) return;
   HostPhase hp("early_planes");
   d.Hall.alloc(std::max<size_t>(total, 1));
   d.hoff = off;

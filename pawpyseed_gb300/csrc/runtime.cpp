@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <condition_variable>
+#include <deque>
 #include <exception>
 #include <map>
 #include <mutex>
@@ -127,6 +128,8 @@ cudaStream_t side_stream() {
   }
   return t_side;
 }
+
+bool thread_has_stream() { return t_stream != nullptr; }
 
 cudaStream_t aux_stream() {
   if (!t_aux) {
@@ -319,46 +322,46 @@ void launch_end(const char *family) {
 namespace {
 // Host worker pool: threads started once (detached; the pool is never
 // destroyed) that wait for jobs, so that short host loops over k-points cost
-// no thread creation. A process forked from one that used the pool starts a
-// pool of its own.
+// no thread creation. Jobs of several calling threads run at once: a worker
+// takes the next item of the oldest job that has items left, and each caller
+// works on its own job too. A process forked from one that used the pool
+// starts a pool of its own.
+struct HostJob {
+  const std::function<void(int)> *f = nullptr;
+  int n = 0, next = 0, done = 0, users = 0;  // guarded by the pool's mutex
+  std::exception_ptr err;
+};
+
 struct HostPool {
   pid_t pid = 0;
   int nthreads = 0;
-  std::mutex submit;  // one job at a time
   std::mutex m;
   std::condition_variable cv_work, cv_done;
-  const std::function<void(int)> *job = nullptr;
-  int n = 0, next = 0, busy = 0;
-  long gen = 0;
-  std::exception_ptr err;
+  std::deque<HostJob *> jobs;  // jobs with items not yet handed out
 
-  void run_items() {
-    for (;;) {
-      int i;
-      {
-        std::lock_guard<std::mutex> lk(m);
-        if (next >= n) return;
-        i = next++;
-      }
-      try {
-        (*job)(i);
-      } catch (...) {
-        std::lock_guard<std::mutex> lk(m);
-        if (!err) err = std::current_exception();
-      }
+  // Runs one item of j (m held on entry and exit).
+  void run_one(HostJob *j, std::unique_lock<std::mutex> &lk) {
+    const int i = j->next++;
+    if (j->next >= j->n) jobs.erase(std::find(jobs.begin(), jobs.end(), j));
+    j->users++;
+    lk.unlock();
+    std::exception_ptr e;
+    try {
+      (*j->f)(i);
+    } catch (...) {
+      e = std::current_exception();
     }
+    lk.lock();
+    if (e && !j->err) j->err = e;
+    j->done++;
+    j->users--;
+    if (j->done == j->n && j->users == 0) cv_done.notify_all();
   }
   void worker() {
-    long seen = 0;
+    std::unique_lock<std::mutex> lk(m);
     for (;;) {
-      {
-        std::unique_lock<std::mutex> lk(m);
-        cv_work.wait(lk, [&] { return gen != seen; });
-        seen = gen;
-      }
-      run_items();
-      std::lock_guard<std::mutex> lk(m);
-      if (--busy == 0) cv_done.notify_all();
+      cv_work.wait(lk, [&] { return !jobs.empty(); });
+      run_one(jobs.front(), lk);
     }
   }
 };
@@ -380,31 +383,21 @@ HostPool *host_pool() {
 
 void host_parallel_for(int n, const std::function<void(int)> &f) {
   HostPool *p = n > 1 ? host_pool() : nullptr;
-  std::unique_lock<std::mutex> own;
-  if (p && p->nthreads > 0) own = std::unique_lock<std::mutex>(p->submit, std::try_to_lock);
-  if (!own.owns_lock()) {
+  if (!p || p->nthreads == 0) {
     for (int i = 0; i < n; i++) f(i);
     return;
   }
-  {
-    std::lock_guard<std::mutex> lk(p->m);
-    p->job = &f;
-    p->n = n;
-    p->next = 0;
-    p->busy = p->nthreads;
-    p->err = nullptr;
-    p->gen++;
-  }
+  HostJob j;
+  j.f = &f;
+  j.n = n;
+  std::unique_lock<std::mutex> lk(p->m);
+  p->jobs.push_back(&j);
   p->cv_work.notify_all();
-  p->run_items();
-  std::exception_ptr e;
-  {
-    std::unique_lock<std::mutex> lk(p->m);
-    p->cv_done.wait(lk, [&] { return p->busy == 0; });
-    e = p->err;
-    p->job = nullptr;
-  }
-  if (e) std::rethrow_exception(e);
+  while (j.next < j.n) p->run_one(&j, lk);
+  // every item is handed out (j has left the queue); wait for the ones still running
+  p->cv_done.wait(lk, [&] { return j.done == j.n && j.users == 0; });
+  lk.unlock();
+  if (j.err) std::rethrow_exception(j.err);
 }
 
 void allow_dynamic_smem(const void *kernel, size_t bytes) {
@@ -524,6 +517,34 @@ float pawpy_gpu_timer_stop_ms(void) {
   PAWPY_CUDA(cudaEventElapsedTime(&ms, r.t0, r.t1));
   return ms;
   PAWPY_API_END(-1.0f)
+}
+
+int pawpy_gpu_host_pool_check(int callers, int n) {
+  PAWPY_API_BEGIN
+  PAWPY_REQUIRE(callers >= 1 && callers <= 64 && n >= 0 && n <= (1 << 20), "host_pool_check: bad sizes");
+  std::vector<std::vector<int>> hits(callers, std::vector<int>(n, 0));
+  std::vector<int> bad(callers, 0);
+  auto one = [&](int c) {
+    host_parallel_for(n, [&](int i) { hits[c][i]++; });
+    bool threw = false;
+    try {
+      host_parallel_for(std::max(n, 2), [&](int i) {
+        if (i == 1) throw std::runtime_error("planted");
+      });
+    } catch (const std::runtime_error &) {
+      threw = true;
+    }
+    for (int i = 0; i < n; i++) bad[c] += hits[c][i] != 1;
+    bad[c] += !threw;
+  };
+  std::vector<std::thread> th;
+  for (int c = 1; c < callers; c++) th.emplace_back(one, c);
+  one(0);
+  for (auto &t : th) t.join();
+  int total = 0;
+  for (int b : bad) total += b;
+  return total;
+  PAWPY_API_END(-1)
 }
 
 void pawpy_gpu_synchronize(void) {

@@ -61,9 +61,9 @@ long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
 // Device bytes a request needs at most, from its sizes: coefficients, one FFT
 // sub-batch, picked points and partial sums, sphere tables, the overlap
-// contraction's operand planes and outputs, the first-pass planes of every
-// band (25% margin).
-long long estimate_bytes(const pswf_t *R, const pswf_t *S, int num_sites, const int *fftg) {
+// contraction's operand planes and outputs (25% margin). Workers run on
+// streams of their own, so requests never hold the early first-pass planes.
+long long estimate_bytes(const pswf_t *R, const pswf_t *S, int num_sites) {
   const long long nbS = S->nband, nbR = R->nband, nk = (long long)S->nspin * S->nwk;
   long long sumW = 0, maxW = 0;
   for (long long k = 0; k < nk; k++) {
@@ -80,9 +80,7 @@ long long estimate_bytes(const pswf_t *R, const pswf_t *S, int num_sites, const 
   const long long tables = pts * (8 * 32 + 8 * nk + 8);
   const long long Kc = round_up(maxW + 32LL * std::max(1, num_sites), 32);
   const long long gemm = 8 * (round_up(nbR, 128) + round_up(nbS, 128)) * Kc * nk + 3 * 8 * nk * nbS * nbR * 4;
-  // the first FFT pass of every band, held until the second (at most 8 GiB)
-  const long long planes = std::min(8LL << 30, 8 * nbS * nk * (long long)fftg[0] * fftg[1] * fftg[2]);
-  return (coeff + fft + tables + gemm + planes) / 4 * 5;
+  return (coeff + fft + tables + gemm) / 4 * 5;
 }
 
 bool admissible(const Server &s) {
@@ -225,7 +223,7 @@ long long pawpy_gpu_server_submit(void *server, const pawpy_gpu_request_t *reque
   std::lock_guard<std::mutex> lk(s->mu);
   PAWPY_REQUIRE(request->basis >= 0 && request->basis < (int)s->bases.size(), "pawpy_gpu_server_submit: no such basis");
   PAWPY_REQUIRE(!s->stop, "pawpy_gpu_server_submit: server stopping");
-  q->est = estimate_bytes(s->bases[request->basis].wf, request->wf, request->num_sites, q->fftg);
+  q->est = estimate_bytes(s->bases[request->basis].wf, request->wf, request->num_sites);
   PAWPY_REQUIRE(q->est <= s->budget, "pawpy_gpu_server_submit: request larger than the memory budget");
   q->id = s->next_id++;
   q->t_submit = Clock::now();

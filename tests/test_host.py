@@ -196,3 +196,16 @@ def test_collinear_and_noncollinear_classes_refuse_each_other():
         Wavefunction.from_arrays(bs, cr, w["dim"], ncl)
     with pytest.raises(PAWpyError):
         NCLWavefunction.from_arrays(bs, cr, w["dim"], col)
+
+
+def test_host_worker_pool_runs_concurrent_loops_once_each():
+    from pawpyseed_gb300 import _lib
+
+    L = _lib.lib()
+    # one caller, then eight callers sharing the workers; a thrown item reaches its caller
+    assert L.pawpy_gpu_host_pool_check(1, 37) == 0
+    assert L.pawpy_gpu_host_pool_check(8, 1000) == 0
+    assert L.pawpy_gpu_host_pool_check(4, 0) == 0
+    assert L.pawpy_gpu_host_pool_check(0, 5) == -1
+    with pytest.raises(_lib.PAWpyGPUError):
+        _lib.check()
