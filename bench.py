@@ -371,7 +371,8 @@ def run_reference(args, rank, world, pg):
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(cores()))
     work = make_workload(args.workload, args.bands, args.nk)
-    w = work[0]
+    w, basis_s, defect_s, cr = work[:4]
+    work = work + (site_lists(basis_s, defect_s, cr),)
     nb_s = args.cpu_sample_bands
     for _ in range(args.warmup):
         cpu_sample(work, nb_s)
