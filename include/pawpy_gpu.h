@@ -269,6 +269,20 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
                           int *M_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S,
                           int flip_spin);
 
+/* Band character of every defect band, from the full overlap matrix that
+ * pawpy_gpu_project_all forms, without moving the matrix to the host: the
+ * reductions of Projector.proportion_conduction (projector.py:384-424) for all
+ * bands at once. With S[bS][bR*NK + k] that matrix (k = s*nwk + kk),
+ *   v[bS*nch + ch] = sum over bR and the k of channel ch of |S|^2 w_v[bR*NK + k]
+ * and c likewise with w_c. nch = 1 sums every k; nch = 2 gives the two spins
+ * separately (k < nwk is spin 0). The weights (occupations or their complement,
+ * k-point weights) come from the caller. Same prerequisites as
+ * pawpy_gpu_project_all. Returns 0 on success. */
+int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, int num_M,
+                             int num_N_R, int num_N_S, int num_N_RS, int *M_R, int *M_S,
+                             int *N_R, int *N_S, int *N_RS_R, int *N_RS_S, const double *w_v,
+                             const double *w_c, int nch, int flip_spin);
+
 /* WAVECAR reader producing a pswf_t with the reference's layout and VASP plane-
  * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf. */
 pswf_t *pawpy_gpu_read_wavefunctions(const char *filename, const double *kpt_weights);

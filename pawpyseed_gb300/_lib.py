@@ -61,6 +61,9 @@ def _declare(L):
     L.pawpy_gpu_project_all.restype = C.c_int
     L.pawpy_gpu_project_all.argtypes = [_zp, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
                                         _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
+    L.pawpy_gpu_band_character.restype = C.c_int
+    L.pawpy_gpu_band_character.argtypes = [_dp, _dp, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           _vp, _vp, _vp, _vp, _vp, _vp, _dp, _dp, C.c_int, C.c_int]
     L.fft3d.argtypes = [_zp, _vp, _dp, _dp, _ip, _vp, C.c_int, _ip]
     L.onto_projector.argtypes = [C.POINTER(S.kpoint_t), C.c_int, C.POINTER(S.real_proj_site_t), C.c_int,
                                  _vp, _dp, _dp, C.c_int, _ip]

@@ -106,4 +106,56 @@ void launch_extract_band(const float2 *S, int nk, int nbS, int nbR, int band, do
   PAWPY_LAUNCH("extract", k_extract_band<<<ceil_div(nk * nbR, 256), 256, 0, stream()>>>(S, nk, nbS, nbR, band, out));
 }
 
+// One block per defect band: the weighted sums of |S|^2 over (basis band, k),
+// per channel, reduced in a fixed order (FP64).
+namespace {
+constexpr int BC_THREADS = 256;
+}
+
+__global__ void __launch_bounds__(BC_THREADS)
+    k_band_character(const float2 *__restrict__ S, int nk, int nbS, int nbR, const double *__restrict__ wv,
+                     const double *__restrict__ wc, int nwk, int nch, double *__restrict__ v,
+                     double *__restrict__ c) {
+  __shared__ double red[4][BC_THREADS];
+  const int bS = blockIdx.x;
+  double sv[2] = {0.0, 0.0}, sc[2] = {0.0, 0.0};
+  const long long n = (long long)nk * nbR;
+  for (long long e = threadIdx.x; e < n; e += BC_THREADS) {
+    const int k = (int)(e / nbR), bR = (int)(e - (long long)k * nbR);
+    const float2 s = S[((long long)k * nbS + bS) * nbR + bR];
+    const double p = (double)s.x * s.x + (double)s.y * s.y;
+    const long long w = (long long)bR * nk + k;
+    if (nch > 1 && k >= nwk) {
+      sv[1] += p * wv[w];
+      sc[1] += p * wc[w];
+    } else {
+      sv[0] += p * wv[w];
+      sc[0] += p * wc[w];
+    }
+  }
+  red[0][threadIdx.x] = sv[0];
+  red[1][threadIdx.x] = sv[1];
+  red[2][threadIdx.x] = sc[0];
+  red[3][threadIdx.x] = sc[1];
+  __syncthreads();
+  for (int h = BC_THREADS / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int q = 0; q < 4; q++) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x < nch) {
+    v[(long long)bS * nch + threadIdx.x] = red[threadIdx.x][0];
+    c[(long long)bS * nch + threadIdx.x] = red[2 + threadIdx.x][0];
+  }
+}
+
+void launch_band_character(const float2 *S, int nk, int nbS, int nbR, const double *wv, const double *wc, int nwk,
+                           int nch, double *v, double *c) {
+  if (nbS <= 0) return;
+  if (nch < 1 || nch > 2 || (nch == 2 && nk != 2 * nwk))
+    throw Error(ERR_ARG, "band character: one channel, or two spin channels of nwk k-points each");
+  PAWPY_LAUNCH("band_character",
+               k_band_character<<<nbS, BC_THREADS, 0, stream()>>>(S, nk, nbS, nbR, wv, wc, nwk, nch, v, c));
+}
+
 }  // namespace pawpy

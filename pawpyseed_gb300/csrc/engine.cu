@@ -1663,6 +1663,20 @@ void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t 
   PAWPY_API_END()
 }
 
+// The full overlap matrix <psi_R|psi_S> of every band pair on the device,
+// Smat[k][bS][bR] = pseudo overlap + PAW terms (one contraction over the
+// augmented columns).
+static void full_overlap(PairState &ps, const std::vector<int> lists[6], int flip_spin, DevBuf<float2> &Smat) {
+  ensure_aug(ps, lists, flip_spin);
+  DevWF &R = *ps.R, &S = *ps.S;
+  int nk = S.nk, npairs = (int)ps.N_RS_R.size();
+  DevBuf<float2> B32((size_t)nk * S.nband * std::max(16, ps.Kcpad));
+  launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, 0, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
+               ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
+  Smat.alloc((size_t)nk * S.nband * R.nband);
+  overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p);
+}
+
 int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M, int num_N_R, int num_N_S,
                           int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S,
                           int flip_spin) {
@@ -1672,14 +1686,10 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
   PairState &ps = pair_state(wf_R, wf_S);
   std::vector<int> lists[6];
   gather_lists(lists, num_M, num_N_R, num_N_S, num_N_RS, M_R, M_S, N_R, N_S, N_RS_R, N_RS_S);
-  ensure_aug(ps, lists, flip_spin);
+  DevBuf<float2> Smat;
+  full_overlap(ps, lists, flip_spin, Smat);
   DevWF &R = *ps.R, &S = *ps.S;
-  int nk = S.nk, npairs = (int)ps.N_RS_R.size();
-  DevBuf<float2> B32((size_t)nk * S.nband * std::max(16, ps.Kcpad));
-  launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, 0, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
-               ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
-  DevBuf<float2> Smat((size_t)nk * S.nband * R.nband);
-  overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p);
+  const int nk = S.nk;
   if (pageable_access()) {
     // the device writes the caller's (pageable) array through the host page tables
     launch_to_host_layout(Smat.p, nk, S.nband, R.nband, reinterpret_cast<double2 *>(out));
@@ -1688,6 +1698,30 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
     launch_to_host_layout(Smat.p, nk, S.nband, R.nband, o64.p);
     o64.download(reinterpret_cast<double2 *>(out), o64.n);
   }
+  sync();
+  return 0;
+  PAWPY_API_END(pawpy_gpu_last_error())
+}
+
+int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, int num_M, int num_N_R,
+                             int num_N_S, int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S, int *N_RS_R,
+                             int *N_RS_S, const double *w_v, const double *w_c, int nch, int flip_spin) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("pawpy_gpu_band_character");
+  PAWPY_REQUIRE(v && c && wf_R && wf_S && w_v && w_c, "pawpy_gpu_band_character: NULL argument");
+  PairState &ps = pair_state(wf_R, wf_S);
+  std::vector<int> lists[6];
+  gather_lists(lists, num_M, num_N_R, num_N_S, num_N_RS, M_R, M_S, N_R, N_S, N_RS_R, N_RS_S);
+  DevBuf<float2> Smat;
+  full_overlap(ps, lists, flip_spin, Smat);
+  DevWF &R = *ps.R, &S = *ps.S;
+  const int nk = S.nk, nw = (int)((size_t)R.nband * nk);
+  DevBuf<double> wv(nw), wc(nw), dv((size_t)S.nband * nch), dc((size_t)S.nband * nch);
+  wv.upload(w_v, nw);
+  wc.upload(w_c, nw);
+  launch_band_character(Smat.p, nk, S.nband, R.nband, wv.p, wc.p, S.nwk, nch, dv.p, dc.p);
+  dv.download(v, dv.n);
+  dc.download(c, dc.n);
   sync();
   return 0;
   PAWPY_API_END(pawpy_gpu_last_error())

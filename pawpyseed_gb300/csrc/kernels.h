@@ -169,6 +169,10 @@ void launch_aug_b(const float2 *P, int Pt, const float2 *WP, int Pw, int nbtot, 
 // out[bS][bR][k] = (complex double) S[k][bS][bR]
 void launch_to_host_layout(const float2 *S, int nk, int nbS, int nbR, double2 *out);
 // out[bR][k] = S[k][band][bR]
+// v[bS*nch + ch] = sum over (bR, k) of channel ch of |S[k][bS][bR]|^2 wv[bR*nk + k], c likewise
+// with wc; one channel (nch = 1) or two spin channels (nch = 2, k >= nwk is spin 1)
+void launch_band_character(const float2 *S, int nk, int nbS, int nbR, const double *wv, const double *wc, int nwk,
+                           int nch, double *v, double *c);
 void launch_extract_band(const float2 *S, int nk, int nbS, int nbR, int band, double2 *out);
 
 // ---- compensation (FP64) ----

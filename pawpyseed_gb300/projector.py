@@ -140,6 +140,32 @@ class Projector:
         _lib.check()
         return out
 
+    def band_character(self, spinpol=False, flip_spin=False):
+        """(v, c) of every defect band, as proportion_conduction gives them for one
+        band (projector.py:384-424), reduced on the device from the full overlap
+        matrix: arrays [nband_wf] (or [nband_wf, nspin] with spinpol) of the
+        valence and conduction character."""
+        basis, wf = self.basis, self.wf
+        nwk, nspin = basis.nwk, basis.nspin
+        nk = nwk * nspin
+        occs = np.asarray(basis._get_occs(), dtype=np.float64).reshape(basis.nband, nk)
+        kw = np.tile(np.asarray(wf.kws, dtype=np.float64), nspin)[None, :]
+        if spinpol:
+            w_v, w_c, nch = occs * kw, (1.0 - occs) * kw, nspin
+        else:
+            full = occs > 0.5
+            w_v, w_c, nch = np.where(full, kw / nspin, 0.0), np.where(full, 0.0, kw / nspin), 1
+        v = np.zeros(wf.nband * nch)
+        c = np.zeros(wf.nband * nch)
+        L = _lib.lib()
+        L.pawpy_gpu_band_character(v, c, basis.wf_ptr, wf.wf_ptr, len(self.M_R), len(self.N_R), len(self.N_S),
+                                   len(self.N_RS_R), *self._lists(), np.ascontiguousarray(w_v.ravel()),
+                                   np.ascontiguousarray(w_c.ravel()), nch, int(flip_spin))
+        _lib.check()
+        if spinpol:
+            return v.reshape(wf.nband, nch), c.reshape(wf.nband, nch)
+        return v, c
+
     # -- reductions (projector.py:384-503) -----------------------------------
 
     def proportion_conduction(self, band_num, spinpol=False):
@@ -189,7 +215,15 @@ class Projector:
                 vbm = vbmband
             min_band, max_band = max(vbm - num_below_ef, 0), min(vbm + num_above_ef, self.wf.nband - 1)
             totest = list(range(min_band, max_band + 1))
-        results = {b: self.proportion_conduction(b, spinpol=spinpol) for b in totest}
+        if self.method == "pseudo":
+            results = {b: self.proportion_conduction(b, spinpol=spinpol) for b in totest}
+        else:
+            # every band's character in one device reduction
+            v, c = self.band_character(spinpol=spinpol)
+            if spinpol:
+                results = {b: (v[b].tolist(), c[b].tolist()) for b in totest}
+            else:
+                results = {b: (float(v[b]), float(c[b])) for b in totest}
         if return_energies:
             return results, self.wf._get_energy_list(totest)
         return results

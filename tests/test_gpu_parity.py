@@ -211,6 +211,42 @@ def test_defect_band_analysis_aug_real(workload_dirs, oracle_projectors):
     assert len(sp) == basis.nband and len(sp[0][0]) == 2
 
 
+@pytest.mark.parametrize("name", ["cfg0", "cfg3s"])
+def test_band_character_reduction_matches_per_band_reduction(name, workload_dirs):
+    """The device reduction of every band's character equals proportion_conduction band by
+    band (which reduces the host copy of single_band_projection), with and without spin
+    channels."""
+    from pawpyseed_gb300.projector import Projector
+
+    basis, wf = load(workload_dirs(name))
+    pr = Projector(wf, basis)
+    v, c = pr.band_character()
+    vs, cs = pr.band_character(spinpol=True)
+    assert v.shape == (wf.nband,) and vs.shape == (wf.nband, basis.nspin)
+    # the same reductions of the same matrix on the host (only the summation order differs)
+    S2 = np.abs(pr.project_all()) ** 2
+    nwk, nspin = basis.nwk, basis.nspin
+    occ = np.asarray(basis._get_occs(), np.float64)
+    kw = np.asarray(wf.kws, np.float64)[np.arange(S2.shape[1]) % nwk]
+    full = occ > 0.5
+    assert np.allclose(v, S2 @ np.where(full, kw / nspin, 0), rtol=1e-9, atol=1e-12)
+    assert np.allclose(c, S2 @ np.where(full, 0, kw / nspin), rtol=1e-9, atol=1e-12)
+    spin = (np.arange(S2.shape[1]) // nwk) % nspin
+    for s_ in range(nspin):
+        m = spin == s_
+        assert np.allclose(vs[:, s_], S2[:, m] @ (occ * kw)[m], rtol=1e-9, atol=1e-12)
+        assert np.allclose(cs[:, s_], S2[:, m] @ ((1 - occ) * kw)[m], rtol=1e-9, atol=1e-12)
+    # and the per-band reduction of single_band_projection (pseudo overlap plus the FP64 PAW
+    # terms per band) within the path's bar
+    for b in range(wf.nband):
+        mv, mc = pr.proportion_conduction(b)
+        assert abs(v[b] - mv) <= TOL and abs(c[b] - mc) <= TOL
+        sv, sc = pr.proportion_conduction(b, spinpol=True)
+        assert np.abs(vs[b] - sv).max() <= TOL and np.abs(cs[b] - sc).max() <= TOL
+    res = pr.defect_band_analysis(analyze_all=True)
+    assert all(res[b] == (float(v[b]), float(c[b])) for b in range(wf.nband))
+
+
 def test_self_projection_of_bands_is_identity_on_pseudo_part(workload_dirs):
     """Projecting a structure onto itself: pseudo overlaps of normalised bands have unit diagonal."""
     from pawpyseed_gb300.projector import Projector
