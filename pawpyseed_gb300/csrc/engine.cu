@@ -739,8 +739,12 @@ static long long l2_bytes() {
 // stream of their own (the serving form) interleave requests instead: with
 // several requests in flight the device has work, and the early form only added
 // memory (measured: 9.7 -> 8.4 M pairs/s with 4 slots).
+// PAWPY_GPU_EARLY_FFT=1 uses the early form whatever the size (0: never).
 static void transform_planes_early(DevWF &d) {
   if (d.h_ready || d.grid_ready || d.nk == 0 || thread_has_stream()) return;
+  const char *sw = getenv("PAWPY_GPU_EARLY_FFT");
+  if (sw && sw[0] == '0') return;
+  const bool force = sw && sw[0] == '1';
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<size_t> off(d.nk);
   size_t total = 0, kmax = 0;
@@ -752,7 +756,7 @@ static void transform_planes_early(DevWF &d) {
     kmax = std::max(kmax, hk);
   }
   if ((long long)(total * sizeof(float2)) > kEarlyPlanesBytes) return;
-  if ((long long)(kmax * sizeof(float2)) <= l2_bytes()) return;
+  if (!force && (long long)(kmax * sizeof(float2)) <= l2_bytes()) return;
   HostPhase hp("early_planes");
   d.Hall.alloc(std::max<size_t>(total, 1));
   d.hoff = off;

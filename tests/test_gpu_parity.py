@@ -138,24 +138,31 @@ def test_project_all_matches_band_loop(name, workload_dirs, oracle_projectors):
 
 
 @pytest.mark.parametrize("name", ["cfg1s", "cfg2s", "cfg3s"])
-def test_deferred_projections_single_fft_pass(name, workload_dirs, oracle_projectors):
+def test_deferred_projections_single_fft_pass(name, workload_dirs, oracle_projectors, monkeypatch):
     """With host projection_t output off, <p|psi> and the smoothed-partial-wave projections of a
-    wavefunction come from one FFT pass; results equal the FP64 truth."""
+    wavefunction come from one FFT pass; results equal the FP64 truth. The first pass issued
+    early (at setup, on the auxiliary stream, for every k-point) and the interleaved form give
+    the same overlaps bit for bit."""
     from pawpyseed_gb300 import _lib
     from pawpyseed_gb300.projector import Projector
 
     L = _lib.lib()
     L.pawpy_gpu_set_host_projections(0)
+    op = oracle_projectors(name)
+    truth = op.full()
     try:
-        basis, wf = load(workload_dirs(name))
-        pr = Projector(wf, basis)
-        full = pr.project_all()
-        op = oracle_projectors(name)
-        truth = op.full()
-        tv = np.array([op.band_vector(truth, b) for b in range(wf.nband)])
-        assert np.abs(full - tv).max() <= TOL
-        one = pr.single_band_projection(wf.nband - 1)
-        assert np.abs(one - tv[-1]).max() <= TOL
+        fulls = {}
+        for early in ("1", "0"):
+            monkeypatch.setenv("PAWPY_GPU_EARLY_FFT", early)
+            basis, wf = load(workload_dirs(name))
+            pr = Projector(wf, basis)
+            full = pr.project_all()
+            tv = np.array([op.band_vector(truth, b) for b in range(wf.nband)])
+            assert np.abs(full - tv).max() <= TOL
+            one = pr.single_band_projection(wf.nband - 1)
+            assert np.abs(one - tv[-1]).max() <= TOL
+            fulls[early] = full
+        assert np.array_equal(fulls["1"], fulls["0"])
     finally:
         L.pawpy_gpu_set_host_projections(1)
 
