@@ -167,6 +167,22 @@ def test_deferred_projections_single_fft_pass(name, workload_dirs, oracle_projec
         L.pawpy_gpu_set_host_projections(1)
 
 
+def test_copied_and_in_place_coefficients_agree(workload_dirs, monkeypatch):
+    """The coefficient upload by copies (hosts whose device cannot read pageable memory) and by
+    in-place reads of the host arrays give the same overlaps bit for bit."""
+    from pawpyseed_gb300.projector import Projector
+
+    outs = []
+    for copy in ("1", ""):
+        if copy:
+            monkeypatch.setenv("PAWPY_GPU_NO_HOST_READ", copy)
+        else:
+            monkeypatch.delenv("PAWPY_GPU_NO_HOST_READ", raising=False)
+        basis, wf = load(workload_dirs("cfg1s"))
+        outs.append(Projector(wf, basis).project_all())
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_results_deterministic_and_cached(workload_dirs):
     from pawpyseed_gb300.projector import Projector
 
