@@ -9,6 +9,7 @@ the reference's (``pswf_t``), created by the library's WAVECAR reader.
 """
 
 import ctypes as C
+import bz2
 import gzip
 import os
 import shutil
@@ -117,9 +118,12 @@ class Wavefunction:
         kws = np.ascontiguousarray(vr.actual_kpoints_weights, dtype=np.float64)
         path = str(wavecar)
         tmp = None
-        if path.endswith(".gz"):
+        # compressed WAVECARs are inflated on the host first (pawpyc.pyx:217-222 reads them
+        # through zopen for names containing .gz or .bz2)
+        opener = gzip.open if ".gz" in path else bz2.open if ".bz2" in path else None
+        if opener is not None:
             tmp = tempfile.NamedTemporaryFile(delete=False)
-            with gzip.open(path, "rb") as src:
+            with opener(path, "rb") as src:
                 shutil.copyfileobj(src, tmp)
             tmp.close()
             path = tmp.name

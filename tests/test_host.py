@@ -63,6 +63,36 @@ def test_wavecar_reader_matches_numpy_reader(workload_dirs):
         L.pawpy_gpu_free_pswf(p)
 
 
+@pytest.mark.parametrize("suffix", [".gz", ".bz2"])
+def test_compressed_wavecar_reads_as_the_plain_file(suffix, workload_dirs, tmp_path):
+    import bz2
+    import gzip
+    import shutil
+
+    from pawpyseed_gb300.wavefunction import Wavefunction
+
+    d = workload_dirs("cfg0")["defect"]
+    for f in ("CONTCAR", "POTCAR", "vasprun.xml"):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    opener = gzip.open if suffix == ".gz" else bz2.open
+    with open(os.path.join(d, "WAVECAR"), "rb") as src, opener(tmp_path / ("WAVECAR" + suffix), "wb") as dst:
+        shutil.copyfileobj(src, dst)
+    plain = Wavefunction.from_directory(d)
+    packed = Wavefunction.from_files(str(tmp_path / "CONTCAR"), str(tmp_path / ("WAVECAR" + suffix)),
+                                     str(tmp_path / "POTCAR"), str(tmp_path / "vasprun.xml"))
+    a, b = plain.wf_ptr.contents, packed.wf_ptr.contents
+    assert (a.nspin, a.nwk, a.nband) == (b.nspin, b.nwk, b.nband)
+    for k in range(a.nspin * a.nwk):
+        ka, kb = a.kpts[k].contents, b.kpts[k].contents
+        assert ka.num_waves == kb.num_waves
+        for band in (0, a.nband - 1):
+            ca = np.ctypeslib.as_array(C.cast(ka.bands[band].contents.Cs, C.POINTER(C.c_float)),
+                                       shape=(2 * ka.num_waves,))
+            cb = np.ctypeslib.as_array(C.cast(kb.bands[band].contents.Cs, C.POINTER(C.c_float)),
+                                       shape=(2 * kb.num_waves,))
+            assert np.array_equal(ca, cb)
+
+
 def test_reference_wavecar_fixture_gsphere(golden):
     """The plane-wave enumeration reproduces the Ga4 WAVECAR's counts (945 at k0)."""
     from pawpyseed_gb300 import vaspio
