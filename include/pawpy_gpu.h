@@ -271,7 +271,7 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
 
 /* Band character of every defect band, from the full overlap matrix that
  * pawpy_gpu_project_all forms, without moving the matrix to the host: the
- * reductions of Projector.proportion_conduction (projector.py:384-424) for all
+ * reductions of Projector.proportion_conduction (projector.py:384-435) for all
  * bands at once. With S[bS][bR*NK + k] that matrix (k = s*nwk + kk),
  *   v[bS*nch + ch] = sum over bR and the k of channel ch of |S|^2 w_v[bR*NK + k]
  * and c likewise with w_c. nch = 1 sums every k; nch = 2 gives the two spins

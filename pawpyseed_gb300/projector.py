@@ -142,7 +142,7 @@ class Projector:
 
     def band_character(self, spinpol=False, flip_spin=False):
         """(v, c) of every defect band, as proportion_conduction gives them for one
-        band (projector.py:384-424), reduced on the device from the full overlap
+        band (projector.py:384-435), reduced on the device from the full overlap
         matrix: arrays [nband_wf] (or [nband_wf, nspin] with spinpol) of the
         valence and conduction character."""
         basis, wf = self.basis, self.wf
