@@ -1,17 +1,27 @@
 """Band-pair projection throughput on one GB300 (pawpyseed aug_real path).
 
 A step is the defect-side work of BasisExpansion-style analysis against a
-resident basis: element setup (get_projector_list), <p|psi> of every defect
+resident basis: element setup (get_projector_list, run in full every step:
+its per-input cache is switched off while timing), <p|psi> of every defect
 band (setup_projections: batched scatter + 3D FFT + sphere gather), the
-overlap setup (overlap_setup_real: smoothed partial waves, N_RS pairs) and the
-full PAW overlap matrix of every defect band against every basis band
-(pseudo overlap + O_M + O_R + O_S + O_N). The metric counts band pairs
-NB_R * NB_S * NK per step.
+overlap setup (overlap_setup_real: smoothed partial waves on both sides, N_RS
+pair matrices) and the full PAW overlap matrix of every defect band against
+every basis band (pseudo overlap + O_M + O_R + O_S + O_N). The metric counts
+band pairs NB_R * NB_S * NK per step. The basis is resident: its coefficients,
+projector coefficients and real-space wavefunctions stay in HBM (not timed).
 
-Workload (default): the 64-atom cubic 10.86 A cell, two species (A: l=0,0,1,1;
-B: l=0,0,1,1,2,2), one A atom removed in the defect, 8 k-points (2x2x2 MP),
-256 bands, ENCUT 400 eV (23,234 plane waves), FFT grid 60^3; synthetic seeded
-coefficients (no dataset exists for this path).
+Headline workload (--workload 2, the largest configuration): the 216-atom cubic
+16.29 A cell (species A:B = 3:1 on diamond sites), defect = two A->B
+substitutions plus seeded displacements within +-0.05 A, Gamma only, 1024
+bands, ENCUT 400 eV (78,517 plane waves), FFT grid 90^3. The 64-atom cell (8
+k-points, 256 bands, 60^3) is measured the same way and reported in the same
+line under "secondary". Synthetic seeded coefficients (no dataset exists for
+this path).
+
+Every timed result is checked: after timing, the overlaps of a seeded sample
+of defect and basis bands at every k-point are compared with an FP64
+evaluation of the same inputs by the oracle, and the line is printed only when
+the largest error is within 1e-5 (the metric's accuracy bar).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -28,21 +38,28 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+TOL = 1e-5  # max |overlap error| vs FP64 of the metric
+
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", type=int, default=1)
+    ap.add_argument("--workload", type=int, default=2)
+    ap.add_argument("--secondary", type=int, default=1, help="second workload in the same line (-1: none)")
     ap.add_argument("--bands", type=int, default=None, help="reduced band count (testing only)")
     ap.add_argument("--nk", type=int, default=None, help="reduced k-point count (testing only)")
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16x3", "tf32"])
-    ap.add_argument("--cpu-sample-bands", type=int, default=16)
+    ap.add_argument("--sample-defect-bands", type=int, default=8,
+                    help="defect bands of the CPU sample and of the FP64 check")
+    ap.add_argument("--sample-basis-bands", type=int, default=32,
+                    help="basis bands of the CPU sample and of the FP64 check")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="leave the serving streams out of the line")
     ap.add_argument("--serve", action="store_true",
-                    help="replay the serving stream (Poisson requests against resident bases) instead")
+                    help="replay only the serving stream (Poisson requests against resident bases)")
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0, help="mean request arrival rate (1/s)")
     ap.add_argument("--slots", type=int, default=4, help="requests in flight at once")
@@ -84,7 +101,7 @@ class Clocks:
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.p = None
@@ -120,6 +137,17 @@ class Clocks:
 
 # ---------------------------------------------------------------- workload
 
+WORKLOAD_NAMES = {
+    0: "8-atom cubic 5.43 A cell, atom 0 moved 0.1 A, 4 k-points, {nb} bands, ENCUT 300 eV, FFT {g}, aug_real",
+    1: "64-atom cubic 10.86 A A/B cell minus one A, 8 k-points (2x2x2 MP), {nb} bands, ENCUT 400 eV, FFT {g}, "
+       "aug_real",
+    2: "216-atom cubic 16.29 A A/B (3:1) cell, two A->B substitutions and displacements within 0.05 A, "
+       "Gamma only, {nb} bands, ENCUT 400 eV, FFT {g}, aug_real",
+    3: "96-atom orthorhombic 10x12x14 A A/B cell, 2 spins x 24 irregular k-points, {nb} bands, ENCUT 450 eV, "
+       "FFT {g}, aug_real",
+}
+
+
 def make_workload(cfg, bands, nk):
     from pawpyseed_gb300 import synth, vaspio
 
@@ -146,23 +174,35 @@ def site_lists(basis_s, defect_s, cr):
     return [a(M_R), a(M_S), a(N_R), a(N_S), a([x for x, _ in N_RS]), a([y for _, y in N_RS])]
 
 
+def workload_name(cfg, w):
+    g = "x".join(str(int(x)) for x in w["dim"])
+    return WORKLOAD_NAMES.get(cfg, "workload %d" % cfg).format(nb=w["nband"], g=g)
+
+
 # ---------------------------------------------------------------- our arm
 
-def run_ours(args, rank, world, local, pg):
+def run_ours(args, cfg, rank, world, local, pg, work=None):
+    """Times one workload: device-resident steps, the plain FP32 form, end-to-end steps and one
+    profiled step. Returns (result dict, work tuple, out matrix of the last bf16x3 step)."""
     import torch
 
     torch.cuda.set_device(local)
     from pawpyseed_gb300 import _lib
     from pawpyseed_gb300.wavefunction import Wavefunction, pack_species
 
-    _lib.set_precision(args.precision)
-    w, basis_s, defect_s, cr, bd, dd = make_workload(args.workload, args.bands, args.nk)
+    if work is None:
+        work = make_workload(cfg, args.bands, args.nk)
+        work = work + (site_lists(work[1], work[2], work[3]),)
+    w, basis_s, defect_s, cr, bd, dd, lists = work
     L = _lib.lib()
+    _lib.set_precision(args.precision)
     L.pawpy_gpu_set_host_projections(0)
     basis = Wavefunction.from_arrays(basis_s, cr, w["dim"], bd)
     wf = Wavefunction.from_arrays(defect_s, cr, w["dim"], dd)
-    basis.check_c_projectors()  # resident basis (not timed)
-    lists = site_lists(basis_s, defect_s, cr)
+    # resident basis (not timed): coefficients, projections and real-space wavefunctions in HBM
+    basis.check_c_projectors()
+    grids = L.pawpy_gpu_prepare_basis(basis.wf_ptr, 1)
+    _lib.check()
     M_R, M_S, N_R, N_S, NRS_R, NRS_S = lists
     P = _lib.ptr
     species = pack_species(cr)
@@ -171,6 +211,8 @@ def run_ours(args, rank, world, local, pg):
     nk = wf.nwk * wf.nspin
     out = np.zeros((wf.nband, basis.nband * nk), np.complex128)
     pairs = basis.nband * wf.nband * nk
+    # every step runs the whole element setup, as the reference does per structure
+    L.pawpy_gpu_set_element_cache(0)
 
     def step():
         pps = L.get_projector_list(len(cr.pps), *species, ge)
@@ -181,46 +223,48 @@ def run_ours(args, rank, world, local, pg):
                                 len(NRS_R), P(M_R), P(M_S), P(N_R), P(N_S), P(NRS_R), P(NRS_S), 0)
         _lib.check()
 
-    # ---- device-resident: coefficients already in HBM
+    def timed(n):
+        L.pawpy_gpu_synchronize()
+        barrier(pg)
+        L.pawpy_gpu_timer_start()
+        for _ in range(n):
+            step()
+        ms = L.pawpy_gpu_timer_stop_ms()
+        barrier(pg)
+        return max_over_ranks(pg, ms / n)
+
+    # ---- device-resident: the defect's coefficients already in HBM
     wf.upload()
     for _ in range(args.warmup):
         step()
     L.pawpy_gpu_synchronize()
     clocks = Clocks(local)
-    barrier(pg)
     clocks.start()
     L.pawpy_gpu_launch_count(1)
-    L.pawpy_gpu_timer_start()
-    for _ in range(args.steps):
-        step()
-    ms = L.pawpy_gpu_timer_stop_ms()
+    ms_step = timed(args.steps)
     launches = L.pawpy_gpu_launch_count(0)
     clk = clocks.stop()
-    _lib.check()
-    barrier(pg)
-    ms_step = max_over_ranks(pg, ms / args.steps)
     value = sum_over_ranks(pg, pairs) / (ms_step / 1e3)
 
-    # ---- the plain FP32 form (CUDA-core contraction) on the same resident inputs, for comparison
+    # ---- the plain FP32 form (CUDA-core contraction) on the same resident inputs, warmed as the headline
     plain = None
     if args.precision != "fp32":
         _lib.set_precision("fp32")
-        step()
-        L.pawpy_gpu_synchronize()
-        barrier(pg)
-        L.pawpy_gpu_timer_start()
-        for _ in range(args.steps):
+        for _ in range(args.warmup):
             step()
-        ms_fp32 = max_over_ranks(pg, L.pawpy_gpu_timer_stop_ms() / args.steps)
+        ms_fp32 = timed(args.steps)
         plain = dict(value=sum_over_ranks(pg, pairs) / (ms_fp32 / 1e3), ms_per_step=ms_fp32)
         _lib.set_precision(args.precision)
-        step()
+        for _ in range(args.warmup):
+            step()
 
-    # ---- end to end: host pswf_t, H2D of the defect's coefficients and D2H of the matrix every step
+    # ---- end to end: host pswf_t, the defect's coefficients read from host memory and the
+    # matrix written to host memory inside every step
     h2d = sum(c.nbytes for c in dd["coeffs"])
     d2h = out.nbytes
     L.pawpy_gpu_release(wf.wf_ptr)
     step()
+    L.pawpy_gpu_synchronize()
     barrier(pg)
     L.pawpy_gpu_timer_start()
     for _ in range(args.steps):
@@ -240,16 +284,19 @@ def run_ours(args, rank, world, local, pg):
     step()
     L.pawpy_gpu_profile(0)
     stats = _lib.kernel_stats(reset=True)
+    L.pawpy_gpu_set_element_cache(1)
     roof = roofline(stats, w, basis, wf, lists, cr)
-
-    result = dict(pairs_per_step=pairs, ms=ms_step, value=value, e2e_ms=e2e_step, e2e_value=e2e_value, plain=plain,
-                  h2d=h2d, d2h=d2h, launches=launches // args.steps, clocks=clk, roofline=roof,
-                  kernel_ms={k: v[0] for k, v in stats.items() if not k.startswith("host.")},
-                  host_ms={k[5:]: v[0] for k, v in stats.items() if k.startswith("host.")})
-    # correctness spot check of this run against itself being finite
     if not np.all(np.isfinite(out)):
         raise RuntimeError("non-finite overlaps")
-    return result, (w, basis_s, defect_s, cr, bd, dd, lists)
+    result = dict(pairs_per_step=pairs, ms=ms_step, value=value, e2e_ms=e2e_step, e2e_value=e2e_value,
+                  plain=plain, h2d=h2d, d2h=d2h, launches=launches // args.steps, clocks=clk, roofline=roof,
+                  resident_real_space_basis=bool(grids == 1),
+                  kernel_ms={k: v[0] for k, v in stats.items() if not k.startswith("host.")},
+                  host_ms={k[5:]: v[0] for k, v in stats.items() if k.startswith("host.")})
+    L.pawpy_gpu_release(wf.wf_ptr)
+    L.pawpy_gpu_release(basis.wf_ptr)
+    del basis, wf
+    return result, work, out
 
 
 def peaks():
@@ -259,6 +306,13 @@ def peaks():
         return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
     except Exception:
         return 6800.0, 1900.0, "fallback"
+
+
+# DRAM bytes per band-FFT of both passes (ncu dram__bytes_read.sum + dram__bytes_write.sum of the
+# pass-A and pass-B launches of one k-point, divided by its band count), per FFT grid
+FFT_TRAFFIC = {
+    (60, 60, 60): (47.9e6 + 195.0e6 + 261.2e6 + 99.1e6) / 256.0,
+}
 
 
 def roofline(stats, w, basis, wf, lists, cr):
@@ -298,17 +352,16 @@ def roofline(stats, w, basis, wf, lists, cr):
         ach = flops / secs / 1e12
         out.update(bound="tensor", achieved=ach, peak=tc, unit="TFLOP/s", frac=ach / tc)
     elif fam == "fft":
-        nbytes = 16.0 * N3 * wf.nband * nk
+        # band-FFTs of the step: the defect's bands, plus the basis's when the basis is not held in
+        # real space and the defect has sites off the basis (N_S)
+        n_fft = wf.nband * nk
+        nbytes = 16.0 * N3 * n_fft
         ach = nbytes / secs / 1e9
         out.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm,
-                   algorithmic_bytes_per_band_fft=16.0 * N3)
-        if tuple(w["dim"]) == (60, 60, 60):
-            # DRAM bytes of both passes per band-FFT from one ncu capture of this workload's
-            # launches (profiles/fft_passes_traffic_60cubed.md, launches of 256 bands, one
-            # k-point): pass A 47.9 MB read + 195.0 MB written, pass B 261.2 MB read + 99.1 MB
-            # written
-            out.update(traffic=(47.9e6 + 195.0e6 + 261.2e6 + 99.1e6) / 256.0,
-                       traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")
+                   algorithmic_bytes_per_band_fft=16.0 * N3, band_ffts=n_fft)
+        t = FFT_TRAFFIC.get(tuple(int(x) for x in w["dim"]))
+        if t is not None:
+            out.update(traffic=t, traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")
     else:
         out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)
     return out
@@ -324,38 +377,103 @@ def comp_columns(cr, lists, basis, wf):
     return kc
 
 
-# ---------------------------------------------------------------- CPU arm (oracle port)
+# ---------------------------------------------------------------- oracle sample (CPU arm and FP64 check)
 
-def cpu_sample(work, nbands_s, repeat=1):
-    """Oracle port (the reference algorithm in C+OpenMP) on k-point 0 and the first
-    nbands_s defect bands against the full basis at that k-point. Returns
-    (pairs/s, seconds per sample, pairs per sample)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
+def sample_bands(n, m, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(n, m), replace=False))
 
-    w, basis_s, defect_s, cr, bd, dd, lists = work
 
-    def sub(d, nb):
-        return dict(d, nwk=1, nspin=1, kpts=d["kpts"][:1], gs=d["gs"][:1],
-                    coeffs=[d["coeffs"][0][:nb]], energies=d["energies"][:1, :nb], occs=d["occs"][:1, :nb],
-                    nband=nb, weights=np.ones(1))
+class OracleSample:
+    """The oracle (the reference algorithm in C + OpenMP, FP64) on a band sample of a workload:
+    nsb defect bands against nrb basis bands at every k-point. Phases are timed separately so the
+    full workload's CPU time can be extrapolated by the band count each phase scales with:
 
-    ob = orc.OracleWavefunction(data=sub(bd, bd["nband"]), struct=basis_s, cr=cr, dim=w["dim"])
-    ob.setup_projectors()  # resident basis, not timed
-    M_R, M_S, N_R, N_S, NRS_R, NRS_S = [list(x) for x in lists]
-    N_RS = list(zip(NRS_R, NRS_S))
-    times = []
-    for _ in range(repeat):
+      band-independent: element setup, sphere tables, smoothed-wave tables, pair matrices
+      per defect band:  FFT + gather of <p|psi> and of the smoothed-wave projections (N_R)
+      per basis band:   FFT + gather of the smoothed-wave projections onto N_S sites
+      per band pair:    pseudo overlap (FP32 accumulation, as cblas_cdotc_sub) + PAW terms
+
+    The basis's own setup (its projections) is resident and not counted. fixed_once reuses the
+    band-independent parts of the first run (timed once) in later runs."""
+
+    def __init__(self, work, nsb, nrb, seed=7):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        self.orc = orc
+        self.work = work
+        w, basis_s, defect_s, cr, bd, dd, lists = work
+        self.sb = sample_bands(dd["nband"], nsb, seed)
+        self.rb = sample_bands(bd["nband"], nrb, seed + 1)
+        self.ob = orc.OracleWavefunction(data=orc.band_subset(bd, self.rb), struct=basis_s, cr=cr, dim=w["dim"])
+        self.ob.setup_projectors()  # resident basis, not timed
+        M_R, M_S, N_R, N_S, NRS_R, NRS_S = [list(map(int, x)) for x in lists]
+        self.lists = (M_R, M_S, N_R, N_S, list(zip(NRS_R, NRS_S)))
+        self.fixed = None
+        self._prev = None
+
+    def run(self, fixed_once=False):
+        orc = self.orc
+        w, basis_s, defect_s, cr, bd, dd, lists = self.work
+        tm = {}
+        reuse = self._prev if (fixed_once and self._prev is not None) else None
         t0 = time.perf_counter()
-        ow = orc.OracleWavefunction(data=sub(dd, nbands_s), struct=defect_s, cr=cr, dim=w["dim"])
-        ow.setup_projectors()
-        op = orc.OracleProjector(ow, ob, lists=(M_R, M_S, N_R, N_S, N_RS))
-        op.pseudo_full(fp32=True)
-        op.comp_full()
-        times.append(time.perf_counter() - t0)
-    pairs = bd["nband"] * nbands_s
-    t = float(np.median(times))
-    return pairs / t, t, pairs
+        ow = orc.OracleWavefunction(data=orc.band_subset(dd, self.sb), struct=defect_s, cr=cr, dim=w["dim"])
+        ow.setup_projectors(timer=tm, reuse=reuse.wf if reuse is not None else None)
+        op = orc.OracleProjector(ow, self.ob, lists=self.lists, timer=tm, reuse=reuse)
+        t1 = time.perf_counter()
+        p32 = op.pseudo_full(fp32=True)
+        comp = op.comp_full()
+        t2 = time.perf_counter()
+        tm["pairs"] = t2 - t1
+        self.total_s = t2 - t0
+        if reuse is None:
+            self.fixed = {k: tm.get(k, 0.0) for k in ("element", "tables", "smooth_tables", "pair_matrices")}
+            self._prev = op
+        self.timings = tm
+        self.op = op
+        self.p32, self.comp = p32, comp
+        return tm
+
+    def truth(self):
+        """FP64 overlaps of the sample: [nk, nsb, nrb] (pseudo in double precision + PAW terms)."""
+        return self.op.pseudo_full(fp32=False) + self.comp
+
+    def extrapolate(self):
+        """(pairs/s of the full workload, seconds) from the last run's per-band phases and the
+        band-independent phases of the first run."""
+        w, basis_s, defect_s, cr, bd, dd, lists = self.work
+        NS, NR = dd["nband"], bd["nband"]
+        ns, nr = len(self.sb), len(self.rb)
+        tm = self.timings
+        fixed = sum(self.fixed.values())
+        per_def = tm.get("project", 0.0) + tm.get("wp_defect", 0.0)
+        per_bas = tm.get("wp_basis", 0.0)
+        secs = fixed + per_def * NS / ns + per_bas * NR / nr + tm["pairs"] * (NS * NR) / (ns * nr)
+        pairs = NS * NR * len(bd["coeffs"])
+        return pairs / secs, secs
+
+    def describe(self):
+        w = self.work[0]
+        return ("oracle port on %d defect x %d basis bands at all %d k-point(s) (seeded sample), phases timed "
+                "and extrapolated to the full %d x %d bands by the band count each scales with; "
+                "band-independent setup (element, sphere and smoothed-wave tables, pair matrices) timed once"
+                % (len(self.sb), len(self.rb), len(w["kpts"]) * w["nspin"], self.work[5]["nband"],
+                   self.work[4]["nband"]))
+
+
+def accuracy(sample, out, nk):
+    """max and RMS |S - S_FP64| of our matrix on the oracle's sample (every k-point)."""
+    truth = sample.truth()  # [nk, nsb, nrb]
+    mine = np.empty_like(truth)
+    for k in range(nk):
+        mine[k] = out[np.ix_(sample.sb, sample.rb * nk + k)]
+    err = np.abs(mine - truth)
+    return dict(max_abs_err_vs_fp64=float(err.max()), rms_abs_err_vs_fp64=float(np.sqrt((err ** 2).mean())),
+                max_abs_overlap=float(np.abs(truth).max()), tolerance=TOL,
+                sample="%d defect x %d basis bands (seeded) at all %d k-point(s): %d overlaps"
+                       % (len(sample.sb), len(sample.rb), nk, err.size))
 
 
 def cores():
@@ -365,46 +483,76 @@ def cores():
         return os.cpu_count() or 1
 
 
+def threads_used():
+    """OpenMP threads of the oracle: OMP_NUM_THREADS when set, else every host core."""
+    try:
+        return int(os.environ["OMP_NUM_THREADS"])
+    except (KeyError, ValueError):
+        return cores()
+
+
 def run_reference(args, rank, world, pg):
-    """The reference algorithm's CPU implementation (oracle port), all host threads."""
+    """The reference algorithm's CPU implementation (oracle port), all host threads, on the same
+    workload: every step times the per-band work of a band sample; the band-independent setup is
+    timed once (first warm-up) and counted in every step's extrapolated value."""
     if rank != 0:
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(cores()))
     work = make_workload(args.workload, args.bands, args.nk)
-    w, basis_s, defect_s, cr = work[:4]
-    work = work + (site_lists(basis_s, defect_s, cr),)
-    nb_s = args.cpu_sample_bands
-    for _ in range(args.warmup):
-        cpu_sample(work, nb_s)
-    rates, ts = [], []
+    work = work + (site_lists(work[1], work[2], work[3]),)
+    w = work[0]
+    smp = OracleSample(work, args.sample_defect_bands, args.sample_basis_bands)
+    smp.run()
+    for _ in range(max(0, args.warmup - 1)):
+        smp.run(fixed_once=True)
+    rates, secs, walls = [], [], []
     for _ in range(args.steps):
-        r, t, pairs = cpu_sample(work, nb_s)
+        smp.run(fixed_once=True)
+        r, s = smp.extrapolate()
         rates.append(r)
-        ts.append(t)
+        secs.append(s)
+        walls.append(smp.total_s)
     value = float(np.median(rates))
-    sample = ("k-point 0 of %d, %d of %d defect bands against all %d basis bands (%d pairs per step); "
-              "defect setup + overlap setup + pseudo overlaps (FP32 accumulate) + PAW terms"
-              % (len(w["kpts"]), nb_s, w["nband"], w["nband"], pairs))
     line = dict(metric="band-pair projections/sec", value=value, unit="pairs/s", n_gpus=args.gpus,
-                steps=args.steps, warmup=args.warmup, ms_per_step=float(np.median(ts)) * 1e3,
-                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="c64/f64", data="synthetic",
-                impl="reference",
-                config=config(args, w, work),
-                cpu_baseline=dict(value=value, unit="pairs/s", cores=cores(), kind="port", sample=sample),
+                steps=args.steps, warmup=args.warmup, ms_per_step=float(np.median(secs)) * 1e3,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="c64 / f64", data="synthetic",
+                impl="reference", config=config(args, args.workload, w, work),
+                cpu_baseline=dict(value=value, unit="pairs/s", cores=threads_used(), kind="port", sample=smp.describe(),
+                                  sample_wall_s=float(np.median(walls))),
                 e2e=dict(value=value, unit="pairs/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line))
 
 
-def config(args, w, work=None):
-    l2 = "inputs larger than L2"
+def config(args, cfg, w, work=None):
+    l2 = None
     if work is not None:
         mb = [sum(c.nbytes for c in d["coeffs"]) / 1e6 for d in (work[4], work[5])]
-        l2 += " (basis coefficients %.0f MB, defect coefficients %.0f MB)" % tuple(mb)
-    return {"workload": "64-atom cubic 10.86 A A/B cell minus one A, 8 k-points (2x2x2 MP), %d bands, "
-                        "ENCUT %g eV, FFT %dx%dx%d, aug_real" % (w["nband"], w["encut"], *w["dim"])
-            if args.workload == 1 else "workload %d" % args.workload,
-            "nband": w["nband"], "nk": len(w["kpts"]) * w["nspin"], "fft_grid": list(w["dim"]),
-            "precision": args.precision, "l2": l2}
+        l2 = ("inputs larger than L2" if min(mb) > 129 else "inputs smaller than L2") + \
+            " (basis coefficients %.0f MB, defect coefficients %.0f MB; no flush between steps)" % tuple(mb)
+    return {"workload": workload_name(cfg, w), "nband": w["nband"], "nk": len(w["kpts"]) * w["nspin"],
+            "fft_grid": [int(x) for x in w["dim"]], "precision": args.precision, "l2": l2}
+
+
+# ---------------------------------------------------------------- serving
+
+def run_serve_streams(args, rank, local, rates=(20.0, 200.0), n=24):
+    """Seeded Poisson streams against the resident 8-, 64- and 216-atom bases: one at a rate the
+    device sustains (latency is service time) and one at 200 requests/s (latency includes queueing)."""
+    import torch
+
+    torch.cuda.set_device(local)
+    from pawpyseed_gb300 import serve
+
+    res = []
+    for rate in rates:
+        bases, reqs = serve.poisson_workload(n_requests=n, rate=rate, seed=4 + rank)
+        r = serve.run_stream(bases, reqs, slots=args.slots, budget=int(args.budget_gb * (1 << 30)),
+                             precision=args.precision)
+        res.append(dict(rate_per_s=rate, requests=len(reqs), value=r["pairs_per_s"], unit="pairs/s",
+                        p50_ms=r["p50_ms"], p99_ms=r["p99_ms"], mean_ms=r["mean_ms"], wall_s=r["wall_s"],
+                        slots=args.slots, budget_gb=args.budget_gb,
+                        peak_admitted_gb=r["peak_est_bytes"] / (1 << 30)))
+    return res
 
 
 def run_serve(args, rank, world, local):
@@ -480,6 +628,30 @@ def run_precision_report(args, local):
                           note="call_ms includes the host-to-device copy of both coefficient sets")))
 
 
+# ---------------------------------------------------------------- main
+
+def measure(args, cfg, rank, world, local, pg, with_cpu):
+    """One workload through our arm, checked against FP64 on the oracle's sample; on rank 0 also the
+    CPU baseline from the same oracle run."""
+    res, work, out = run_ours(args, cfg, rank, world, local, pg)
+    w = work[0]
+    acc, cpu = None, None
+    if rank == 0:
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores()))
+        smp = OracleSample(work, args.sample_defect_bands, args.sample_basis_bands)
+        smp.run()
+        nk = len(w["kpts"]) * w["nspin"]
+        acc = accuracy(smp, out, nk)
+        if not acc["max_abs_err_vs_fp64"] <= TOL:
+            raise RuntimeError("workload %d: max |overlap error| vs FP64 %.3e exceeds %.0e on the sample"
+                               % (cfg, acc["max_abs_err_vs_fp64"], TOL))
+        if with_cpu:
+            r, secs = smp.extrapolate()
+            cpu = dict(value=r, unit="pairs/s", cores=threads_used(), kind="port", sample=smp.describe(),
+                       sample_wall_s=smp.total_s, extrapolated_s=secs)
+    return res, work, acc, cpu
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init(args.gpus)
@@ -492,25 +664,40 @@ def main():
     if args.serve:
         run_serve(args, rank, world, local)
         return
-    res, work = run_ours(args, rank, world, local, pg)
+    res, work, acc, cpu = measure(args, args.workload, rank, world, local, pg, not args.no_cpu_baseline)
     w = work[0]
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        os.environ.setdefault("OMP_NUM_THREADS", str(cores()))
-        r, t, pairs = cpu_sample(work, args.cpu_sample_bands)
-        cpu = dict(value=r, unit="pairs/s", cores=cores(), kind="port",
-                   sample="k-point 0, %d defect bands x %d basis bands (%d pairs) of the same workload, "
-                          "%.1f s" % (args.cpu_sample_bands, w["nband"], pairs, t))
+    del work
+    secondary = None
+    if args.secondary >= 0 and args.secondary != args.workload and args.bands is None and args.nk is None:
+        r2, work2, acc2, cpu2 = measure(args, args.secondary, rank, world, local, pg, not args.no_cpu_baseline)
+        if rank == 0:
+            secondary = dict(config=config(args, args.secondary, work2[0], work2), value=r2["value"],
+                             ms_per_step=r2["ms"], e2e=dict(value=r2["e2e_value"], ms_per_step=r2["e2e_ms"],
+                                                            h2d_bytes_per_step=r2["h2d"],
+                                                            d2h_bytes_per_step=r2["d2h"]),
+                             accuracy=acc2, roofline=r2["roofline"], cpu_baseline=cpu2,
+                             plain_fp32_form=r2["plain"], gpu_launches=r2["launches"],
+                             kernel_ms=r2["kernel_ms"])
+        del work2
+    serve_res = None
+    if not args.no_serve and args.bands is None and args.nk is None:
+        serve_res = run_serve_streams(args, rank, local)
     if rank == 0:
+        plain = res["plain"]
+        if plain is not None:
+            plain = dict(plain, bf16x3_over_fp32=res["value"] / plain["value"])
         line = dict(metric="band-pair projections/sec", value=res["value"], unit="pairs/s", n_gpus=world,
                     steps=args.steps, warmup=args.warmup, ms_per_step=res["ms"], higher_is_better=True,
                     scaling="weak", vs_baseline=None, dtype="c64 (fp32 accumulate) / f64 setup",
-                    data="synthetic (seeded VASP-format WAVECAR/POTCAR content)", config=config(args, w, work),
+                    data="synthetic (seeded VASP-format WAVECAR/POTCAR content)",
+                    config=config(args, args.workload, w, None) | {
+                        "l2": "inputs larger than L2 (defect coefficients %.0f MB per step)" % (res["h2d"] / 1e6)},
                     e2e=dict(value=res["e2e_value"], unit="pairs/s", ms_per_step=res["e2e_ms"],
                              h2d_bytes_per_step=res["h2d"], d2h_bytes_per_step=res["d2h"]),
-                    gpu_launches=res["launches"], roofline=res["roofline"], cpu_baseline=cpu,
-                    clocks=res["clocks"], kernel_ms=res["kernel_ms"], host_ms=res["host_ms"],
-                    plain_fp32_form=res["plain"])
+                    accuracy=acc, gpu_launches=res["launches"], roofline=res["roofline"], cpu_baseline=cpu,
+                    clocks=res["clocks"], plain_fp32_form=plain,
+                    resident_real_space_basis=res["resident_real_space_basis"],
+                    kernel_ms=res["kernel_ms"], host_ms=res["host_ms"], secondary=secondary, serve=serve_res)
         print(json.dumps(line))
 
 

@@ -2,9 +2,10 @@
  *
  * Drop-in for the hot path of pawpyseed's C core: the structs below have the
  * binary layout of pawpyseed/core/utils.h:30-166 (the Cython layer reads
- * pswf_t members directly, e.g. pawpyc.pyx:537), and the seven entry points
+ * pswf_t members directly, e.g. pawpyc.pyx:537), and the nine entry points
  * in section 2 keep the exact names and signatures that pawpyc_extern.pxd
- * declares, so the Cython extension links against this library unchanged.
+ * declares, so the Cython extension links against this library unchanged
+ * (the aug_recip pair overlap_setup_recip / compensation_terms_recip included).
  * Section 3 adds batched entry points, status reporting and host helpers;
  * they use a pawpy_gpu_ prefix so that they never collide with reference
  * symbols.
@@ -215,6 +216,37 @@ void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S,
                         double *proj_coords, int *ref_labels, double *ref_coords,
                         int *fft_grid, int flip_spin);
 
+/* Replaces overlap_setup_recip (projector.c:727-848; called pawpyc.pyx:674-678),
+ * the setup of the aug_recip method. Same arguments as overlap_setup_real.
+ * Instead of real-space smoothed-wave projections it forms the augmentation
+ * coefficients CAs of get_aug_freqs (projector.c:276-331, 420-453): for every
+ * band of wf_R (sites N_R) and of wf_S (sites N_S), the band's projector
+ * coefficients times the smoothed (phi - phit) Y_lm of those sites, spread on
+ * the grid and transformed forward (fwd_fft3d, linalg.c:47-79) onto the
+ * plane waves -- on the device, in single precision. Also the N_RS pair
+ * matrices as overlap_setup_real. band->CAs are filled (malloc'd complex64 in
+ * the file's plane-wave order) unless host projections are disabled; they are
+ * recomputed for every setup of a pair (the reference keeps the first ones).
+ * The overlaps of the pair (compensation_terms_recip, pawpy_gpu_project_all,
+ * pawpy_gpu_band_character) then follow the aug_recip method until the next
+ * overlap setup of the pair. */
+void overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, int *labels_R, int *labels_S,
+                         double *coords_R, double *coords_S, int *N_R, int *N_S,
+                         int *N_RS_R, int *N_RS_S, int num_N_R, int num_N_S,
+                         int num_N_RS);
+
+/* Replaces compensation_terms_recip (projector.c:965-1077; called
+ * pawpyc.pyx:717-721): adds <CA_R|C_S> + <C_R|CA_S> + O_M + O_N of defect
+ * band BAND_NUM into overlap[b*NK + k]. The cross terms come from the
+ * device contraction of the pair (precision as pawpy_gpu_set_precision), the
+ * O_M and O_N terms in double precision. Needs overlap_setup_recip. */
+void compensation_terms_recip(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S,
+                              pswf_t *wf_R, int num_M, int num_N_R, int num_N_S,
+                              int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S,
+                              int *N_RS_R, int *N_RS_S, int *proj_labels,
+                              double *proj_coords, int *ref_labels, double *ref_coords,
+                              int *fft_grid, int flip_spin);
+
 /* Replaces fft3d (linalg.c:14-45; called from C only). x[i*N2*N3 + j*N3 + k] =
  * V^-1/2 sum_w Cs[w] exp(2 pi i (g1 i/N1 + g2 j/N2 + g3 k/N3)). The transform
  * runs on the device in single precision (|error| well below the 1e-5 that
@@ -254,6 +286,12 @@ void pawpy_gpu_set_tc_splits(int splits);
  * 0, or -1 with the status set. */
 int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
                              pawpy_c64 *out, int precision);
+
+/* Whether get_projector_list keeps its results per exact input (default 1:
+ * requests with the same species and grid share the element setup, as a
+ * resident basis does; a deep copy is returned every call). With 0 every call
+ * runs the whole element setup, as the reference does. */
+void pawpy_gpu_set_element_cache(int on);
 
 /* Whether setup_projections / overlap_setup_real also fill the host
  * projection_t arrays (default 1, as the reference). */
@@ -311,16 +349,24 @@ int pawpy_gpu_upload(pswf_t *wf);
  * synchronisation of cudaMalloc/cudaFree):
  *   out[n*M + m] = sum_{k<K} conj(A[m*lda + k]) * B[n*ldb + k]
  * on caller-owned device buffers (complex64, A/B 16-byte aligned, lda/ldb even
- * and >= K, K a multiple of 16 with zero padding), FP32 accumulation, split-K
- * partial sums reduced in a fixed order -- the contraction of pseudoprojection.
- * It allocates nothing: partial sums and the launch descriptor live in a
- * static device array of 32 MiB (+256 B) that every GPU loading the library
- * holds until exit; outputs larger than M*N = 4,194,304 values are rejected.
- * The first call on each device looks up that array's device address (make it
- * before any stream capture). Calls share the array, so calls whose work
- * overlaps on the GPU (e.g. on different streams) race. stream: a
- * cudaStream_t, or NULL for the library's stream; the call is asynchronous.
- * Returns the split count used (>= 1) or a negative status. */
+ * and >= K, K a multiple of 16 with zero padding) -- the contraction of
+ * pseudoprojection in its plain FP32 form: FP32 accumulation on the CUDA
+ * cores, split-K partial sums reduced in a fixed order. Its error against FP64
+ * grows with K for coherent sums: a unit-norm band against itself over K =
+ * 78,517 plane waves is off by up to 4.8e-5 (random-phase overlaps by ~3e-7);
+ * the split-BF16 form of pawpy_gpu_project_all stays under 1e-5.
+ * It allocates nothing: the partial sums live in a static device array of
+ * 32 MiB that every GPU loading the library holds until exit; outputs larger
+ * than M*N = 4,194,304 values are rejected. The first call on each device
+ * sets up that device (looks up the array's device address and the SM count;
+ * with lazy module loading it also loads the module, which reserves the
+ * 32 MiB then), so a caller with a fixed memory budget makes it early, and
+ * before any stream capture. The address is kept for the process: a
+ * cudaDeviceReset invalidates it. Calls share the array, so calls whose work
+ * overlaps on the GPU (e.g. on different streams) race and may leave wrong
+ * values in each other's outputs (each call writes only its own out).
+ * stream: a cudaStream_t, or NULL for the library's stream; the call is
+ * asynchronous. Returns the split count used (>= 1) or a negative status. */
 int pawpy_gpu_overlap_noalloc(const pawpy_c64 *A, long long lda, const pawpy_c64 *B, long long ldb,
                               int M, int N, int K, pawpy_c64 *out, void *stream);
 

@@ -596,6 +596,68 @@ void oracle_project_bands(int nb, const float *Cs, long stride, const int *Gs, i
 }
 
 /* ------------------------------------------------------------------------ */
+/* aug_recip augmentation coefficients (get_aug_freqs, projector.c:276-331,    */
+/* 420-453; fwd_fft3d, linalg.c:47-79)                                          */
+/* ------------------------------------------------------------------------ */
+
+/* For nb bands: x(r) = sum over the table's sites s and channels p of
+ * P[b][pcol[s] + p] * values_s,p(r) * exp(-i k.path) (get_aug_freqs_helper,
+ * projector.c:305-329), the forward transform of x scaled by sqrt(V)/N^3 and
+ * read at the nw plane waves Gs (fwd_fft3d). The forward transform is the
+ * conjugate of the backward one of conj(x). P: complex128 [nb][pstride];
+ * out: complex128 [nb][nw]. */
+void oracle_aug_coefficients(int nb, const double *P, long pstride, const int *pcol, const int *Gs, int nw,
+                             const int *fftg, const double *L, const double *kcart, int nsites,
+                             const int *npts, const long *toff, const long *voff, const int *total,
+                             const int *indices, const double *paths, const double *values, double *out) {
+  double vol = L[0] * L[4] * L[8] + L[1] * L[5] * L[6] + L[2] * L[3] * L[7] -
+               L[2] * L[4] * L[6] - L[1] * L[3] * L[8] - L[0] * L[5] * L[7];
+  long tot = (long)fftg[0] * fftg[1] * fftg[2];
+  double scale = sqrt(vol) / tot;
+#pragma omp parallel
+  {
+    double complex *x = malloc(sizeof(double complex) * tot);
+    oplan pl[3];
+    int mx = 0;
+    for (int a = 0; a < 3; a++) {
+      oplan_init(&pl[a], fftg[a]);
+      if (fftg[a] > mx) mx = fftg[a];
+    }
+    double complex *line = malloc(sizeof(double complex) * mx);
+    double complex *work = malloc(sizeof(double complex) * mx);
+#pragma omp for schedule(dynamic)
+    for (int b = 0; b < nb; b++) {
+      memset(x, 0, sizeof(double complex) * tot);
+      const double complex *pb = (const double complex *)P + (long)b * pstride;
+      for (int s = 0; s < nsites; s++) {
+        const int *ind = indices + toff[s];
+        const double *pth = paths + 3 * toff[s];
+        const double complex *val = (const double complex *)(values) + voff[s];
+        for (int i = 0; i < npts[s]; i++) {
+          double kr = kcart[0] * pth[3 * i] + kcart[1] * pth[3 * i + 1] + kcart[2] * pth[3 * i + 2];
+          double complex ph = cexp(-I * kr);
+          for (int p = 0; p < total[s]; p++) x[ind[i]] += pb[pcol[s] + p] * val[(long)i * total[s] + p] * ph;
+        }
+      }
+      for (long i = 0; i < tot; i++) x[i] = conj(x[i]);
+      offt3d(x, fftg, pl, line, work);
+      for (int w = 0; w < nw; w++) {
+        int g1 = (Gs[3 * w] + fftg[0]) % fftg[0];
+        int g2 = (Gs[3 * w + 1] + fftg[1]) % fftg[1];
+        int g3 = (Gs[3 * w + 2] + fftg[2]) % fftg[2];
+        double complex v = conj(x[((long)g1 * fftg[1] + g2) * fftg[2] + g3]) * scale;
+        out[2 * ((long)b * nw + w)] = creal(v);
+        out[2 * ((long)b * nw + w) + 1] = cimag(v);
+      }
+    }
+    free(x);
+    free(line);
+    free(work);
+    for (int a = 0; a < 3; a++) oplan_free(&pl[a]);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* off-site overlap (radial.c:116-196; sbf utils.c:804-824)                   */
 /* ------------------------------------------------------------------------ */
 
@@ -670,6 +732,27 @@ void oracle_offsite(const double *dc, const double *k1, const double *f1, const 
   }
   *re = creal(total);
   *im = cimag(total);
+}
+
+/* The whole pair matrix Q[tj][tk] = conj(offsite(lm_j of site 1, lm_k of site 2)) of one
+ * N_RS pair (projector.c:699-712), each element as oracle_offsite. f and s hold every
+ * channel of an element back to back (size and 3 size values per channel); n, l, m list the
+ * element's lm channels in projector order. out: 2 T1 T2 doubles (re, im). */
+void oracle_offsite_matrix(const double *dc, const double *k1, const double *f1, const double *s1,
+                           int size1, int T1, const int *n1, const int *l1, const int *m1,
+                           const double *k2, const double *f2, const double *s2, int size2, int T2,
+                           const int *n2, const int *l2, const int *m2, const double *sbtfacs,
+                           double *out) {
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < T1 * T2; t++) {
+    int tj = t / T2, tk = t % T2;
+    double re, im;
+    oracle_offsite(dc, k1, f1 + (long)n1[tj] * size1, s1 + (long)n1[tj] * 3 * size1, size1, k2,
+                   f2 + (long)n2[tk] * size2, s2 + (long)n2[tk] * 3 * size2, size2, l1[tj], m1[tj],
+                   l2[tk], m2[tk], sbtfacs, &re, &im);
+    out[2 * t] = re;
+    out[2 * t + 1] = -im;
+  }
 }
 
 /* ------------------------------------------------------------------------ */

@@ -72,10 +72,19 @@ void oracle_project_bands(int nb, const float *Cs, long stride, const int *Gs,
                           const double *paths, const double *values, double *out);
 
 /* ---- off-site partial-wave overlap (radial.c:116-196) ---- */
+void oracle_aug_coefficients(int nb, const double *P, long pstride, const int *pcol, const int *Gs, int nw,
+                             const int *fftg, const double *L, const double *kcart, int nsites,
+                             const int *npts, const long *toff, const long *voff, const int *total,
+                             const int *indices, const double *paths, const double *values, double *out);
 void oracle_offsite(const double *dcoord, const double *k1, const double *f1,
                     const double *s1, int size1, const double *k2, const double *f2,
                     const double *s2, int size2, int l1, int m1, int l2, int m2,
                     const double *sbtfacs, double *re, double *im);
+void oracle_offsite_matrix(const double *dc, const double *k1, const double *f1, const double *s1,
+                           int size1, int T1, const int *n1, const int *l1, const int *m1,
+                           const double *k2, const double *f2, const double *s2, int size2, int T2,
+                           const int *n2, const int *l2, const int *m2, const double *sbtfacs,
+                           double *out);
 
 /* ---- pseudoprojection, all S bands (pseudoprojector.c:63-90) ----
  * out[(bS*nbR + bR)] = sum_w conj(CR[bR][w]) CS[bS][w] for one k; fp32 != 0

@@ -24,6 +24,7 @@ import math
 import os
 import subprocess
 import sys
+import time
 
 import numpy as np
 
@@ -63,9 +64,13 @@ def lib():
         L.oracle_offsite.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, C.c_int,
                                      C.c_int, C.c_int, C.c_int, C.c_int, _dp,
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_offsite_matrix.argtypes = [_dp, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip, _ip,
+                                            _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip, _ip, _dp, _dp]
         L.oracle_pseudo_k.argtypes = [C.c_int, C.c_int, C.c_int, _fp, C.c_long, _fp, C.c_long,
                                       C.c_int, _dp]
         L.oracle_fft3d.argtypes = [_dp, _ip, _fp, C.c_int, _ip, C.c_double]
+        L.oracle_aug_coefficients.argtypes = [C.c_int, _dp, C.c_long, _ip, _ip, C.c_int, _ip, _dp, _dp, C.c_int,
+                                              _ip, _lp, _lp, _ip, _ip, _dp, _dp, _dp]
         L.oracle_spline_coeff.argtypes = [_dp, _dp, C.c_int, _dp, _dp, _dp]
         L.oracle_legendre.restype = C.c_double
         L.oracle_legendre.argtypes = [C.c_int, C.c_int, C.c_double]
@@ -218,6 +223,25 @@ class SiteTables:
                                self.paths, self.values, out)
         return (out[0::2] + 1j * out[1::2]).reshape(nb, self.ntot)
 
+    def aug_coefficients(self, P, pcol, gs, fftg, lattice, kcart):
+        """get_aug_freqs (projector.c:276-331, 420-453) of every band: P complex128 [nb, *] projector
+        coefficients (site s of these tables at column pcol[s]) -> CAs complex128 [nb, W]."""
+        L = lib()
+        nb = P.shape[0]
+        nw = gs.shape[0]
+        if self.nsites == 0 or nb == 0:
+            return np.zeros((nb, nw), np.complex128)
+        out = np.zeros(2 * nb * nw)
+        Pc = np.ascontiguousarray(P, dtype=np.complex128)
+        L.oracle_aug_coefficients(nb, Pc.view(np.float64).reshape(-1), Pc.shape[1],
+                                  np.ascontiguousarray(pcol, dtype=np.int32),
+                                  np.ascontiguousarray(gs.reshape(-1), dtype=np.int32), nw,
+                                  np.ascontiguousarray(fftg, dtype=np.int32),
+                                  np.ascontiguousarray(lattice, dtype=np.float64).reshape(-1),
+                                  np.ascontiguousarray(kcart, dtype=np.float64), self.nsites, self.npts,
+                                  self.toff, self.voff, self.total, self.indices, self.paths, self.values, out)
+        return (out[0::2] + 1j * out[1::2]).reshape(nb, nw)
+
 
 class OracleWavefunction:
     """One structure: WAVECAR data, species tables and <p|psi> for every band."""
@@ -244,19 +268,39 @@ class OracleWavefunction:
     def kcart(self, kidx):
         return self.kpts[kidx % self.nwk] @ vaspio.reciprocal_lattice(self.lattice)
 
-    def setup_projectors(self):
+    def setup_projectors(self, timer=None, reuse=None):
+        """Element setup, sphere tables and <p|psi> of every band. timer (a dict) receives the
+        seconds of the phases 'element', 'tables' (band-independent) and 'project' (per band).
+        reuse: a wavefunction of the same structure whose element setup and tables are taken
+        instead of being built again."""
+        t0 = time.perf_counter()
         grid_encut = float(np.max((np.pi * self.dim / self.struct.abc) ** 2 / 0.262))
         self.grid_encut = grid_encut
-        self.species = [OSpecies(self.cr.pps[e], grid_encut) for e in self.cr.pps]
-        self.tables = SiteTables(self.lattice, self.dim, list(range(len(self.struct))), self.nums,
-                                 self.coords, self.species, smooth=False)
+        self.species = reuse.species if reuse is not None else [OSpecies(self.cr.pps[e], grid_encut)
+                                                                for e in self.cr.pps]
+        t1 = time.perf_counter()
+        self.tables = reuse.tables if reuse is not None else SiteTables(
+            self.lattice, self.dim, list(range(len(self.struct))), self.nums, self.coords, self.species,
+            smooth=False)
         self.site_off = self.tables.ooff
+        t2 = time.perf_counter()
         self.P = [self.tables.project(self.data["coeffs"][k], self.data["gs"][k], self.dim,
                                       self.lattice, self.kcart(k)) for k in range(self.nk)]
+        t3 = time.perf_counter()
+        if timer is not None:
+            for name, dt in (("element", t1 - t0), ("tables", t2 - t1), ("project", t3 - t2)):
+                timer[name] = timer.get(name, 0.0) + dt
 
     def site_block(self, P, s):
         o = self.site_off[s]
         return P[:, o: o + self.tables.total[s]]
+
+
+def band_subset(data, idx):
+    """In-memory WAVECAR content restricted to the bands idx (every k-point and spin)."""
+    idx = np.asarray(idx, dtype=np.int64)
+    return dict(data, nband=len(idx), coeffs=[np.ascontiguousarray(c[idx]) for c in data["coeffs"]],
+                energies=np.asarray(data["energies"])[:, idx], occs=np.asarray(data["occs"])[:, idx])
 
 
 def site_lists(basis_struct, wf_struct, basis_cr, wf_cr):
@@ -296,8 +340,20 @@ def min_cart_path(coord, center, lattice):
 class OracleProjector:
     """aug_real projection of wf (S) onto basis (R), full matrices in FP64."""
 
-    def __init__(self, wf, basis, lists=None):
+    def __init__(self, wf, basis, lists=None, timer=None, reuse=None, recip=False):
+        """timer (a dict) receives the seconds of the overlap setup's phases: 'smooth_tables'
+        (band-independent), 'wp_defect' (per defect band), 'wp_basis' (per basis band) and
+        'pair_matrices' (band-independent). reuse: a projector of the same two structures and
+        lists whose band-independent parts (smoothed-wave tables, pair matrices) are taken.
+        recip: the aug_recip method (overlap_setup_recip, projector.c:727-848): instead of
+        real-space smoothed-wave projections, the augmentation coefficients CA_R (R's bands on
+        its N_R sites) and CA_S (S's bands on its N_S sites), complex128 [nk][nband][W]."""
+        self.recip = recip
         self.wf, self.basis = wf, basis
+        tm = {} if timer is None else timer
+
+        def tick(name, t0):
+            tm[name] = tm.get(name, 0.0) + time.perf_counter() - t0
         L = lib()
         for w in (basis, wf):
             if not hasattr(w, "P"):
@@ -311,38 +367,99 @@ class OracleProjector:
         # <(phi-phit)_R|psi_S> on N_R sites of R in S's grid (projector.c:625-646)
         self.WP_S = [np.zeros((wf.nband, 0), np.complex128)] * nk
         self.WP_R = [np.zeros((basis.nband, 0), np.complex128)] * nk
-        if self.N_R:
-            tab = SiteTables(wf.lattice, wf.dim, self.N_R, basis.nums, basis.coords, basis.species, True)
+        if recip:
+            self._setup_recip(reuse, tick)
+        elif self.N_R:
+            t0 = time.perf_counter()
+            tab = reuse.tab_NR if reuse is not None else SiteTables(wf.lattice, wf.dim, self.N_R, basis.nums,
+                                                                    basis.coords, basis.species, True)
             self.tab_NR = tab
+            tick("smooth_tables", t0)
+            t0 = time.perf_counter()
             self.WP_S = [tab.project(wf.data["coeffs"][k], wf.data["gs"][k], wf.dim, wf.lattice,
                                      wf.kcart(k)) for k in range(nk)]
-        if self.N_S:
-            tab = SiteTables(basis.lattice, basis.dim, self.N_S, wf.nums, wf.coords, wf.species, True)
+            tick("wp_defect", t0)
+        if self.N_S and not recip:
+            t0 = time.perf_counter()
+            tab = reuse.tab_NS if reuse is not None else SiteTables(basis.lattice, basis.dim, self.N_S, wf.nums,
+                                                                    wf.coords, wf.species, True)
             self.tab_NS = tab
+            tick("smooth_tables", t0)
+            t0 = time.perf_counter()
             self.WP_R = [tab.project(basis.data["coeffs"][k], basis.data["gs"][k], basis.dim,
                                      basis.lattice, basis.kcart(k)) for k in range(nk)]
+            tick("wp_basis", t0)
         # N_RS pair matrices (projector.c:682-719)
+        t0 = time.perf_counter()
         facs = sbtfacs()
         self.Q, self.dcoords = [], []
-        for s1, s2 in zip(self.N_RS_R, self.N_RS_S):
+        if reuse is not None:
+            self.Q, self.dcoords = reuse.Q, reuse.dcoords
+        for s1, s2 in zip(self.N_RS_R, self.N_RS_S) if reuse is None else ():
             sp1 = basis.species[basis.nums[s1]]
             sp2 = wf.species[wf.nums[s2]]
             dc, _ = min_cart_path(wf.coords[s2], basis.coords[s1], basis.lattice)
             dc = np.ascontiguousarray(dc, dtype=np.float64)
-            Q = np.zeros((sp1.total, sp2.total), np.complex128)
-            ng1, ng2 = sp1.ngrid, sp2.ngrid
-            for tj, (n1, l1, m1) in enumerate(sp1.nlm):
-                f1 = np.ascontiguousarray(sp1.kwave[n1 * ng1:(n1 + 1) * ng1])
-                s1p = np.ascontiguousarray(sp1.kwave_spl[n1 * 3 * ng1:(n1 + 1) * 3 * ng1])
-                for tk, (n2, l2, m2) in enumerate(sp2.nlm):
-                    f2 = np.ascontiguousarray(sp2.kwave[n2 * ng2:(n2 + 1) * ng2])
-                    s2p = np.ascontiguousarray(sp2.kwave_spl[n2 * 3 * ng2:(n2 + 1) * 3 * ng2])
-                    re, im = C.c_double(), C.c_double()
-                    L.oracle_offsite(dc, sp1.kgrid, f1, s1p, ng1, sp2.kgrid, f2, s2p, ng2,
-                                     l1, m1, l2, m2, facs, C.byref(re), C.byref(im))
-                    Q[tj, tk] = complex(re.value, -im.value)  # conj, projector.c:706
+            T1, T2 = sp1.total, sp2.total
+            n1, l1, m1 = [np.ascontiguousarray([x[i] for x in sp1.nlm], dtype=np.int32) for i in range(3)]
+            n2, l2, m2 = [np.ascontiguousarray([x[i] for x in sp2.nlm], dtype=np.int32) for i in range(3)]
+            q = np.zeros(2 * T1 * T2)
+            # conj of the off-site overlap per (lm, lm') (projector.c:706), looped in C
+            L.oracle_offsite_matrix(dc, sp1.kgrid, sp1.kwave, sp1.kwave_spl, sp1.ngrid, T1, n1, l1, m1,
+                                    sp2.kgrid, sp2.kwave, sp2.kwave_spl, sp2.ngrid, T2, n2, l2, m2, facs, q)
+            Q = (q[0::2] + 1j * q[1::2]).reshape(T1, T2)
             self.Q.append(Q)
             self.dcoords.append(dc)
+        tick("pair_matrices", t0)
+
+    def _setup_recip(self, reuse, tick):
+        b, w = self.basis, self.wf
+        nk = b.nk
+        self.CA_R = [np.zeros((b.nband, b.data["coeffs"][k].shape[1]), np.complex128) for k in range(nk)]
+        self.CA_S = [np.zeros((w.nband, w.data["coeffs"][k].shape[1]), np.complex128) for k in range(nk)]
+        for side, (W, lst, name) in enumerate(((b, self.N_R, "tab_NR"), (w, self.N_S, "tab_NS"))):
+            if not lst:
+                continue
+            t0 = time.perf_counter()
+            tab = getattr(reuse, name) if reuse is not None else SiteTables(W.lattice, W.dim, lst, W.nums,
+                                                                            W.coords, W.species, True)
+            setattr(self, name, tab)
+            tick("smooth_tables", t0)
+            t0 = time.perf_counter()
+            pcol = [int(W.site_off[s]) for s in lst]
+            out = self.CA_R if side == 0 else self.CA_S
+            for k in range(nk):
+                out[k] = tab.aug_coefficients(W.P[k], pcol, W.data["gs"][k], W.dim, W.lattice, W.kcart(k))
+            tick("wp_basis" if side == 0 else "wp_defect", t0)
+
+    def cross_full(self, flip_spin=False, fp32=False):
+        """aug_recip cross terms <CA_R|C_S> + <C_R|CA_S> (compensation_terms_recip,
+        projector.c:1000-1016), [nk, nbS, nbR]. fp32: as the reference evaluates them (CAs stored
+        as complex64, cblas_cdotc_sub accumulating in single precision)."""
+        L = lib()
+        b, w = self.basis, self.wf
+        out = np.zeros((b.nk, w.nband, b.nband), np.complex128)
+
+        def dots(A, B):
+            A = np.ascontiguousarray(A, dtype=np.complex64)
+            B = np.ascontiguousarray(B, dtype=np.complex64)
+            tmp = np.zeros(2 * B.shape[0] * A.shape[0])
+            L.oracle_pseudo_k(A.shape[0], B.shape[0], A.shape[1], A.view(np.float32).reshape(-1), A.shape[1],
+                              B.view(np.float32).reshape(-1), B.shape[1], 1, tmp)
+            return (tmp[0::2] + 1j * tmp[1::2]).reshape(B.shape[0], A.shape[0])
+
+        for k in range(b.nk):
+            kR = self._kR(k, flip_spin)
+            CR, CS = b.data["coeffs"][kR], w.data["coeffs"][k]
+            if fp32:
+                if self.N_R:
+                    out[k] += dots(self.CA_R[kR], CS)
+                if self.N_S:
+                    out[k] += dots(CR, self.CA_S[k])
+            else:
+                out[k] = (CS.astype(np.complex128) @ self.CA_R[kR].conj().T +
+                          self.CA_S[k] @ CR.astype(np.complex128).conj().T)
+        return out
 
     def _kR(self, k, flip):
         b = self.basis
@@ -367,7 +484,8 @@ class OracleProjector:
         return out
 
     def comp_full(self, flip_spin=False):
-        """The PAW terms O_M + O_R + O_S + O_N (projector.c:850-963), [nk, nbS, nbR]."""
+        """The PAW terms O_M + O_R + O_S + O_N (projector.c:850-963), [nk, nbS, nbR]; for aug_recip
+        O_M + O_N only (compensation_terms_recip, projector.c:1018-1075; see cross_full)."""
         b, w = self.basis, self.wf
         out = np.zeros((b.nk, w.nband, b.nband), np.complex128)
         for k in range(b.nk):
@@ -377,12 +495,12 @@ class OracleProjector:
             for s1, s2 in zip(self.M_R, self.M_S):
                 sp = b.species[b.nums[s1]]
                 acc += b.site_block(PR, s1).conj() @ sp.Dfull @ w.site_block(PS, s2).T
-            for si, s in enumerate(self.N_R):
+            for si, s in enumerate([] if self.recip else self.N_R):
                 pr = b.site_block(PR, s)
                 o = self.tab_NR.ooff[si]
                 ws = self.WP_S[k][:, o:o + self.tab_NR.total[si]]
                 acc += pr.conj() @ ws.T
-            for si, s in enumerate(self.N_S):
+            for si, s in enumerate([] if self.recip else self.N_S):
                 ps = w.site_block(PS, s)
                 o = self.tab_NS.ooff[si]
                 wr = self.WP_R[kR][:, o:o + self.tab_NS.total[si]]
@@ -395,7 +513,10 @@ class OracleProjector:
         return out
 
     def full(self, flip_spin=False, fp32=False):
-        return self.pseudo_full(flip_spin, fp32) + self.comp_full(flip_spin)
+        tot = self.pseudo_full(flip_spin, fp32) + self.comp_full(flip_spin)
+        if self.recip:
+            tot += self.cross_full(flip_spin, fp32)
+        return tot
 
     @staticmethod
     def band_vector(full, band):

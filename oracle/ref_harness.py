@@ -14,7 +14,10 @@ layer for ``Projector(wf, basis).single_band_projection(b)`` with the default
   ``sites[i]`` for the S-side rmax (projector.py:157);
 * ``CProjector._setup_overlap`` -> ``overlap_setup_real`` (pawpyc.pyx:651-683);
 * per band ``pseudoprojection`` + ``compensation_terms`` (projector.py:210-223,
-  pawpyc.pyx:311-325, 685-702).
+  pawpyc.pyx:311-325, 685-702);
+* for the ``aug_recip`` method, ``overlap_setup_recip`` (pawpyc.pyx:674-678) and per band
+  ``pseudoprojection`` + ``compensation_terms_recip`` (projector.py:225-236,
+  pawpyc.pyx:704-721).
 """
 
 import ctypes as C
@@ -52,6 +55,8 @@ def load_ref():
                                        C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, _ip, _dp, _ip, _dp, _ip, C.c_int]
+    lib.overlap_setup_recip.argtypes = lib.overlap_setup_real.argtypes
+    lib.compensation_terms_recip.argtypes = lib.compensation_terms.argtypes
     lib.fft3d.argtypes = [_zp, C.c_void_p, _dp, _dp, _ip, C.c_void_p, C.c_int, _ip]
     lib.free_pswf.argtypes = [C.POINTER(S.pswf_t)]
     return lib
@@ -137,6 +142,15 @@ class RefWavefunction:
             out.append(v[0::2] + 1j * v[1::2])
         return out
 
+    def aug_coefficients(self, band, kidx):
+        """band->CAs of one band (complex64 in the file's plane-wave order), or None."""
+        kp = self.ptr.contents.kpts[kidx].contents
+        bd = kp.bands[band].contents
+        if not bd.CAs:
+            return None
+        v = np.ctypeslib.as_array(C.cast(bd.CAs, C.POINTER(C.c_float)), shape=(2 * kp.num_waves,)).copy()
+        return (v[0::2] + 1j * v[1::2]).astype(np.complex64)
+
     def free(self):
         if self.ptr:
             self.lib.free_pswf(self.ptr)
@@ -144,10 +158,11 @@ class RefWavefunction:
 
 
 class RefProjector:
-    """The reference aug_real projection of wf (S) onto basis (R)."""
+    """The reference aug_real (or, with recip, aug_recip) projection of wf (S) onto basis (R)."""
 
-    def __init__(self, lib, basis, wf):
+    def __init__(self, lib, basis, wf, recip=False):
         self.lib, self.basis, self.wf = lib, basis, wf
+        self.recip = recip
         basis.setup_projectors()
         wf.setup_projectors()
         M_R, M_S, N_R, N_S, N_RS = site_lists(basis.struct, wf.struct, basis.cr, wf.cr)
@@ -157,9 +172,10 @@ class RefProjector:
         self.lists = dict(M_R=a(M_R), M_S=a(M_S), N_R=a(N_R), N_S=a(N_S),
                           N_RS_R=a(N_RS_R), N_RS_S=a(N_RS_S))
         L = self.lists
-        lib.overlap_setup_real(basis.ptr, wf.ptr, basis.nums, wf.nums, basis.coords, wf.coords,
-                               _ptr(L["N_R"]), _ptr(L["N_S"]), _ptr(L["N_RS_R"]), _ptr(L["N_RS_S"]),
-                               len(N_R), len(N_S), len(N_RS))
+        setup = lib.overlap_setup_recip if recip else lib.overlap_setup_real
+        setup(basis.ptr, wf.ptr, basis.nums, wf.nums, basis.coords, wf.coords,
+              _ptr(L["N_R"]), _ptr(L["N_S"]), _ptr(L["N_RS_R"]), _ptr(L["N_RS_S"]),
+              len(N_R), len(N_S), len(N_RS))
 
     def pseudo(self, band, flip_spin=False):
         nk = self.basis.nwk * self.basis.nspin
@@ -170,12 +186,13 @@ class RefProjector:
     def single_band_projection(self, band, flip_spin=False):
         res = self.pseudo(band, flip_spin)
         L = self.lists
-        self.lib.compensation_terms(res, band, self.wf.ptr, self.basis.ptr,
-                                    len(L["M_R"]), len(L["N_R"]), len(L["N_S"]), len(L["N_RS_R"]),
-                                    _ptr(L["M_R"]), _ptr(L["M_S"]), _ptr(L["N_R"]), _ptr(L["N_S"]),
-                                    _ptr(L["N_RS_R"]), _ptr(L["N_RS_S"]),
-                                    self.wf.nums, self.wf.coords, self.basis.nums, self.basis.coords,
-                                    self.wf.dim, int(flip_spin))
+        comp = self.lib.compensation_terms_recip if self.recip else self.lib.compensation_terms
+        comp(res, band, self.wf.ptr, self.basis.ptr,
+             len(L["M_R"]), len(L["N_R"]), len(L["N_S"]), len(L["N_RS_R"]),
+             _ptr(L["M_R"]), _ptr(L["M_S"]), _ptr(L["N_R"]), _ptr(L["N_S"]),
+             _ptr(L["N_RS_R"]), _ptr(L["N_RS_S"]),
+             self.wf.nums, self.wf.coords, self.basis.nums, self.basis.coords,
+             self.wf.dim, int(flip_spin))
         return res
 
     def overlaps_NRS(self):

@@ -55,9 +55,11 @@ def _declare(L):
     L.setup_projections.argtypes = [_wfp, _ppp, C.c_int, C.c_int, _ip, _ip, _dp]
     L.overlap_setup_real.argtypes = [_wfp, _wfp, _ip, _ip, _dp, _dp, _vp, _vp, _vp, _vp,
                                      C.c_int, C.c_int, C.c_int]
+    L.overlap_setup_recip.argtypes = L.overlap_setup_real.argtypes
     L.pseudoprojection.argtypes = [_zp, _wfp, _wfp, C.c_int, C.c_int]
     L.compensation_terms.argtypes = [_zp, C.c_int, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
                                      _vp, _vp, _vp, _vp, _vp, _vp, _ip, _dp, _ip, _dp, _ip, C.c_int]
+    L.compensation_terms_recip.argtypes = L.compensation_terms.argtypes
     L.pawpy_gpu_project_all.restype = C.c_int
     L.pawpy_gpu_project_all.argtypes = [_zp, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
                                         _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]
@@ -70,6 +72,7 @@ def _declare(L):
     L.pawpy_gpu_set_precision.argtypes = [C.c_int]
     L.pawpy_gpu_get_precision.restype = C.c_int
     L.pawpy_gpu_set_tc_splits.argtypes = [C.c_int]
+    L.pawpy_gpu_set_element_cache.argtypes = [C.c_int]
     L.pawpy_gpu_prepare_basis.restype = C.c_int
     L.pawpy_gpu_prepare_basis.argtypes = [_wfp, C.c_int]
     L.pawpy_gpu_thread_stream.restype = C.c_int

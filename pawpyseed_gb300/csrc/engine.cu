@@ -12,6 +12,7 @@
 // overlap_setup_real, the N_RS pair matrices, the cached pseudo overlap
 // matrices and the augmentation columns of the PAW terms.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <exception>
@@ -140,8 +141,9 @@ static void join_uploads(DevWF &d) {
 struct AugKey {
   std::vector<int> lists[6];
   int flip;
+  bool recip = false;  // aug_recip columns: O_M and O_N only
   bool operator==(const AugKey &o) const {
-    if (flip != o.flip) return false;
+    if (flip != o.flip || recip != o.recip) return false;
     for (int i = 0; i < 6; i++)
       if (lists[i] != o.lists[i]) return false;
     return true;
@@ -169,14 +171,24 @@ struct PairState {
   DevBuf<int> a_src, b_ptr, b_col, b_pair;
   DevBuf<double2> b_val;
   DevBuf<double2> pair_phase;  // [nk][npairs]
+  // aug_recip: set by overlap_setup_recip (the overlaps then follow that method). The
+  // augmentation coefficients of R's bands on its N_R sites and of S's bands on its N_S
+  // sites, [nk][nband][Wpad] in the sorted plane-wave order (empty when the list is);
+  // D_S = C_S + CA_S. cross[f] = <CA_R|C_S> + <C_R|CA_S> [nk][nbS][nbR] per flip.
+  bool recip = false;
+  DevBuf<float2> CA_R, CA_S, D_S;
+  DevBuf<float2> cross[2];
+  bool cross_ready[2] = {false, false};
+  int cross_prec[2] = {-1, -1};
 };
 
 static std::recursive_mutex g_mu;
 static std::map<const pswf_t *, std::unique_ptr<DevWF>> g_wfs;
 static std::map<std::pair<const pswf_t *, const pswf_t *>, std::unique_ptr<PairState>> g_pairs;
-static int g_precision = PAWPY_GPU_FP32;
-static int g_tc_splits = 0;  // K split of the tensor-core contraction, 0 = from the SM count
-static bool g_host_proj = true;
+// process-wide switches; serving threads read them while a caller may set them
+static std::atomic<int> g_precision{PAWPY_GPU_FP32};
+static std::atomic<int> g_tc_splits{0};  // K split of the tensor-core contraction, 0 = from the SM count
+static std::atomic<bool> g_host_proj{true};
 
 void release_device(pswf_t *wf) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
@@ -1147,6 +1159,67 @@ static PairState &pair_state(pswf_t *R, pswf_t *S) {
   return *ptr;
 }
 
+// N_RS pair matrices (projector.c:682-719, 816-843): radial integrals on the device,
+// assembly on the host worker pool; the minimum-image displacements of the pairs.
+static void pair_matrices(PairState &ps, pswf_t *wf_R, pswf_t *wf_S, const int *labels_R, const int *labels_S,
+                          const double *coords_R, const double *coords_S) {
+  const int nNRS = (int)ps.N_RS_R.size();
+  ps.Q.assign(nNRS, {});
+  HostPhase hp_pairs("pair_matrices");
+  ps.dcoords.assign(3 * (size_t)nNRS, 0.0);
+  {
+    std::vector<int> eR(nNRS), eS(nNRS);
+    std::vector<double> Rs(nNRS);
+    for (int i = 0; i < nNRS; i++) {
+      int s1 = ps.N_RS_R[i], s2 = ps.N_RS_S[i];
+      double r;
+      min_image_path(coords_S + 3 * s2, coords_R + 3 * s1, wf_R->lattice, ps.dcoords.data() + 3 * i, &r);
+      eR[i] = labels_R[s1];
+      eS[i] = labels_S[s2];
+      Rs[i] = pair_distance(ps.dcoords.data() + 3 * i);
+    }
+    std::vector<std::vector<double>> I;
+    std::vector<int> Lmax;
+    offsite_radial_integrals(wf_R->pps, wf_S->pps, eR, eS, Rs, I, Lmax);
+    for (int i = 0; i < nNRS; i++) {
+      const ppot_t *p1 = wf_R->pps + eR[i];
+      const ppot_t *p2 = wf_S->pps + eS[i];
+      ps.Q[i].assign((size_t)p1->total_projs * p2->total_projs, 0.0);
+    }
+    // pairs are independent: the host worker pool assembles them in parallel
+    host_parallel_for(nNRS, [&](int i) {
+      offsite_pair_matrix(wf_R->pps + eR[i], wf_S->pps + eS[i], ps.dcoords.data() + 3 * i, I[i].data(), Lmax[i],
+                          reinterpret_cast<pawpy_c128 *>(ps.Q[i].data()));
+    });
+  }
+}
+
+// The pair matrices and displacements as host-visible results with the reference's
+// ownership (wf_S->overlaps / dcoords, freed by free_pswf).
+static void publish_pair_matrices(PairState &ps, pswf_t *wf_R, pswf_t *wf_S) {
+  const int nNRS = (int)ps.N_RS_R.size();
+  if (wf_S->overlaps) {
+    for (int i = 0; i < wf_S->num_aug_overlap_sites; i++) std::free(wf_S->overlaps[i]);
+    std::free(wf_S->overlaps);
+    wf_S->overlaps = nullptr;
+  }
+  std::free(wf_S->dcoords);
+  wf_S->dcoords = nullptr;
+  if (nNRS > 0) {
+    wf_S->overlaps = static_cast<pawpy_c128 **>(std::malloc(sizeof(pawpy_c128 *) * nNRS));
+    wf_S->dcoords = static_cast<double *>(std::malloc(sizeof(double) * 3 * nNRS));
+    if (!wf_S->overlaps || !wf_S->dcoords) throw std::bad_alloc();
+    for (int i = 0; i < nNRS; i++) {
+      wf_S->overlaps[i] = static_cast<pawpy_c128 *>(std::malloc(sizeof(pawpy_c128) * ps.Q[i].size()));
+      if (!wf_S->overlaps[i]) throw std::bad_alloc();
+      std::memcpy(wf_S->overlaps[i], ps.Q[i].data(), sizeof(pawpy_c128) * ps.Q[i].size());
+    }
+    std::memcpy(wf_S->dcoords, ps.dcoords.data(), sizeof(double) * 3 * nNRS);
+  }
+  wf_S->num_aug_overlap_sites = nNRS;
+  wf_R->num_aug_overlap_sites = nNRS;
+}
+
 static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_R, const int *labels_S,
                                   const double *coords_R, const double *coords_S, const int *N_R, const int *N_S,
                                   const int *N_RS_R, const int *N_RS_S, int nNR, int nNS, int nNRS) {
@@ -1165,6 +1238,8 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
                 "overlap_setup_real: NULL site list with a nonzero length");
   ps.aug_ready = false;
   ps.pseudo_ready[0] = ps.pseudo_ready[1] = false;
+  ps.recip = false;
+  ps.cross_ready[0] = ps.cross_ready[1] = false;
   // smoothed partial waves of R's N_R sites on S's grid, and of S's N_S sites on R's grid
   build_spheres(ps.sm_NR, ps.N_R, labels_R, coords_R, R.species, true, S.lattice, S.N, S.vol, S.kp, S.rec);
   build_spheres(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, R.lattice, R.N, R.vol, R.kp, R.rec);
@@ -1188,53 +1263,8 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
     if (!sets.empty()) project_bands(W, sets, outs);
     if (!W.p_ready) W.p_ready = true;  // a prepared, shared basis is only read
   }
-  // N_RS pair matrices (projector.c:682-719): radial integrals on the device, assembly on the host
-  ps.Q.assign(nNRS, {});
-  HostPhase hp_pairs("pair_matrices");
-  ps.dcoords.assign(3 * (size_t)nNRS, 0.0);
-  {
-    std::vector<int> eR(nNRS), eS(nNRS);
-    std::vector<double> Rs(nNRS);
-    for (int i = 0; i < nNRS; i++) {
-      int s1 = ps.N_RS_R[i], s2 = ps.N_RS_S[i];
-      double r;
-      min_image_path(coords_S + 3 * s2, coords_R + 3 * s1, wf_R->lattice, ps.dcoords.data() + 3 * i, &r);
-      eR[i] = labels_R[s1];
-      eS[i] = labels_S[s2];
-      Rs[i] = pair_distance(ps.dcoords.data() + 3 * i);
-    }
-    std::vector<std::vector<double>> I;
-    std::vector<int> Lmax;
-    offsite_radial_integrals(wf_R->pps, wf_S->pps, eR, eS, Rs, I, Lmax);
-    for (int i = 0; i < nNRS; i++) {
-      const ppot_t *p1 = wf_R->pps + eR[i];
-      const ppot_t *p2 = wf_S->pps + eS[i];
-      ps.Q[i].assign((size_t)p1->total_projs * p2->total_projs, 0.0);
-      offsite_pair_matrix(p1, p2, ps.dcoords.data() + 3 * i, I[i].data(), Lmax[i],
-                          reinterpret_cast<pawpy_c128 *>(ps.Q[i].data()));
-    }
-  }
-  // host-visible results with the reference's ownership (freed by free_pswf)
-  if (wf_S->overlaps) {
-    for (int i = 0; i < wf_S->num_aug_overlap_sites; i++) std::free(wf_S->overlaps[i]);
-    std::free(wf_S->overlaps);
-    wf_S->overlaps = nullptr;
-  }
-  std::free(wf_S->dcoords);
-  wf_S->dcoords = nullptr;
-  if (nNRS > 0) {
-    wf_S->overlaps = static_cast<pawpy_c128 **>(std::malloc(sizeof(pawpy_c128 *) * nNRS));
-    wf_S->dcoords = static_cast<double *>(std::malloc(sizeof(double) * 3 * nNRS));
-    if (!wf_S->overlaps || !wf_S->dcoords) throw std::bad_alloc();
-    for (int i = 0; i < nNRS; i++) {
-      wf_S->overlaps[i] = static_cast<pawpy_c128 *>(std::malloc(sizeof(pawpy_c128) * ps.Q[i].size()));
-      if (!wf_S->overlaps[i]) throw std::bad_alloc();
-      std::memcpy(wf_S->overlaps[i], ps.Q[i].data(), sizeof(pawpy_c128) * ps.Q[i].size());
-    }
-    std::memcpy(wf_S->dcoords, ps.dcoords.data(), sizeof(double) * 3 * nNRS);
-  }
-  wf_S->num_aug_overlap_sites = nNRS;
-  wf_R->num_aug_overlap_sites = nNRS;
+  pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
+  publish_pair_matrices(ps, wf_R, wf_S);
   free_wave_projections(wf_R);
   free_wave_projections(wf_S);
   wf_R->wp_num = nNS;
@@ -1272,6 +1302,202 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   if (g_host_proj) sync();  // without host outputs the work stays queued (see do_setup_projections)
 }
 
+
+// ============================================================= overlap_setup_recip
+
+static void ensure_projections(DevWF &d);
+
+// Device copy of a RecipSpread (the sphere points of a set per grid cell, see kernels.h).
+struct RecipSpreadDev {
+  DevBuf<int> cell_first, ucell, ent_first, ent_site, site_npts, site_total, site_pcol;
+  DevBuf<long long> ent_pt, site_pt, site_val;
+  RecipSpread view;
+};
+
+// Groups the points of sphere set S (sites site_nums of W, tables on W's grid) per grid
+// cell of each plane j, entries of a cell in site order (the order of the sums in
+// get_aug_freqs_helper, projector.c:305-329).
+static void build_recip_spread(const SphereSet &S, const DevWF &W, const std::vector<int> &site_nums,
+                               RecipSpreadDev &out) {
+  HostPhase hp("recip_spread_lists");
+  const int N2 = W.N[1];
+  std::vector<int> idx(std::max<long long>(1, S.npts));
+  S.idx.download(idx.data(), S.npts);
+  sync();
+  // entries per plane, site-major as the segments are
+  std::vector<std::vector<std::pair<int, long long>>> per_plane(N2);  // (cell, point)
+  std::vector<std::vector<int>> per_plane_site(N2);
+  for (int q = 0; q < S.nseg; q++) {
+    const SegFill &f = S.segs[q];
+    const int j = S.seg_plane[q];
+    for (int t = 0; t < f.npts; t++) {
+      per_plane[j].emplace_back(idx[f.pt_off + t], f.pt_off + t);
+      per_plane_site[j].push_back(f.site);
+    }
+  }
+  std::vector<int> cell_first(N2 + 1, 0), ucell, ent_first(1, 0), ent_site;
+  std::vector<long long> ent_pt;
+  for (int j = 0; j < N2; j++) {
+    auto &v = per_plane[j];
+    std::vector<int> ord(v.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    // by cell; equal cells keep their site-major order
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return v[a].first < v[b].first; });
+    for (size_t e = 0; e < ord.size(); e++) {
+      const int o = ord[e];
+      if (e == 0 || v[o].first != v[ord[e - 1]].first) {
+        if (e > 0) ent_first.push_back((int)ent_pt.size());
+        ucell.push_back(v[o].first);
+      }
+      ent_pt.push_back(v[o].second);
+      ent_site.push_back(per_plane_site[j][o]);
+    }
+    if (!ord.empty()) ent_first.push_back((int)ent_pt.size());
+    cell_first[j + 1] = (int)ucell.size();
+  }
+  PAWPY_REQUIRE(ent_first.size() == ucell.size() + 1, "aug_recip: spread lists are inconsistent");
+  std::vector<int> npts(S.nsites), tot(S.nsites), pcol(S.nsites);
+  for (int s = 0; s < S.nsites; s++) {
+    npts[s] = S.site_npts[s];
+    tot[s] = S.host[s].total;
+    pcol[s] = W.site_lmoff[site_nums[s]];
+  }
+  auto up_i = [](DevBuf<int> &d, const std::vector<int> &h) {
+    d.alloc(std::max<size_t>(1, h.size()));
+    d.upload(h.data(), h.size());
+  };
+  auto up_l = [](DevBuf<long long> &d, const std::vector<long long> &h) {
+    d.alloc(std::max<size_t>(1, h.size()));
+    d.upload(h.data(), h.size());
+  };
+  up_i(out.cell_first, cell_first);
+  up_i(out.ucell, ucell);
+  up_i(out.ent_first, ent_first);
+  up_i(out.ent_site, ent_site);
+  up_l(out.ent_pt, ent_pt);
+  up_l(out.site_pt, S.site_pt);
+  up_l(out.site_val, S.site_val);
+  up_i(out.site_npts, npts);
+  up_i(out.site_total, tot);
+  up_i(out.site_pcol, pcol);
+  RecipSpread &c = out.view;
+  c.cell_first = out.cell_first.p;
+  c.ucell = out.ucell.p;
+  c.ent_first = out.ent_first.p;
+  c.ent_site = out.ent_site.p;
+  c.ent_pt = out.ent_pt.p;
+  c.site_pt = out.site_pt.p;
+  c.site_val = out.site_val.p;
+  c.site_npts = out.site_npts.p;
+  c.site_total = out.site_total.p;
+  c.site_pcol = out.site_pcol.p;
+  c.tab = S.tab.p;
+  c.phase = S.phase.p;
+  c.npts = S.npts;
+}
+
+// CA[k][band][Wpad] of every band of W (get_aug_freqs for the sites site_nums of W whose
+// smoothed tables on W's own grid are sm), in the sorted plane-wave order; with D given
+// also D = C + CA. Needs W's projector coefficients.
+static void recip_coefficients(DevWF &W, const SphereSet &sm, const std::vector<int> &site_nums,
+                               DevBuf<float2> &CA, DevBuf<float2> *D) {
+  HostPhase hp("recip_coefficients");
+  ensure_coeffs(W);
+  const size_t total = W.C.n;
+  CA.alloc(std::max<size_t>(1, total));
+  CA.zero();
+  if (D) {
+    D->alloc(std::max<size_t>(1, total));
+    D->zero();
+  }
+  if (sm.nsites == 0) return;
+  RecipSpreadDev sp;
+  build_recip_spread(sm, W, site_nums, sp);
+  int maxn1 = 0;
+  for (auto &q : W.kp) maxn1 = std::max(maxn1, q.n1);
+  const long long hband = (long long)maxn1 * W.N[1] * W.N[2] * (long long)sizeof(float2);
+  const int fbatch = (int)std::max(1LL, std::min<long long>(W.nband, kFftBatchBytes / std::max(1LL, hband)));
+  DevBuf<float2> H((size_t)fbatch * maxn1 * W.N[1] * W.N[2]);
+  const int Pt = W.proj.Ptot;
+  for (int k = 0; k < W.nk; k++) {
+    PlaneGeom g;
+    plane_geom(W, k, g);
+    DevKpt &q = W.kp[k];
+    const float2 *Ck = coeffs(W, k);
+    for (int b0 = 0; b0 < W.nband; b0 += fbatch) {
+      const int nb = std::min(fbatch, W.nband - b0);
+      launch_recip_xspread(sp.view, W.P.p + ((size_t)k * W.nband + b0) * Pt, Pt, W.nk, k, g, W.r[0], W.tw[0].p,
+                           H.p, nb);
+      const size_t off = q.c_off + (size_t)b0 * q.Wpad;
+      launch_recip_planes_pick(H.p, g, q.plane_start.p, q.plane_off.p, W.r[1], W.r[2], W.tw[1].p, W.tw[2].p,
+                               Ck + (size_t)b0 * q.Wpad, q.Wpad, CA.p + off, D ? D->p + off : nullptr, nb);
+    }
+  }
+}
+
+// band->CAs of every band of W (malloc'd complex64 in the file's plane-wave order), as
+// get_aug_freqs leaves them (projector.c:445-446).
+static void publish_recip_coefficients(DevWF &W, const DevBuf<float2> &CA) {
+  std::vector<float2> h(W.C.n);
+  CA.download(h.data(), h.size());
+  sync();
+  for (int k = 0; k < W.nk; k++) {
+    const DevKpt &q = W.kp[k];
+    for (int b = 0; b < W.nband; b++) {
+      band_t *bd = W.wf->kpts[k]->bands[b];
+      std::free(bd->CAs);
+      bd->CAs = static_cast<pawpy_c64 *>(std::calloc(std::max(1, q.W), sizeof(pawpy_c64)));
+      if (!bd->CAs) throw std::bad_alloc();
+      const float2 *src = h.data() + q.c_off + (size_t)b * q.Wpad;
+      for (int t = 0; t < q.W; t++) bd->CAs[q.perm[t]] = pawpy_c64(src[t].x, src[t].y);
+    }
+  }
+}
+
+static void do_overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, const int *labels_R, const int *labels_S,
+                                   const double *coords_R, const double *coords_S, const int *N_R, const int *N_S,
+                                   const int *N_RS_R, const int *N_RS_S, int nNR, int nNS, int nNRS) {
+  PAWPY_REQUIRE(wf_R && wf_S, "overlap_setup_recip: NULL wavefunction");
+  DevWF &R = mirror(wf_R);
+  DevWF &S = mirror(wf_S);
+  PAWPY_REQUIRE(R.tables_ready && S.tables_ready, "overlap_setup_recip needs setup_projections on both wavefunctions");
+  PAWPY_REQUIRE(R.nk == S.nk, "basis and defect differ in k-points");
+  PairState &ps = pair_state(wf_R, wf_S);
+  ps.N_R.assign(N_R, N_R + (N_R ? nNR : 0));
+  ps.N_S.assign(N_S, N_S + (N_S ? nNS : 0));
+  ps.N_RS_R.assign(N_RS_R, N_RS_R + (N_RS_R ? nNRS : 0));
+  ps.N_RS_S.assign(N_RS_S, N_RS_S + (N_RS_S ? nNRS : 0));
+  PAWPY_REQUIRE((int)ps.N_R.size() == nNR && (int)ps.N_S.size() == nNS && (int)ps.N_RS_R.size() == nNRS &&
+                    (int)ps.N_RS_S.size() == nNRS,
+                "overlap_setup_recip: NULL site list with a nonzero length");
+  ps.aug_ready = false;
+  ps.pseudo_ready[0] = ps.pseudo_ready[1] = false;
+  ps.cross_ready[0] = ps.cross_ready[1] = false;
+  ps.recip = true;
+  // smoothed partial waves of R's N_R sites on R's grid and of S's N_S sites on S's grid
+  // (overlap_setup_recip, projector.c:746-789); no real-space smoothed-wave projections
+  build_spheres(ps.sm_NR, ps.N_R, labels_R, coords_R, R.species, true, R.lattice, R.N, R.vol, R.kp, R.rec);
+  build_spheres(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, S.lattice, S.N, S.vol, S.kp, S.rec);
+  ps.WP_S.alloc(1);
+  ps.WP_R.alloc(1);
+  ensure_projections(R);
+  ensure_projections(S);
+  recip_coefficients(R, ps.sm_NR, ps.N_R, ps.CA_R, nullptr);
+  recip_coefficients(S, ps.sm_NS, ps.N_S, ps.CA_S, &ps.D_S);
+  pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
+  publish_pair_matrices(ps, wf_R, wf_S);
+  free_wave_projections(wf_R);
+  free_wave_projections(wf_S);
+  wf_R->wp_num = nNS;
+  wf_S->wp_num = nNR;
+  if (g_host_proj) {
+    if (!ps.N_R.empty()) publish_recip_coefficients(R, ps.CA_R);
+    if (!ps.N_S.empty()) publish_recip_coefficients(S, ps.CA_S);
+  }
+  ps.ready = true;
+  if (g_host_proj) sync();
+}
+
 // ============================================================= overlap matrices
 
 static int flip_k(const DevWF &R, int k, int flip) {
@@ -1287,9 +1513,16 @@ static int choose_splits(int M, int N, int nz, int maxK) {
   return std::min(s, 64);
 }
 
-// S[k][bS][bR] = <C_R,bR,kR | C_S,bS,k> plus, with B32 given, the augmentation
-// columns (A32 of the pair, B32[k][bS][Kcpad]).
-static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out) {
+// What an overlap contraction sums, per k-point (kR = k with the spins swapped under flip):
+//   kPseudo:    <C_R|C_S>
+//   kAugmented: aug_real  <C_R|C_S> + [augmentation columns A32 | B32]
+//               aug_recip <C_R|C_S + CA_S> + <CA_R|C_S> + [A32 | B32] (the M and N_RS columns)
+//   kCross:     aug_recip cross terms only, <CA_R|C_S> + <C_R|CA_S>
+// into S[k][bS][bR]; each is one grouped launch with up to three K segments.
+enum class Contraction { kPseudo, kAugmented, kCross };
+
+static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out, int prec,
+                         Contraction what = Contraction::kAugmented) {
   HostPhase hp("overlap_gemm");
   DevWF &R = *ps.R, &S = *ps.S;
   ensure_coeffs(R);
@@ -1298,34 +1531,55 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   int nk = S.nk;
   std::vector<GemmBatch> hb(nk);
   int maxK = 0;
+  const bool recip = ps.recip && what != Contraction::kPseudo;
+  const bool haveCA_R = recip && !ps.N_R.empty(), haveCA_S = recip && !ps.N_S.empty();
   for (int k = 0; k < nk; k++) {
     int kR = flip_k(R, k, flip);
     const DevKpt &qR = R.kp[kR], &qS = S.kp[k];
     PAWPY_REQUIRE(qR.W == qS.W && qR.gsorted == qS.gsorted,
                   "basis and defect plane-wave sets differ at a k-point (lattice, ENCUT or k mismatch)");
-    GemmBatch &g = hb[k];
-    g.A1 = coeffs(R, kR);
-    g.B1 = coeffs(S, k);
-    g.lda1 = qR.Wpad;
-    g.ldb1 = qS.Wpad;
-    g.K1 = qR.Wpad;
-    if (B32) {
-      g.A2 = ps.A32.p + (size_t)kR * R.nband * ps.Kcpad;
-      g.B2 = B32 + (size_t)k * S.nband * ps.Kcpad;
-      g.lda2 = g.ldb2 = ps.Kcpad;
-      g.K2 = ps.Kcpad;
+    struct Seg {
+      const float2 *A, *B;
+      long long lda, ldb;
+      int K;
+    };
+    std::vector<Seg> segs;
+    const float2 *CR = coeffs(R, kR), *CS = coeffs(S, k);
+    const long long w = qR.Wpad;
+    if (what == Contraction::kCross) {
+      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, qR.Wpad});
+      if (haveCA_S) segs.push_back({CR, ps.CA_S.p + qS.c_off, w, w, qR.Wpad});
     } else {
-      g.A2 = g.B2 = nullptr;
-      g.lda2 = g.ldb2 = 0;
-      g.K2 = 0;
+      segs.push_back({CR, haveCA_S ? ps.D_S.p + qS.c_off : CS, w, w, qR.Wpad});
+      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, qR.Wpad});
+      if (B32 && what == Contraction::kAugmented)
+        segs.push_back({ps.A32.p + (size_t)kR * R.nband * ps.Kcpad, B32 + (size_t)k * S.nband * ps.Kcpad,
+                        ps.Kcpad, ps.Kcpad, ps.Kcpad});
+    }
+    GemmBatch &g = hb[k];
+    g.A1 = g.B1 = g.A2 = g.B2 = nullptr;
+    g.lda1 = g.ldb1 = g.lda2 = g.ldb2 = 0;
+    g.K1 = g.K2 = 0;
+    if (segs.size() > 0) {
+      g.A1 = segs[0].A, g.B1 = segs[0].B, g.lda1 = segs[0].lda, g.ldb1 = segs[0].ldb, g.K1 = segs[0].K;
+    }
+    if (segs.size() > 1) {
+      g.A2 = segs[1].A, g.B2 = segs[1].B, g.lda2 = segs[1].lda, g.ldb2 = segs[1].ldb, g.K2 = segs[1].K;
+    }
+    if (segs.size() > 2) {
+      g.A3 = segs[2].A, g.B3 = segs[2].B, g.lda3 = segs[2].lda, g.ldb3 = segs[2].ldb, g.K3 = segs[2].K;
     }
     g.out = out + (size_t)k * S.nband * R.nband;
-    maxK = std::max(maxK, g.K1 + g.K2);
+    maxK = std::max(maxK, g.K1 + g.K2 + g.K3);
+  }
+  if (maxK == 0) {
+    PAWPY_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * (size_t)nk * S.nband * R.nband, stream()));
+    return;
   }
   DevBuf<GemmBatch> db(nk);
   db.upload(hb.data(), nk);
-  if (g_precision == PAWPY_GPU_BF16X3 || g_precision == PAWPY_GPU_TF32) {
-    launch_zgemm_tc(db.p, hb, R.nband, S.nband, g_precision == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+  if (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32) {
+    launch_zgemm_tc(db.p, hb, R.nband, S.nband, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
     return;
   }
   int splits = choose_splits(R.nband, S.nband, nk, maxK);
@@ -1336,12 +1590,25 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
 
 static void ensure_pseudo(PairState &ps, int flip) {
   int f = flip ? 1 : 0;
-  if (ps.pseudo_ready[f] && ps.pseudo_prec[f] == g_precision) return;
+  const int prec = g_precision.load();
+  if (ps.pseudo_ready[f] && ps.pseudo_prec[f] == prec) return;
   DevWF &R = *ps.R, &S = *ps.S;
   ps.pseudo[f].alloc((size_t)S.nk * S.nband * R.nband);
-  overlap_gemm(ps, f, nullptr, ps.pseudo[f].p);
+  overlap_gemm(ps, f, nullptr, ps.pseudo[f].p, prec, Contraction::kPseudo);
   ps.pseudo_ready[f] = true;
-  ps.pseudo_prec[f] = g_precision;
+  ps.pseudo_prec[f] = prec;
+}
+
+// aug_recip cross terms <CA_R|C_S> + <C_R|CA_S> of every band pair, cached per flip.
+static void ensure_cross(PairState &ps, int flip) {
+  int f = flip ? 1 : 0;
+  const int prec = g_precision.load();
+  if (ps.cross_ready[f] && ps.cross_prec[f] == prec) return;
+  DevWF &R = *ps.R, &S = *ps.S;
+  ps.cross[f].alloc((size_t)S.nk * S.nband * R.nband);
+  overlap_gemm(ps, f, nullptr, ps.cross[f].p, prec, Contraction::kCross);
+  ps.cross_ready[f] = true;
+  ps.cross_prec[f] = prec;
 }
 
 // Column maps of the augmentation (see aug.cu) for the given site lists.
@@ -1358,6 +1625,7 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
   AugKey key;
   for (int i = 0; i < 6; i++) key.lists[i] = lists[i];
   key.flip = flip ? 1 : 0;
+  key.recip = ps.recip;
   if (ps.aug_ready && ps.aug_key == key) return;
   HostPhase hp("aug_setup");
   PAWPY_REQUIRE(ps.ready, "overlap_setup_real has not been called for this basis/defect pair");
@@ -1391,8 +1659,9 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
       add_b(-1);
     }
   }
-  // O_R: basis projectors on N_R sites against <smooth (phi-phit)_R | psi_S>
-  for (size_t si = 0; si < ps.N_R.size(); si++) {
+  // O_R: basis projectors on N_R sites against <smooth (phi-phit)_R | psi_S> (aug_recip has
+  // these terms as <CA_R|C_S> and <C_R|CA_S> instead, compensation_terms_recip projector.c:1000-1016)
+  for (size_t si = 0; si < (ps.recip ? 0 : ps.N_R.size()); si++) {
     int s = ps.N_R[si];
     const SiteDesc &h = ps.sm_NR.host[si];
     for (int i = 0; i < h.total; i++) {
@@ -1403,7 +1672,7 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
     }
   }
   // O_S: <smooth (phi-phit)_S | psi_R> against defect projectors on N_S sites
-  for (size_t si = 0; si < ps.N_S.size(); si++) {
+  for (size_t si = 0; si < (ps.recip ? 0 : ps.N_S.size()); si++) {
     int s = ps.N_S[si];
     const SiteDesc &h = ps.sm_NS.host[si];
     for (int i = 0; i < h.total; i++) {
@@ -1490,6 +1759,7 @@ void pawpy_gpu_set_precision(int precision) {
 }
 int pawpy_gpu_get_precision(void) { return g_precision; }
 void pawpy_gpu_set_tc_splits(int splits) { g_tc_splits = splits < 0 ? 0 : splits; }
+void pawpy_gpu_set_element_cache(int on) { set_projector_list_cache(on != 0); }
 
 int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
                              pawpy_c64 *out, int precision) {
@@ -1627,19 +1897,20 @@ void pseudoprojection(pawpy_c128 *projections, pswf_t *wf_ref, pswf_t *wf_proj, 
   PAWPY_API_END()
 }
 
-void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t *wf_R, int num_M, int num_N_R,
-                        int num_N_S, int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S, int *N_RS_R,
-                        int *N_RS_S, int *proj_labels, double *proj_coords, int *ref_labels, double *ref_coords,
-                        int *fft_grid, int flip_spin) {
-  PAWPY_API_BEGIN
-  (void)proj_labels;
-  (void)proj_coords;
-  (void)ref_labels;
-  (void)ref_coords;
-  (void)fft_grid;
-  PAWPY_REQUIRE(overlap && wf_S && wf_R, "compensation_terms: NULL argument");
-  PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < wf_S->nband, "compensation_terms: band index out of range");
+}  // extern "C"
+
+// compensation_terms / compensation_terms_recip of one defect band: the PAW terms in FP64 from
+// the augmentation columns, plus (aug_recip) the cross terms <CA_R|C_S> + <C_R|CA_S>.
+static void do_compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t *wf_R, int num_M,
+                                  int num_N_R, int num_N_S, int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S,
+                                  int *N_RS_R, int *N_RS_S, int flip_spin, bool recip) {
+  const char *name = recip ? "compensation_terms_recip" : "compensation_terms";
+  PAWPY_REQUIRE(overlap && wf_S && wf_R, std::string(name) + ": NULL argument");
+  PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < wf_S->nband, std::string(name) + ": band index out of range");
   PairState &ps = pair_state(wf_R, wf_S);
+  PAWPY_REQUIRE(!ps.ready || ps.recip == recip,
+                recip ? "compensation_terms_recip needs overlap_setup_recip (overlap_setup_real was run)"
+                      : "compensation_terms needs overlap_setup_real (overlap_setup_recip was run)");
   std::vector<int> lists[6];
   gather_lists(lists, num_M, num_N_R, num_N_S, num_N_RS, M_R, M_S, N_R, N_S, N_RS_R, N_RS_S);
   ensure_aug(ps, lists, flip_spin);
@@ -1656,14 +1927,68 @@ void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t 
       launch_zgemv_f64(ps.A64.p + (size_t)kR * R.nband * ps.Kc, ps.Kc, R.nband, ps.Kc, B64.p + (size_t)k * ps.Kc,
                        acc.p + (size_t)k * R.nband);
   }
-  std::vector<double2> h(acc.n);
+  std::vector<double2> h(acc.n), hx;
   acc.download(h.data(), h.size());
+  if (recip) {
+    // cross terms of this band, col[bR][k]
+    ensure_cross(ps, flip_spin);
+    DevBuf<double2> col((size_t)R.nband * nk);
+    launch_extract_band(ps.cross[flip_spin ? 1 : 0].p, nk, S.nband, R.nband, BAND_NUM, col.p);
+    hx.resize(col.n);
+    col.download(hx.data(), hx.size());
+  }
   sync();
   for (int b = 0; b < R.nband; b++)
     for (int k = 0; k < nk; k++) {
       double2 v = h[(size_t)k * R.nband + b];
       overlap[(size_t)b * nk + k] += pawpy_c128(v.x, v.y);
+      if (recip) {
+        double2 x = hx[(size_t)b * nk + k];
+        overlap[(size_t)b * nk + k] += pawpy_c128(x.x, x.y);
+      }
     }
+}
+
+extern "C" {
+
+void compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t *wf_R, int num_M, int num_N_R,
+                        int num_N_S, int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S, int *N_RS_R,
+                        int *N_RS_S, int *proj_labels, double *proj_coords, int *ref_labels, double *ref_coords,
+                        int *fft_grid, int flip_spin) {
+  PAWPY_API_BEGIN
+  (void)proj_labels;
+  (void)proj_coords;
+  (void)ref_labels;
+  (void)ref_coords;
+  (void)fft_grid;
+  do_compensation_terms(overlap, BAND_NUM, wf_S, wf_R, num_M, num_N_R, num_N_S, num_N_RS, M_R, M_S, N_R, N_S,
+                        N_RS_R, N_RS_S, flip_spin, false);
+  PAWPY_API_END()
+}
+
+void compensation_terms_recip(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S, pswf_t *wf_R, int num_M,
+                              int num_N_R, int num_N_S, int num_N_RS, int *M_R, int *M_S, int *N_R, int *N_S,
+                              int *N_RS_R, int *N_RS_S, int *proj_labels, double *proj_coords, int *ref_labels,
+                              double *ref_coords, int *fft_grid, int flip_spin) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("compensation_terms_recip");
+  (void)proj_labels;
+  (void)proj_coords;
+  (void)ref_labels;
+  (void)ref_coords;
+  (void)fft_grid;
+  do_compensation_terms(overlap, BAND_NUM, wf_S, wf_R, num_M, num_N_R, num_N_S, num_N_RS, M_R, M_S, N_R, N_S,
+                        N_RS_R, N_RS_S, flip_spin, true);
+  PAWPY_API_END()
+}
+
+void overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, int *labels_R, int *labels_S, double *coords_R,
+                         double *coords_S, int *N_R, int *N_S, int *N_RS_R, int *N_RS_S, int num_N_R, int num_N_S,
+                         int num_N_RS) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("overlap_setup_recip");
+  do_overlap_setup_recip(wf_R, wf_S, labels_R, labels_S, coords_R, coords_S, N_R, N_S, N_RS_R, N_RS_S, num_N_R,
+                         num_N_S, num_N_RS);
   PAWPY_API_END()
 }
 
@@ -1678,7 +2003,7 @@ static void full_overlap(PairState &ps, const std::vector<int> lists[6], int fli
   launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, 0, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
                ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
   Smat.alloc((size_t)nk * S.nband * R.nband);
-  overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p);
+  overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p, g_precision.load());
 }
 
 int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M, int num_N_R, int num_N_S,

@@ -13,16 +13,16 @@ namespace {
 constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 }
 
-__global__ void __launch_bounds__(NT) k_zgemm_f32(const GemmBatch *__restrict__ batches, int M, int N,
-                                                  int splits, float2 *__restrict__ ws, int nz) {
+// One 64 x 64 output tile of batch z over split sp of its K range (the body of
+// both kernels below; bt is the batch's descriptor in registers).
+__device__ __forceinline__ void zgemm_f32_tile(const GemmBatch &bt, int z, int sp, int M, int N, int splits,
+                                               float2 *__restrict__ ws, int nz) {
   __shared__ float2 As[2][BK][BM + 1];
   __shared__ float2 Bs[2][BK][BN + 1];
-  const int z = blockIdx.z / splits, sp = blockIdx.z % splits;
-  const GemmBatch bt = batches[z];
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int K1 = bt.K1, K2 = bt.K2;
-  const int chunks = (K1 + K2) / BK;
+  const int K1 = bt.K1, K2 = bt.K2, K12 = bt.K1 + bt.K2;
+  const int chunks = (K12 + bt.K3) / BK;
   const int c0 = (int)((long long)chunks * sp / splits), c1 = (int)((long long)chunks * (sp + 1) / splits);
   // loader mapping: 64 rows x 16 complex per tile, 4 complex per thread
   const int lr = tid >> 2, lk = (tid & 3) * 4;
@@ -41,11 +41,16 @@ __global__ void __launch_bounds__(NT) k_zgemm_f32(const GemmBatch *__restrict__ 
       B = bt.B1 + k;
       lda = bt.lda1;
       ldb = bt.ldb1;
-    } else {
+    } else if (k < K12) {
       A = bt.A2 + (k - K1);
       B = bt.B2 + (k - K1);
       lda = bt.lda2;
       ldb = bt.ldb2;
+    } else {
+      A = bt.A3 + (k - K12);
+      B = bt.B3 + (k - K12);
+      lda = bt.lda3;
+      ldb = bt.ldb3;
     }
     float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     if (m0 + lr < M) {
@@ -117,6 +122,18 @@ __global__ void __launch_bounds__(NT) k_zgemm_f32(const GemmBatch *__restrict__ 
     }
 }
 
+__global__ void __launch_bounds__(NT) k_zgemm_f32(const GemmBatch *__restrict__ batches, int M, int N,
+                                                  int splits, float2 *__restrict__ ws, int nz) {
+  const int z = blockIdx.z / splits, sp = blockIdx.z % splits;
+  const GemmBatch bt = batches[z];
+  zgemm_f32_tile(bt, z, sp, M, N, splits, ws, nz);
+}
+
+__global__ void __launch_bounds__(NT) k_zgemm_f32_one(const GemmBatch bt, int M, int N, int splits,
+                                                      float2 *__restrict__ ws) {
+  zgemm_f32_tile(bt, 0, blockIdx.z, M, N, splits, ws, 1);
+}
+
 __global__ void k_split_reduce(const GemmBatch *__restrict__ batches, const float2 *__restrict__ ws, int M,
                                int N, int splits, int nz) {
   const int z = blockIdx.y;
@@ -126,6 +143,20 @@ __global__ void k_split_reduce(const GemmBatch *__restrict__ batches, const floa
     float2 s = make_float2(0.f, 0.f);
     for (int sp = 0; sp < splits; sp++) {
       float2 v = ws[((long long)sp * nz + z) * MN + e];
+      s.x += v.x;
+      s.y += v.y;
+    }
+    out[e] = s;
+  }
+}
+
+__global__ void k_split_reduce_one(float2 *__restrict__ out, const float2 *__restrict__ ws, int M, int N,
+                                   int splits) {
+  long long MN = (long long)M * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < MN; e += (long long)gridDim.x * blockDim.x) {
+    float2 s = make_float2(0.f, 0.f);
+    for (int sp = 0; sp < splits; sp++) {
+      float2 v = ws[(long long)sp * MN + e];
       s.x += v.x;
       s.y += v.y;
     }

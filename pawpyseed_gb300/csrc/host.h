@@ -31,6 +31,9 @@ double interp_log(double r, int n, const double *x, const double *f, double *con
 void spline_integral_weights(const double *x, int n, double *w);
 // get_projector_list served from a cache of earlier results with identical
 // inputs (a deep copy the caller owns), computed by device_projector_list otherwise
+// Whether get_projector_list keeps its results per exact input (on by default);
+// off, every call runs the whole element setup.
+void set_projector_list_cache(bool on);
 ppot_t *cached_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
                               const double *projectors, const double *aewaves, const double *pswaves,
                               const double *rmaxs, double grid_encut);

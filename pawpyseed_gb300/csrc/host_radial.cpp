@@ -194,11 +194,36 @@ double pair_distance(const double *dcoord) {
   return R;
 }
 
+namespace {
+// bessel_fac(lx, ly, L, mx, my) for lx >= ly, 0 <= my <= ly <= lx <= 3, |mx| <= lx, L <= 6: the
+// same values, computed once (the pair matrices ask for them ~10^5 times per 216-atom pair set)
+struct BesselFacTable {
+  double v[4][4][7][7][4];
+  BesselFacTable() {
+    for (int lx = 0; lx < 4; lx++)
+      for (int ly = 0; ly <= lx; ly++)
+        for (int L = 0; L < 7; L++)
+          for (int mx = -lx; mx <= lx; mx++)
+            for (int my = 0; my <= ly; my++) v[lx][ly][L][mx + 3][my] = bessel_fac(lx, ly, L, mx, my);
+  }
+};
+const BesselFacTable &bessel_fac_table() {
+  static const BesselFacTable t;
+  return t;
+}
+}  // namespace
+
 void offsite_pair_matrix(const ppot_t *p1, const ppot_t *p2, const double *dcoord, const double *I, int Lmax,
                          pawpy_c128 *out) {
   double R, th, ph;
   pair_geometry(dcoord, &R, &th, &ph);
   static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+  const BesselFacTable &bf = bessel_fac_table();
+  // Y_L^m of the pair direction for every (L, m) the sums below reach (m = m1 - m2)
+  cd Y[7][13];
+  if (R > 10e-10)
+    for (int L = 0; L <= Lmax && L < 7; L++)
+      for (int m = -L; m <= L; m++) Y[L][m + 6] = ylm(L, m, th, ph);
   int nf2 = p2->num_projs;
   int t1 = 0;
   for (int f1 = 0; f1 < p1->num_projs; f1++) {
@@ -224,11 +249,13 @@ void offsite_pair_matrix(const ppot_t *p1, const ppot_t *p2, const double *dcoor
           int lo = std::abs(l1 - l2);
           for (int L = lo; L <= l1 + l2; L += 2) {
             double integ = I[((long)f1 * nf2 + f2) * (Lmax + 1) + L];
-            if (R > 10e-10)
-              total += integ * bessel_fac(lx, ly, L, mx, my) * ylm(L, m1 - m2, th, ph) *
-                       ipow[((l2 + L - l1) % 4 + 4) % 4] * sign;
-            else if (L == 0 && l1 == l2 && m1 == m2)
+            if (R > 10e-10) {
+              // ylm(L, m, .) is zero for |m| > L (plm's factorials of negative arguments)
+              cd y = std::abs(m1 - m2) <= L ? Y[L][m1 - m2 + 6] : ylm(L, m1 - m2, th, ph);
+              total += integ * bf.v[lx][ly][L][mx + 3][my] * y * ipow[((l2 + L - l1) % 4 + 4) % 4] * sign;
+            } else if (L == 0 && l1 == l2 && m1 == m2) {
               total += integ * 2 / M_PI;
+            }
           }
           out[(long)t1 * p2->total_projs + t2] = std::conj(total);
         }

@@ -139,6 +139,10 @@ struct GemmBatch {
   long long lda1, ldb1, lda2, ldb2;  // row strides (elements)
   int K1, K2;                        // segment lengths, multiples of 16 (may differ per batch)
   float2 *out;                       // [N][M] row-major, leading dimension M
+  // an optional third K segment (K3 = 0: none), after the first two
+  const float2 *A3 = nullptr, *B3 = nullptr;
+  long long lda3 = 0, ldb3 = 0;
+  int K3 = 0;
 };
 // One grouped launch over nz batches (uneven K allowed). splits > 1 needs a
 // workspace of splits*nz*N*M float2 and reduces in split order.
@@ -157,6 +161,36 @@ void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> 
 __global__ void __launch_bounds__(256) k_zgemm_f32(const GemmBatch *batches, int M, int N, int splits,
                                                    float2 *ws, int nz);
 __global__ void k_split_reduce(const GemmBatch *batches, const float2 *ws, int M, int N, int splits, int nz);
+// The same two kernels for one batch whose descriptor is a launch argument (nothing
+// read from device memory before the tile starts): grid (M/64, N/64, splits), and
+// out[e] = sum over splits of ws[sp*M*N + e] in split order.
+__global__ void __launch_bounds__(256) k_zgemm_f32_one(const GemmBatch bt, int M, int N, int splits, float2 *ws);
+__global__ void k_split_reduce_one(float2 *out, const float2 *ws, int M, int N, int splits);
+
+// ---- aug_recip augmentation coefficients (recip.cu) ----
+// The sphere points of a set grouped per grid cell, per real-space plane j of
+// the second axis: cells [cell_first[j], cell_first[j+1]) of plane j at
+// ucell[u] = i*N3 + k, each summing the entries [ent_first[u], ent_first[u+1])
+// (point ent_pt[e] of set site ent_site[e], in site order).
+struct RecipSpread {
+  const int *cell_first = nullptr, *ucell = nullptr, *ent_first = nullptr, *ent_site = nullptr;
+  const long long *ent_pt = nullptr;
+  const long long *site_pt = nullptr, *site_val = nullptr;  // per set site: first point, first table value
+  const int *site_npts = nullptr, *site_total = nullptr;    // points, lm channels
+  const int *site_pcol = nullptr;                           // first column of the site in the P rows
+  const float2 *tab = nullptr;                              // the set's tables [total][site points] per site
+  const float2 *phase = nullptr;                            // exp(i k.path) [nkp][npts]
+  long long npts = 0;
+};
+// pass 1: H[b][p][j][k] = sum_i y_b(i, j, k) exp(+2 pi i g1(p) i / N1) with y_b the spread of band b
+// (P rows [b][Pstride] of k-point kq); grid (N2 planes, nb bands)
+void launch_recip_xspread(const RecipSpread &c, const float2 *P, int Pstride, int nkp, int kq, const PlaneGeom &g,
+                          const Radices &r1, const float2 *tw1, float2 *H, int nb);
+// pass 2: CA[b][t] = conj(2D backward transform of H[b][p] at coefficient t of plane p); D = C + CA when
+// D is given; grid (n1 planes, nb bands)
+void launch_recip_planes_pick(const float2 *H, const PlaneGeom &g, const int *pstart, const int *poff,
+                              const Radices &r2, const Radices &r3, const float2 *tw2, const float2 *tw3,
+                              const float2 *C, int Wpad, float2 *CA, float2 *D, int nb);
 
 // ---- augmentation columns of the PAW terms ----
 // A[kslice][b][c] = src[c] < Pt ? P[kslice][b][src[c]] : WP[kslice][b][src[c]-Pt]; zero for c >= Kc

@@ -13,6 +13,7 @@
 // layout and ownership (the ABI returns host structs).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -500,6 +501,8 @@ struct ListCache {
   std::vector<std::pair<std::vector<unsigned char>, ppot_t *>> entries;  // (inputs, master copy)
   std::vector<int> counts;                                               // elements of each entry
 };
+std::atomic<bool> g_list_cache_on{true};
+
 ListCache &list_cache() {
   static ListCache c;
   return c;
@@ -517,6 +520,8 @@ ppot_t *cached_projector_list(int num_els, const int *labels, const int *ls, con
                               const double *rmaxs, double grid_encut) {
   PAWPY_REQUIRE(num_els > 0 && labels && ls && wave_grids && projectors && aewaves && pswaves && rmaxs,
                 "get_projector_list: missing input array");
+  if (!g_list_cache_on.load())
+    return device_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
   long npt = 0, ngt = 0, ndp = 0, ngp = 0;
   for (int e = 0; e < num_els; e++) {
     const long np = labels[4 * e + 1], nd = labels[4 * e + 2], ng = labels[4 * e + 3];
@@ -562,6 +567,8 @@ ppot_t *cached_projector_list(int num_els, const int *labels, const int *ls, con
   c.counts.push_back(num_els);
   return out;
 }
+
+void set_projector_list_cache(bool on) { g_list_cache_on = on; }
 
 ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, const double *wave_grids,
                               const double *projectors, const double *aewaves, const double *pswaves,

@@ -133,7 +133,7 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
 }
 
 // Instruction descriptor of kind::f16 (BF16 inputs) or kind::tf32, FP32
-// accumulation, both operands K-major, M = 128, N = 256.
+// accumulation, both operands K-major, M = TM (128), N = TN (128).
 __host__ __device__ constexpr uint32_t idesc(bool tf32, bool negA) {
   return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) | ((negA ? 1u : 0u) << 13) |
          (static_cast<uint32_t>(TN >> 3) << 17) | (static_cast<uint32_t>(TM >> 4) << 24);
@@ -373,8 +373,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 // Splits one operand into planes [plane][z][rows_pad][Kc]: element (z, row, k)
-// is A1[row][k] (k < K1), A2[row][k - K1] (k < K1 + K2) or zero; rows >= rows
-// are zero. side 0 takes the A pointers of the batch, side 1 the B pointers.
+// is A1[row][k] (k < K1), A2[row][k - K1] (k < K1 + K2), A3[row][k - K1 - K2]
+// (k < K1 + K2 + K3) or zero; rows >= rows are zero. side 0 takes the A pointers of the batch, side 1 the B pointers.
 template <bool TF32>
 __global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, int rows, int rows_pad, int Kc,
                                int nz, void *__restrict__ planes) {
@@ -384,7 +384,9 @@ __global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, 
   const GemmBatch &bt = batches[z];
   const float2 *s1 = side ? bt.B1 : bt.A1;
   const float2 *s2 = side ? bt.B2 : bt.A2;
+  const float2 *s3 = side ? bt.B3 : bt.A3;
   const long long ld1 = side ? bt.ldb1 : bt.lda1, ld2 = side ? bt.ldb2 : bt.lda2;
+  const long long ld3 = side ? bt.ldb3 : bt.lda3;
   float2 v[4];
 #pragma unroll
   for (int e = 0; e < 4; e++) {
@@ -395,6 +397,8 @@ __global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, 
         v[e] = s1[row * ld1 + k];
       else if (k < bt.K1 + bt.K2)
         v[e] = s2[row * ld2 + (k - bt.K1)];
+      else if (k < bt.K1 + bt.K2 + bt.K3)
+        v[e] = s3[row * ld3 + (k - bt.K1 - bt.K2)];
     }
   }
   const size_t plane = (size_t)nz * rows_pad * Kc;
@@ -473,7 +477,7 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
   int maxK = 0, minkb = 1 << 30;
   std::vector<int> kbl(nz);
   for (int z = 0; z < nz; z++) {
-    const int K = hb[z].K1 + hb[z].K2;
+    const int K = hb[z].K1 + hb[z].K2 + hb[z].K3;
     maxK = std::max(maxK, K);
     kbl[z] = ceil_div(K, P::KB);
     minkb = std::min(minkb, kbl[z]);

@@ -1,8 +1,8 @@
 """``Projector``: PAW band projections of a defect wavefunction onto a basis.
 
 Mirrors ``pawpyseed.core.projector.Projector`` (projector.py:10-503) and its
-Cython base ``CProjector`` (pawpyc.pyx:628-702) for the ``aug_real`` and
-``pseudo`` methods: site classification (``make_site_lists``), the overlap
+Cython base ``CProjector`` (pawpyc.pyx:628-721) for the ``aug_real``,
+``aug_recip`` and ``pseudo`` methods: site classification (``make_site_lists``), the overlap
 setup, ``single_band_projection``, ``proportion_conduction`` and
 ``defect_band_analysis``. ``project_all`` adds the batched form: every defect
 band against every basis band in one device contraction.
@@ -24,9 +24,9 @@ class Projector:
         self.method = method
         if method not in self.METHODS:
             raise PAWpyError("method not recognized for Projector")
-        if method in ("realspace", "aug_recip"):
+        if method == "realspace":
             raise PAWpyError("method %r is not part of this library's projection path; "
-                             "use 'aug_real' (the reference default) or 'pseudo'" % method)
+                             "use 'aug_real' (the reference default), 'aug_recip' or 'pseudo'" % method)
         if wf.ncl or basis.ncl:
             raise PAWpyError("Projection not supported for noncollinear case!")
         if unsym_basis or unsym_wf:
@@ -83,13 +83,15 @@ class Projector:
         Timer.overlap_time(time.monotonic() - start)
 
     def _setup_overlap(self, site_cat):
+        """overlap_setup_real, or overlap_setup_recip for the aug_recip method (pawpyc.pyx:651-683)."""
         a = lambda x: np.array(x, dtype=np.int32)  # noqa: E731
         self.M_R, self.M_S, self.N_R, self.N_S, self.N_RS_R, self.N_RS_S = [a(x) for x in site_cat]
         L = _lib.lib()
-        L.overlap_setup_real(self.basis.wf_ptr, self.wf.wf_ptr, self.basis.nums, self.wf.nums,
-                             self.basis.coords, self.wf.coords, _lib.ptr(self.N_R), _lib.ptr(self.N_S),
-                             _lib.ptr(self.N_RS_R), _lib.ptr(self.N_RS_S),
-                             len(self.N_R), len(self.N_S), len(self.N_RS_R))
+        setup = L.overlap_setup_recip if self.method == "aug_recip" else L.overlap_setup_real
+        setup(self.basis.wf_ptr, self.wf.wf_ptr, self.basis.nums, self.wf.nums,
+              self.basis.coords, self.wf.coords, _lib.ptr(self.N_R), _lib.ptr(self.N_S),
+              _lib.ptr(self.N_RS_R), _lib.ptr(self.N_RS_S),
+              len(self.N_R), len(self.N_S), len(self.N_RS_R))
         _lib.check()
 
     def _lists(self):
@@ -100,10 +102,11 @@ class Projector:
 
     def _add_augmentation_terms(self, res, band_num, flip_spin):
         L = _lib.lib()
-        L.compensation_terms(res, int(band_num), self.wf.wf_ptr, self.basis.wf_ptr,
-                             len(self.M_R), len(self.N_R), len(self.N_S), len(self.N_RS_R),
-                             *self._lists(), self.wf.nums, self.wf.coords, self.basis.nums,
-                             self.basis.coords, self.wf.dimv, int(flip_spin))
+        comp = L.compensation_terms_recip if self.method == "aug_recip" else L.compensation_terms
+        comp(res, int(band_num), self.wf.wf_ptr, self.basis.wf_ptr,
+             len(self.M_R), len(self.N_R), len(self.N_S), len(self.N_RS_R),
+             *self._lists(), self.wf.nums, self.wf.coords, self.basis.nums,
+             self.basis.coords, self.wf.dimv, int(flip_spin))
         _lib.check()
 
     def _single_band_projection_pseudo(self, band_num, flip_spin=False):
@@ -122,7 +125,20 @@ class Projector:
             raise ValueError("Band index out of range (0-indexed)")
         if self.method == "pseudo":
             return self._single_band_projection_pseudo(band_num, flip_spin)
+        if self.method == "aug_recip":
+            return self._single_band_projection_aug_recip(band_num, flip_spin)
         return self._single_band_projection_aug_real(band_num, flip_spin)
+
+    def _single_band_projection_aug_recip(self, band_num, flip_spin=False):
+        """All-electron projection with the augmentation evaluated in reciprocal space
+        (projector.py:225-236): the smoothed partial-wave differences are spread on the grid,
+        transformed onto the plane waves (band->CAs) and contracted with the other structure's
+        coefficients, plus O_M and O_N."""
+        res = self.wf.pseudoprojection(band_num, self.basis, flip_spin)
+        start = time.monotonic()
+        self._add_augmentation_terms(res, band_num, flip_spin)
+        Timer.augmentation_time(time.monotonic() - start)
+        return res
 
     def project_all(self, flip_spin=False):
         """All defect bands at once: out[band_num] == single_band_projection(band_num).
@@ -218,6 +234,11 @@ class Projector:
         if self.method == "pseudo":
             results = {b: self.proportion_conduction(b, spinpol=spinpol) for b in totest}
         else:
+            # the reference reaches single_band_projection for each band, which rejects indices
+            # outside [0, wf.nband) (projector.py:270-271); check them before the batched call
+            for b in totest:
+                if b >= self.wf.nband or b < 0:
+                    raise ValueError("Band index out of range (0-indexed)")
             # every band's character in one device reduction
             v, c = self.band_character(spinpol=spinpol)
             if spinpol:

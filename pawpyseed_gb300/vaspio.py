@@ -10,7 +10,7 @@ facts that any reader must share with VASP; they follow the reference reader
 the nb{1,2,3}max bounds) and ``reader.c:129-315`` (``read_wavecar``: record
 layout, G loop ig3 outer / ig2 / ig1 inner, wrap ``ig > nbmax -> ig-2*nbmax-1``
 computed in double and truncated to int, keep ``|k+G|^2/c <= ENCUT``).
-The C reader that the library ships (``csrc/wavecar.cpp``) implements the same
+The C reader that the library ships (``csrc/host_wavecar.cpp``) implements the same
 order; this module is the writer used for synthetic inputs.
 
 The POTCAR text follows the keyword layout that the reference parser splits on

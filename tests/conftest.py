@@ -24,6 +24,23 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (runs the library's kernels)")
 
 
+class GoldenInputsDiffer(UserWarning):
+    """The regenerated synthetic inputs are not byte-identical to the ones the golden fixtures
+    were made from, so the fixture comparisons run at the tolerance of the FP64 truth instead
+    of at rounding level."""
+
+
+def same_golden_inputs(dirs, g, name):
+    """Whether the regenerated workload has the fixture's bytes; warns (loudly) when not."""
+    import warnings
+
+    same = fingerprint(dirs["basis"]) == str(g["fp_basis"]) and fingerprint(dirs["defect"]) == str(g["fp_defect"])
+    if not same:
+        warnings.warn(GoldenInputsDiffer("%s: regenerated inputs differ in bytes from the golden fixture's; "
+                                         "comparing at the FP64-truth tolerance instead" % name))
+    return same
+
+
 def fingerprint(path):
     h = hashlib.sha256()
     for name in ("WAVECAR", "POTCAR", "CONTCAR", "vasprun.xml"):

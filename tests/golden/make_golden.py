@@ -17,7 +17,12 @@ Fixtures:
   direct plane-wave sum.
 * ``<name>.npz``   -- reference ``single_band_projection`` (aug_real) for every
   defect band: total PAW overlaps, pseudo overlaps, per-band projector
-  coefficients, N_RS pair matrices.
+  coefficients, N_RS pair matrices; and the same projections with the
+  ``aug_recip`` method (``recip_total_*``) with the augmentation coefficients
+  band->CAs of band 0 of each side that has them, per k-point, first 4096
+  plane waves in file order (``recip_CA_<side>_k<k>``).
+
+The reference tree is read from $PAWPY_REFERENCE (default /root/reference).
 """
 
 import hashlib
@@ -34,6 +39,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from pawpyseed_gb300 import synth, vaspio  # noqa: E402
+
+REFERENCE = os.environ.get("PAWPY_REFERENCE", "/root/reference")
 
 CASES = {
     # name: (workload, nband, nk, flips)
@@ -56,7 +63,7 @@ def fft_fixture():
     import ref_harness as rh
 
     lib = rh.load_ref()
-    wc = "/root/reference/test_files/WAVECAR"
+    wc = os.path.join(REFERENCE, "test_files", "WAVECAR")
     d = vaspio.read_wavecar_numpy(wc)
     g = np.ascontiguousarray(d["gs"][0], dtype=np.int32)
     c = np.ascontiguousarray(d["coeffs"][0][0], dtype=np.complex64)
@@ -103,6 +110,20 @@ def case_fixture(name, cfg, nband, nk, flips):
             out["dcoords"] = dc
         for k, v in pr.lists.items():
             out["list_" + k] = v
+        # the aug_recip method on fresh wavefunctions (band->CAs are kept per band)
+        b2 = rh.RefWavefunction(lib, paths["basis"])
+        d2 = rh.RefWavefunction(lib, paths["defect"])
+        prr = rh.RefProjector(lib, b2, d2, recip=True)
+        for flip in flips:
+            tag = "flip" if flip else "noflip"
+            out["recip_total_" + tag] = np.array([prr.single_band_projection(i, flip) for i in range(d2.nband)])
+        for side, wfr in (("basis", b2), ("defect", d2)):
+            for k in range(nkt):
+                ca = wfr.aug_coefficients(0, k)
+                if ca is not None:
+                    out["recip_CA_%s_k%d" % (side, k)] = ca[:4096]
+        b2.free()
+        d2.free()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, "written", {k: getattr(v, "shape", v) for k, v in out.items() if k.startswith("total")})
         b.free()

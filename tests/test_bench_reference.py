@@ -12,12 +12,13 @@ from conftest import ROOT
 def test_reference_arm_prints_one_contract_line():
     env = dict(os.environ, OMP_NUM_THREADS="2")
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "0",
-                          "--steps", "1", "--warmup", "0", "--cpu-sample-bands", "1"],
+                          "--steps", "1", "--warmup", "0", "--sample-defect-bands", "2", "--sample-basis-bands", "4"],
                          capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     line = json.loads(out.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "pairs/s" and line["value"] > 0
     assert line["higher_is_better"] is True and line["steps"] == 1
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert "2 defect x 4 basis bands" in line["cpu_baseline"]["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, fingerprint
+from conftest import CASES, same_golden_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -105,7 +105,7 @@ def test_single_band_projection(name, workload_dirs, oracle_projectors, golden):
     pr = Projector(wf, basis)
     op = oracle_projectors(name)
     g = golden(name)
-    same = fingerprint(dirs["basis"]) == str(g["fp_basis"]) and fingerprint(dirs["defect"]) == str(g["fp_defect"])
+    same = same_golden_inputs(dirs, g, name)
     flips = [False, True] if "total_flip" in g.files else [False]
     for flip in flips:
         truth = op.full(flip)  # FP64

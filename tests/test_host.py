@@ -200,12 +200,14 @@ def test_site_lists_match_reference(name, workload_dirs, golden):
     assert [a for a, _ in N_RS] == list(g["list_N_RS_R"]) and [c for _, c in N_RS] == list(g["list_N_RS_S"])
 
 
-def test_synthetic_inputs_are_reproducible(workload_dirs, golden):
-    """Regenerating a workload gives the fixture's bytes (reported, not required)."""
-    d = workload_dirs("cfg0")
-    g = golden("cfg0")
-    if fingerprint(d["basis"]) != str(g["fp_basis"]):
-        pytest.skip("this platform's numpy regenerates different bytes; tolerance tests still apply")
+@pytest.mark.parametrize("name", list(CASES))
+def test_synthetic_inputs_are_reproducible(name, workload_dirs, golden):
+    """Regenerating a workload gives the bytes the golden fixtures were made from, so the fixture
+    comparisons run at rounding level (elsewhere they fall back to tolerances, with a warning)."""
+    d = workload_dirs(name)
+    g = golden(name)
+    assert fingerprint(d["basis"]) == str(g["fp_basis"])
+    assert fingerprint(d["defect"]) == str(g["fp_defect"])
 
 
 def test_collinear_and_noncollinear_classes_refuse_each_other():
@@ -239,3 +241,28 @@ def test_host_worker_pool_runs_concurrent_loops_once_each():
     assert L.pawpy_gpu_host_pool_check(0, 5) == -1
     with pytest.raises(_lib.PAWpyGPUError):
         _lib.check()
+
+
+@pytest.mark.parametrize("bad", [[-1], [0, 99]])
+def test_defect_band_analysis_rejects_out_of_range_bands(bad):
+    """aug_real band lists are checked before the batched reduction, with the reference's error
+    (single_band_projection raises it for every band it is given, projector.py:270-271)."""
+    from pawpyseed_gb300.projector import Projector
+
+    class WF:
+        nband, nwk, nspin = 4, 1, 1
+
+        def _get_occs(self):
+            return np.array([1.0, 1.0, 0.0, 0.0])
+
+    pr = Projector.__new__(Projector)
+    pr.method = "aug_real"
+    pr.wf = WF()
+    pr.basis = WF()
+
+    def no_device(*a, **k):
+        raise AssertionError("reached the device reduction")
+
+    pr.band_character = no_device
+    with pytest.raises(ValueError, match="Band index out of range"):
+        pr.defect_band_analysis(band_list=bad)

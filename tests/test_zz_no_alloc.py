@@ -74,6 +74,52 @@ def test_noalloc_overlap_matches_pseudoprojection(workload_dirs):
         assert np.array_equal(outs[0], outs[1])
 
 
+def _random_rows(rng, n, k):
+    c = (rng.standard_normal((n, k)) + 1j * rng.standard_normal((n, k))).astype(np.complex64)
+    return (c / np.linalg.norm(c, axis=1, keepdims=True)).astype(np.complex64)
+
+
+@pytest.mark.parametrize("M,N,K,use_lib_stream", [
+    (2048, 2040, 64, False),   # 4,177,920 output values, just under the limit: one split, direct write
+    (40, 24, 8192, False),     # a small output over a long K: many splits through the scratch
+    (96, 80, 1024, True),      # NULL stream: the library's own stream
+])
+def test_noalloc_overlap_matches_fp64_contraction(M, N, K, use_lib_stream):
+    """Shapes the workload case above does not reach, each against conj(A) B^T in FP64, two calls
+    in a row. With the split heuristic (two waves of 64 x 64 tiles) no output fits fewer
+    splits than it asks for, so the capacity clamp never binds; the largest output goes
+    through the direct-write path."""
+    import torch
+
+    _l, L = _lib()
+    rng = np.random.default_rng(M * 7 + N + K)
+    a = _random_rows(rng, M, K)
+    b = _random_rows(rng, N, K)
+    truth = b.astype(np.complex128) @ a.astype(np.complex128).conj().T  # [N][M]
+    dev = torch.device("cuda:0")
+    A = torch.from_numpy(a).to(dev)
+    B = torch.from_numpy(b).to(dev)
+    stream = None if use_lib_stream else C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    outs = []
+    for _ in range(2):
+        out = torch.full((N, M), float("nan"), dtype=torch.complex64, device=dev)
+        splits = L.pawpy_gpu_overlap_noalloc(A.data_ptr(), K, B.data_ptr(), K, M, N, K, out.data_ptr(), stream)
+        _l.check()
+        if M * N > 4_000_000:
+            assert splits == 1
+        elif K >= 8192:
+            assert splits >= 2
+        if use_lib_stream:
+            L.pawpy_gpu_synchronize()
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy())
+    for o in outs:
+        assert np.all(np.isfinite(o))
+        assert np.abs(o - truth).max() <= TOL
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_noalloc_overlap_rejects_oversized_output():
     _l, L = _lib()
     # 4096 x 4096 outputs exceed the 4,194,304-value scratch limit; rejected before any launch
