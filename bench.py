@@ -283,7 +283,7 @@ def run_ours(args, cfg, rank, world, local, pg, work=None):
     L.pawpy_gpu_profile(1)
     step()
     L.pawpy_gpu_profile(0)
-    stats = _lib.kernel_stats(reset=True)
+    stats = _lib.kernel_stats(reset=True, work=True)
     L.pawpy_gpu_set_element_cache(1)
     roof = roofline(stats, w, basis, wf, lists, cr)
     if not np.all(np.isfinite(out)):
@@ -316,65 +316,55 @@ FFT_TRAFFIC = {
 
 
 def roofline(stats, w, basis, wf, lists, cr):
-    """Dominant kernel family of one step: achieved algorithmic rate against the measured peak.
+    """Dominant kernel family of one profiled step: achieved algorithmic rate against the measured peak.
 
-    Per-launch work is uniform within a family, so achieved = (units of the step x
-    algorithmic bytes or flops per unit) / (device time of the family in the step).
-    The FFT family is the two passes of the transform (fft_planes + fft_x_pick) with
-    16 N^3 bytes per band-FFT (one complex64 read and write of the grid); the overlap
-    GEMM counts 8 NB_R NB_S (W + K_aug) useful flops per k-point.
+    The library's launches declare their algorithmic work while profiling: 8 N1 N2 N3 bytes per
+    band and FFT pass (so 16 N^3 per band-FFT over the two passes: one complex64 read and write
+    of the grid), 8 bytes per picked value the sphere contraction reads, and 8 M N K useful flops
+    of the overlap contraction per k-point (K: plane waves plus augmentation columns). achieved =
+    the family's declared work in the step / its device time in the step (CUDA events around
+    every launch, on the stream it runs on); per-launch work is uniform within a family.
     """
-    from pawpyseed_gb300 import vaspio
-
     hbm, tc, src = peaks()
     if not stats:
         return None
     fams = {}
-    for name, (ms, n) in stats.items():
+    for name, (ms, n, work) in stats.items():
         if name.startswith("host."):
             continue
-        key = "fft" if name.startswith("fft") else name
-        a = fams.setdefault(key, [0.0, 0, []])
+        key = "fft" if name in ("fft_planes", "fft_x_pick") else name
+        a = fams.setdefault(key, [0.0, 0, 0.0, []])
         a[0] += ms
         a[1] += n
-        a[2].append(name)
+        a[2] += work
+        a[3].append(name)
+    by_family = {}
+    for key, (ms, n, work, members) in fams.items():
+        if work <= 0 or ms <= 0:
+            continue
+        if key.startswith("gemm"):
+            by_family[key] = dict(ms=ms, achieved=work / (ms / 1e3) / 1e12, unit="TFLOP/s",
+                                  frac=work / (ms / 1e3) / 1e12 / tc, bound="tensor")
+        else:
+            by_family[key] = dict(ms=ms, achieved=work / (ms / 1e3) / 1e9, unit="GB/s",
+                                  frac=work / (ms / 1e3) / 1e9 / hbm, bound="hbm")
     fam = max(fams, key=lambda k: fams[k][0])
-    ms, n, members = fams[fam]
-    secs = ms / 1e3
-    nk = wf.nwk * wf.nspin
-    N3 = int(np.prod(w["dim"]))
-    W = float(vaspio.gvectors(wf.structure.lattice, w["kpts"][0], w["encut"]).shape[0])
+    ms, n, work, members = fams[fam]
     out = dict(kernel="+".join(members), launches=n, ms_per_launch=ms / max(n, 1), peak_source=src,
-               traffic=None)
-    if fam.startswith("gemm"):
-        kc = comp_columns(cr, lists, basis, wf)
-        flops = 8.0 * basis.nband * wf.nband * (W + kc) * nk
-        ach = flops / secs / 1e12
-        out.update(bound="tensor", achieved=ach, peak=tc, unit="TFLOP/s", frac=ach / tc)
-    elif fam == "fft":
-        # band-FFTs of the step: the defect's bands, plus the basis's when the basis is not held in
-        # real space and the defect has sites off the basis (N_S)
-        n_fft = wf.nband * nk
-        nbytes = 16.0 * N3 * n_fft
-        ach = nbytes / secs / 1e9
-        out.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm,
-                   algorithmic_bytes_per_band_fft=16.0 * N3, band_ffts=n_fft)
+               traffic=None, by_family=by_family)
+    if fam in by_family:
+        f = by_family[fam]
+        out.update(bound=f["bound"], achieved=f["achieved"], unit=f["unit"], frac=f["frac"],
+                   peak=tc if f["bound"] == "tensor" else hbm, algorithmic_work_per_launch=work / max(n, 1))
+    else:
+        out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)
+    if fam == "fft":
+        N3 = int(np.prod(w["dim"]))
+        out.update(algorithmic_bytes_per_band_fft=16.0 * N3)
         t = FFT_TRAFFIC.get(tuple(int(x) for x in w["dim"]))
         if t is not None:
             out.update(traffic=t, traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")
-    else:
-        out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)
     return out
-
-
-def comp_columns(cr, lists, basis, wf):
-    tot = {e: sum(2 * l + 1 for l in cr.pps[e].ls) for e in cr.pps}
-    M_R, M_S, N_R, N_S, NRS_R, NRS_S = lists
-    kc = sum(tot[basis.structure.species[i]] for i in M_R)
-    kc += sum(tot[basis.structure.species[i]] for i in N_R)
-    kc += sum(tot[wf.structure.species[i]] for i in N_S)
-    kc += sum(tot[basis.structure.species[i]] for i in NRS_R)
-    return kc
 
 
 # ---------------------------------------------------------------- oracle sample (CPU arm and FP64 check)

@@ -441,9 +441,12 @@ int pawpy_gpu_host_pool_check(int callers, int n);
 /* Kernels launched by this library since the counter was last reset. */
 long long pawpy_gpu_launch_count(int reset);
 /* Per-kernel-family device time: enables CUDA-event bracketing of launches;
- * pawpy_gpu_kernel_stats writes "name ms launches first last\n" lines into buf
- * (first start and last end of the family's launches, or of the host phase
- * "host.<name>", in ms after profiling was switched on). */
+ * pawpy_gpu_kernel_stats writes "name ms launches first last work\n" lines into
+ * buf (first start and last end of the family's launches, or of the host phase
+ * "host.<name>", in ms after profiling was switched on; work: the algorithmic
+ * bytes the launches declared -- 8 N1 N2 N3 per band and FFT pass, 8 per picked
+ * value read by the sphere contraction -- or, for the overlap contractions,
+ * their useful flops, 8 M N K per batch). */
 void pawpy_gpu_profile(int on);
 int pawpy_gpu_kernel_stats(char *buf, int len, int reset);
 /* Bytes of device memory the library holds. */

@@ -160,10 +160,12 @@ def overlap_matrix(As, Bs, precision="fp32"):
     return out
 
 
-def kernel_stats(reset=True, spans=False):
+def kernel_stats(reset=True, spans=False, work=False):
     """{family: (ms, launches)} of the launches profiled since the last reset; with spans,
     {family: (ms, launches, first start, last end)}, the times in ms after profiling was
-    switched on (host phases "host.<name>" on the host clock from the same moment)."""
+    switched on (host phases "host.<name>" on the host clock from the same moment); with work,
+    {family: (ms, launches, work)}: the algorithmic bytes (or, for the overlap contractions,
+    useful flops) the family's launches declared."""
     L = lib()
     n = L.pawpy_gpu_kernel_stats(None, 0, 0)
     buf = C.create_string_buffer(max(n, 1))
@@ -171,8 +173,11 @@ def kernel_stats(reset=True, spans=False):
     check()
     out = {}
     for line in buf.value.decode().splitlines():
-        name, ms, cnt, t0, t1 = line.split()
-        out[name] = (float(ms), int(cnt), float(t0), float(t1)) if spans else (float(ms), int(cnt))
+        name, ms, cnt, t0, t1, wk = line.split()
+        if work:
+            out[name] = (float(ms), int(cnt), float(wk))
+        else:
+            out[name] = (float(ms), int(cnt), float(t0), float(t1)) if spans else (float(ms), int(cnt))
     return out
 
 

@@ -146,6 +146,9 @@ struct DevBuf {
 // so that the count (and, when profiling, per-family device time) is known.
 void launch_begin(const char *family);
 void launch_end(const char *family);
+// While profiling: the algorithmic work (bytes or flops, per the family's unit) of a launch of
+// the family, reported beside its device time by pawpy_gpu_kernel_stats.
+void note_work(const char *family, double units);
 void check_launch(const char *what);
 // Counts launches made outside PAWPY_LAUNCH (no events, no allocation).
 void note_launches(int n);

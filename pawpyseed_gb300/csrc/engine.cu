@@ -384,8 +384,6 @@ static void ensure_coeffs(DevWF &d) {
   DevBuf<float2> raw((size_t)d.nband * maxW);
   for (int k = 0; k < d.nk; k++) {
     DevKpt &q = d.kp[k];
-    kpoint_t *kp = d.wf->kpts[k];
-    (void)kp;
     for (int b = 0; b < d.nband; b++)
       PAWPY_CUDA(cudaMemcpyAsync(raw.p + (size_t)b * q.W, host_band(d, k, b), sizeof(float2) * q.W,
                                  cudaMemcpyHostToDevice, stream()));
@@ -925,14 +923,38 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   // Contraction batch: rows are (k-point, band) pairs, k-major, so that one
   // launch covers several k-points (the tables do not depend on k; the Bloch
   // phase is applied at the pick); picked points and partial sums of up to 2 GiB.
+  // A wavefunction held in real space skips X: the contraction gathers its grid values.
+  const bool gather = d.grid_ready;
   const long long xstride = (xtot + 3) / 4 * 4;
-  const long long per_row = (xstride + ptot) * (long long)sizeof(float2);
+  const long long per_row = ((gather ? 0 : xstride) + ptot) * (long long)sizeof(float2);
   const long long rows = (long long)d.nk * d.nband;
   const long long cbatch =
       std::min({rows, 32768LL, std::max<long long>(fbatch, (2LL << 30) / std::max(1LL, per_row))});
   const bool early = d.h_ready && !d.grid_ready;
   DevBuf<float2> H(d.grid_ready || early ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
-  DevBuf<float2> X((size_t)cbatch * std::max(1LL, xstride));
+  DevBuf<float2> X(gather ? 1 : (size_t)cbatch * std::max(1LL, xstride));
+  ContractSource src;
+  DevBuf<int> gcell, seg_j_d;
+  DevBuf<float2> gphase;
+  if (gather) {
+    // global cell and Bloch phase of every point of the merged point space
+    std::vector<int> seg_j(std::max<size_t>(1, sorted.size()));
+    for (size_t q = 0; q < order.size(); q++) seg_j[q] = plane_of[order[q]];
+    seg_j_d.alloc(seg_j.size());
+    seg_j_d.upload(seg_j.data(), seg_j.size());
+    gcell.alloc(std::max(1LL, xtot));
+    gphase.alloc(std::max(1LL, xtot * d.nk));
+    launch_point_index(segs_d.p, seg_j_d.p, (int)sorted.size(), d.N[1], d.N[2], d.nk, xtot, gcell.p, gphase.p);
+    src.grid = d.grid.p;
+    src.n3d = (long long)d.N[0] * d.N[1] * d.N[2];
+    src.npts = xtot;
+    src.nband = d.nband;
+    src.gcell = gcell.p;
+    src.gphase = gphase.p;
+  } else {
+    src.X = X.p;
+    src.xstride = xstride;
+  }
   DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<char> fast(d.nk);
@@ -949,16 +971,13 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       const int step = early ? std::max(1, bhi - blo) : fbatch;
       for (int b0 = blo; b0 < bhi; b0 += step) {
         const int nb = std::min(step, bhi - b0);
-        float2 *xb = X.p + ((long long)k * d.nband + b0 - r0) * xstride;
+        float2 *xb = gather ? nullptr : X.p + ((long long)k * d.nband + b0 - r0) * xstride;
         if (early) {
           PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
           launch_fft_x_pick_fast(d.Hall.p + d.hoff[k] + (size_t)b0 * q.n1 * d.N[1] * d.N[2], g, plist, k, xb,
                                  xstride, nb);
-        } else if (d.grid_ready) {
-          // resident real-space wavefunctions: a gather instead of the transform
-          const size_t n3d = (size_t)d.N[0] * d.N[1] * d.N[2];
-          launch_grid_pick(d.grid.p + ((size_t)k * d.nband + b0) * n3d, d.N[0], d.N[1], d.N[2], plist, k, xb,
-                           xstride, nb);
+        } else if (gather) {
+          // resident real-space wavefunctions: the contraction reads them directly
         } else if (fast[k]) {
           launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                                  H.p, nb);
@@ -971,7 +990,8 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       }
     }
     const int cn = (int)(r1 - r0);
-    launch_chunk_contract(ch_d.p, (int)chunks.size(), max_total, X.p, xstride, partial.p, ptot, cn);
+    src.r0 = r0;
+    launch_contract_staged(ch_d.p, (int)chunks.size(), max_total, src, partial.p, ptot, cn, xtot);
     for (size_t i = 0; i < sets.size(); i++) {
       const SphereSet &S = *sets[i];
       if (S.nsites == 0) continue;
@@ -1578,6 +1598,9 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   }
   DevBuf<GemmBatch> db(nk);
   db.upload(hb.data(), nk);
+  double flops = 0;  // useful flops: 8 per complex multiply-add of every K segment
+  for (const GemmBatch &g : hb) flops += 8.0 * R.nband * S.nband * (double)(g.K1 + g.K2 + g.K3);
+  note_work(prec == PAWPY_GPU_BF16X3 ? "gemm_bf16x3" : prec == PAWPY_GPU_TF32 ? "gemm_tf32" : "gemm_f32", flops);
   if (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32) {
     launch_zgemm_tc(db.p, hb, R.nband, S.nband, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
     return;

@@ -83,6 +83,7 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   };
   int mult = tune(std::make_tuple(1, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
   run(mult);
+  note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 
 void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb) {
@@ -92,29 +93,7 @@ void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb
   PAWPY_REQUIRE(fn, "no register FFT for this grid");
   dim3 grd(ceil_div(nb, bpc), g.N2);
   PAWPY_LAUNCH("fft_x_grid", fn<<<grd, FT, 0, stream()>>>(H, nb, g, grid));
-}
-
-// X[b][xo[q]] = grid[b][(x N2 + j) N3 + z] * phase[q] for the points q of plane j (cell = x N3 + z);
-// grid (N2 planes, nb bands)
-__global__ void k_grid_pick(const float2 *__restrict__ grid, int N1, int N2, int N3,
-                            const int *__restrict__ plane_first, const int *__restrict__ cell,
-                            const int *__restrict__ xo, const float2 *__restrict__ phase, float2 *__restrict__ X,
-                            long long xstride) {
-  const int j = blockIdx.x, b = blockIdx.y;
-  const float2 *gb = grid + (long long)b * N1 * N2 * N3;
-  float2 *xb = X + (long long)b * xstride;
-  for (int q = plane_first[j] + threadIdx.x; q < plane_first[j + 1]; q += blockDim.x) {
-    const int c = cell[q], x = c / N3, z = c - x * N3;
-    xb[xo[q]] = cmul(gb[((long long)x * N2 + j) * N3 + z], phase[q]);
-  }
-}
-
-void launch_grid_pick(const float2 *grid, int N1, int N2, int N3, const PickList &pl, int kq, float2 *X,
-                      long long xstride, int nb) {
-  if (nb <= 0) return;
-  dim3 grd(N2, nb);
-  PAWPY_LAUNCH("grid_pick", k_grid_pick<<<grd, 128, 0, stream()>>>(grid, N1, N2, N3, pl.plane_first, pl.cell, pl.xo,
-                                                                     pl.phase + (long long)kq * pl.npts, X, xstride));
+  note_work("fft_x_grid", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 
 // One CTA per segment: its points go to positions base[si] + p of the flat list.

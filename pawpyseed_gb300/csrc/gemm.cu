@@ -21,7 +21,7 @@ __device__ __forceinline__ void zgemm_f32_tile(const GemmBatch &bt, int z, int s
   __shared__ float2 Bs[2][BK][BN + 1];
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int K1 = bt.K1, K2 = bt.K2, K12 = bt.K1 + bt.K2;
+  const int K1 = bt.K1, K12 = bt.K1 + bt.K2;
   const int chunks = (K12 + bt.K3) / BK;
   const int c0 = (int)((long long)chunks * sp / splits), c1 = (int)((long long)chunks * (sp + 1) / splits);
   // loader mapping: 64 rows x 16 complex per tile, 4 complex per thread

@@ -49,9 +49,6 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
                             long long xstride, int nb);
 // pass B writing whole grids: grid[b] = [N1][N2][N3] real-space values of band b (register sizes only)
 void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb);
-// the pick of launch_fft_x_pick_fast from resident grids [b][N1][N2][N3]
-void launch_grid_pick(const float2 *grid, int N1, int N2, int N3, const PickList &pl, int kq, float2 *X,
-                      long long xstride, int nb);
 // fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
 void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).
@@ -111,6 +108,26 @@ struct ChunkContract {
   int npts, total;
   int part_off;          // offset of the chunk's partial sums in the per-band partial vector
 };
+// Source of the staged contraction (launch_contract_staged): the picked-point
+// rows X[row][xstride], or (grid != nullptr) the real-space grids of rows
+// R = r0 + row ([R][n3d], R = k nband + band) read at gcell[xo] times
+// gphase[k][xo] (npts points per k).
+struct ContractSource {
+  const float2 *X = nullptr;
+  long long xstride = 0;
+  const float2 *grid = nullptr;
+  long long n3d = 0, r0 = 0, npts = 0;
+  int nband = 1;
+  const int *gcell = nullptr;
+  const float2 *gphase = nullptr;
+};
+// partial[row][part_off + l] = sum over the chunk's points of source(row, point) * tab[l][point];
+// npts (the merged point space) sizes the declared work
+void launch_contract_staged(const ChunkContract *chunks, int nchunks, int max_total, const ContractSource &src,
+                            float2 *partial, int ptot, int nb, long long npts);
+// the global cell and Bloch phase of every point of the merged point space
+void launch_point_index(const GatherSeg *segs, const int *seg_j, int nsegs, int N2, int N3, int nkp, long long Q,
+                        int *gcell, float2 *gphase);
 // pass 1: count the inside points of every slab
 void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, const double *lattice,
                        const int *fftg, int *counts);
@@ -123,9 +140,6 @@ void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const
 // the segments of plane j (segs sorted by plane; plane_start[N2+1])
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
                        const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb);
-// partial[b][part_off + lm] = sum_p X[b][x_off + p] * tab[lm][p] over each chunk, bands b < nb
-void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
-                           long long xstride, float2 *partial, int ptot, int nb);
 // P[(band_base + b)*Ptot + o] = sum over c < col[o].y of partial[b][col[o].x + c*col[o].z]: the
 // chunks of column o's site, in chunk order
 void launch_chunk_reduce(const float2 *partial, int ptot, const int4 *col, float2 *P, int Ptot, int nb,

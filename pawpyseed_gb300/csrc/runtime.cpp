@@ -46,6 +46,7 @@ struct Runtime {
     double ms = 0;
     long long n = 0;
     double first = -1, last = -1;
+    double work = 0;  // algorithmic bytes or flops the launches declared (note_work)
   };
   std::map<std::string, Fam> fams;
   std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -310,6 +311,12 @@ void launch_begin(const char *family) {
     PAWPY_CUDA(cudaEventRecord(a, t_stream ? t_stream : r.s));
     r.pending.push_back({family, {a, b}});
   }
+}
+
+void note_work(const char *family, double units) {
+  Runtime &r = rt();
+  std::lock_guard<std::recursive_mutex> g(r.mu);
+  if (r.profile) r.fams[family].work += units;
 }
 
 void launch_end(const char *family) {
@@ -582,9 +589,9 @@ int pawpy_gpu_kernel_stats(char *buf, int len, int reset) {
   drain_locked(r);
   std::string out;
   for (auto &f : r.fams) {
-    char line[256];
-    snprintf(line, sizeof line, "%s %.6f %lld %.6f %.6f\n", f.first.c_str(), f.second.ms, f.second.n,
-             f.second.first, f.second.last);
+    char line[320];
+    snprintf(line, sizeof line, "%s %.6f %lld %.6f %.6f %.6e\n", f.first.c_str(), f.second.ms, f.second.n,
+             f.second.first, f.second.last, f.second.work);
     out += line;
   }
   if (reset) r.fams.clear();

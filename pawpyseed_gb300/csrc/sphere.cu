@@ -261,104 +261,204 @@ void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, c
   dim3 grid(g.N2, nb);
   PAWPY_LAUNCH("fft_x_pick", k_fft_x_pick<<<grid, 256, smem, stream()>>>(H, g, r1, tw1, segs, plane_start, kq, X,
                                                                         xstride));
+  note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 
 // ---------------------------------------------------------------------------
 // <p_lm|psi_b> = sum_p X[b][p] tab[lm][p], chunk by chunk (the sum over the
 // grid points of one site in onto_projector, projector.c:266-311, for every
-// band at once).
+// band at once). A chunk is <= CHUNK_PTS points of one site with a compile-time
+// bound of 8, 18 or 32 lm channels.
 //
-// One CTA per (chunk, block of CT bands), one band per thread. The chunk's
-// table (<= CHUNK_PTS points x its lm channels) is staged in shared memory
-// once and read as warp-wide broadcasts of two points (16 bytes); each thread
-// streams its band's picked values UP points at a time with all UP/2 16-byte
-// loads issued before they are used, so that a warp keeps several memory
-// requests in flight. The table is stored shifted by the parity of the
-// chunk's first point so that both streams stay 16-byte aligned. The channel
-// count is a compile-time bound chosen per chunk (8, 18 or 32).
+// One CTA per (chunk, block of TC rows), one row per thread. The chunk's points
+// are taken in tiles of TP: the tile's picked values are copied with cp.async,
+// each warp reading along points (consecutive addresses) into shared memory
+// transposed to [point][row], so that the row threads read them conflict-free;
+// the tile's table slice [lm][point] is read as broadcasts. Tiles are
+// double-buffered: the copies of tile t + 1 are in flight while tile t is
+// summed. Two sources: the rows of the picked-point vector X (the projection
+// pass's output) or, for a wavefunction held in real space, its grid values at
+// the points' cells (the pick itself, fused: no X is written); there the CTA's
+// rows belong to one k-point and its Bloch phase is folded into the staged
+// table slice.
 namespace {
-constexpr int CT = 128;
-constexpr int UP = 16;
-constexpr int TSTRIDE = CHUNK_PTS + 2;
-}
+constexpr int TC = 128;          // rows per CTA
+constexpr int TP = 16;           // points per staged tile (divides 32)
+constexpr int XS = TC + 1;       // row stride of a staged tile (float2)
 
-template <int NL>
-__device__ __forceinline__ void chunk_body(const ChunkContract &cc, const float2 *__restrict__ ts, int shift,
-                                           const float2 *__restrict__ x, float2 *__restrict__ o) {
+__device__ __forceinline__ void cpa8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+}  // namespace
+
+template <int NL, bool GATHER>
+__global__ void __launch_bounds__(TC) k_contract_staged(const ChunkContract *__restrict__ chunks,
+                                                        ContractSource src, float2 *__restrict__ partial, int ptot,
+                                                        int nb) {
+  extern __shared__ float4 smem4[];
+  float2 *xs = reinterpret_cast<float2 *>(smem4);  // [2][TP][XS]
+  float2 *tt = xs + 2 * TP * XS;                   // [2][NL][TP]
+  const ChunkContract cc = chunks[blockIdx.x];
+  const int n = cc.npts;
+  // rows [row0, row1) of the batch; with GATHER a block never crosses a k-point
+  int row0, row1;
+  long long kq = 0;
+  if (GATHER) {
+    const int bpk = (src.nband + TC - 1) / TC;
+    kq = src.r0 / src.nband + blockIdx.y / bpk;
+    const long long lo = kq * src.nband + (long long)(blockIdx.y % bpk) * TC;  // global row
+    const long long hi = min(min(lo + TC, (kq + 1) * src.nband), src.r0 + nb);
+    row0 = (int)(max(lo, src.r0) - src.r0);
+    row1 = (int)(hi - src.r0);
+  } else {
+    row0 = blockIdx.y * TC;
+    row1 = min(row0 + TC, nb);
+  }
+  const int nrows = row1 - row0;
+  if (nrows <= 0) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = (n + TP - 1) / TP;
+
+  auto load_tile = [&](int t, int buf) {
+    const int p0 = t * TP;
+    float2 *tb = tt + buf * NL * TP;
+    for (int e = threadIdx.x; e < NL * TP; e += TC) {
+      const int l = e / TP, q = e - l * TP, pp = p0 + q;
+      float2 v = make_float2(0.f, 0.f);
+      if (l < cc.total && pp < n) {
+        v = cc.tab[(long long)l * cc.site_npts + pp];
+        if (GATHER) {
+          const float2 f = src.gphase[kq * src.npts + cc.x_off + pp];
+          v = make_float2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
+        }
+      }
+      tb[e] = v;
+    }
+    // a warp instruction copies 32 / TP rows of TP points: lane -> (point pl, row rfirst + k RSTEP)
+    const int pl = lane % TP, rsub = lane / TP;
+    constexpr int RSTEP = (TC / 32) * (32 / TP);  // rows per pass of the whole CTA
+    const int p = p0 + pl;
+    if (p < n) {
+      const long long xo = cc.x_off + p;
+      float2 *dst = xs + ((long long)buf * TP + pl) * XS;
+      const int rfirst = warp * (32 / TP) + rsub;
+      if (GATHER) {
+        const float2 *g = src.grid + (src.r0 + row0) * src.n3d + src.gcell[xo];
+        for (int r = rfirst; r < nrows; r += RSTEP) cpa8(dst + r, g + (long long)r * src.n3d);
+      } else {
+        const float2 *x = src.X + (long long)row0 * src.xstride + xo;
+        for (int r = rfirst; r < nrows; r += RSTEP) cpa8(dst + r, x + (long long)r * src.xstride);
+      }
+    }
+    cpa_commit();
+  };
+
   float ar[NL], ai[NL];
 #pragma unroll
   for (int l = 0; l < NL; l++) ar[l] = ai[l] = 0.f;
-  const int n = cc.npts;
-  auto mac = [&](int l, float2 t, float2 v) {
-    ar[l] = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar[l]));
-    ai[l] = fmaf(t.x, v.y, fmaf(t.y, v.x, ai[l]));
-  };
-  int p = 0;
-  if (shift && n > 0) {  // odd first point: one point alone
-    const float2 v = x[0];
-#pragma unroll
-    for (int l = 0; l < NL; l++) mac(l, ts[l * TSTRIDE + shift], v);
-    p = 1;
-  }
-  for (; p + UP <= n; p += UP) {
-    float4 v[UP / 2];
-#pragma unroll
-    for (int i = 0; i < UP / 2; i++) v[i] = *reinterpret_cast<const float4 *>(x + p + 2 * i);
-#pragma unroll
-    for (int i = 0; i < UP / 2; i++)
+  load_tile(0, 0);
+  for (int t = 0; t < ntiles; t++) {
+    const int buf = t & 1;
+    if (t + 1 < ntiles) {
+      load_tile(t + 1, buf ^ 1);
+      cpa_wait<1>();
+    } else {
+      cpa_wait<0>();
+    }
+    __syncthreads();  // tile t (copies and table slice) is visible to every thread
+    const int m = min(TP, n - t * TP);
+    const float2 *xt = xs + (long long)buf * TP * XS + threadIdx.x;
+    const float2 *tb = tt + buf * NL * TP;
+    int q = 0;
+    for (; q + 1 < m; q += 2) {
+      const float2 v0 = xt[q * XS], v1 = xt[(q + 1) * XS];
 #pragma unroll
       for (int l = 0; l < NL; l++) {
-        const float4 t = *reinterpret_cast<const float4 *>(ts + l * TSTRIDE + shift + p + 2 * i);
-        mac(l, make_float2(t.x, t.y), make_float2(v[i].x, v[i].y));
-        mac(l, make_float2(t.z, t.w), make_float2(v[i].z, v[i].w));
+        const float4 w = *reinterpret_cast<const float4 *>(tb + l * TP + q);
+        ar[l] = fmaf(w.x, v0.x, fmaf(-w.y, v0.y, ar[l]));
+        ai[l] = fmaf(w.x, v0.y, fmaf(w.y, v0.x, ai[l]));
+        ar[l] = fmaf(w.z, v1.x, fmaf(-w.w, v1.y, ar[l]));
+        ai[l] = fmaf(w.z, v1.y, fmaf(w.w, v1.x, ai[l]));
       }
-  }
-  for (; p < n; p++) {
-    const float2 v = x[p];
+    }
+    if (q < m) {
+      const float2 v0 = xt[q * XS];
 #pragma unroll
-    for (int l = 0; l < NL; l++) mac(l, ts[l * TSTRIDE + shift + p], v);
+      for (int l = 0; l < NL; l++) {
+        const float2 w = tb[l * TP + q];
+        ar[l] = fmaf(w.x, v0.x, fmaf(-w.y, v0.y, ar[l]));
+        ai[l] = fmaf(w.x, v0.y, fmaf(w.y, v0.x, ai[l]));
+      }
+    }
+    __syncthreads();  // tile t is consumed before tile t + 2 overwrites its buffer
   }
+  if ((int)threadIdx.x >= nrows) return;
+  float2 *o = partial + (long long)(row0 + threadIdx.x) * ptot + cc.part_off;
 #pragma unroll
   for (int l = 0; l < NL; l++)
     if (l < cc.total) o[l] = make_float2(ar[l], ai[l]);
 }
 
-__global__ void __launch_bounds__(CT) k_chunk_contract(const ChunkContract *__restrict__ chunks,
-                                                       const float2 *__restrict__ X, long long xstride,
-                                                       float2 *__restrict__ partial, int ptot, int nb) {
-  extern __shared__ float4 ts4[];  // [nl][TSTRIDE] float2
-  float2 *ts = reinterpret_cast<float2 *>(ts4);
-  const ChunkContract cc = chunks[blockIdx.x];
-  const int shift = (int)(cc.x_off & 1);  // X rows are 16-byte aligned (even xstride)
-  const int nl = cc.total <= 8 ? 8 : cc.total <= 18 ? 18 : 32;
-  for (int e = threadIdx.x; e < nl * TSTRIDE; e += blockDim.x) {
-    const int l = e / TSTRIDE, q = e - l * TSTRIDE - shift;
-    ts[e] = l < cc.total && q >= 0 && q < cc.npts ? cc.tab[(long long)l * cc.site_npts + q] : make_float2(0.f, 0.f);
+template <int NL, bool GATHER>
+static void contract_staged(const ChunkContract *chunks, int nchunks, const ContractSource &src, float2 *partial,
+                            int ptot, int nb) {
+  const size_t smem = sizeof(float2) * (2 * (size_t)TP * XS + 2 * (size_t)NL * TP);
+  allow_dynamic_smem((const void *)k_contract_staged<NL, GATHER>, smem);
+  int blocks_y = ceil_div(nb, TC);
+  if (GATHER) {
+    // row blocks per k-point, over the k-points the batch [r0, r0 + nb) touches
+    const long long k0 = src.r0 / src.nband, k1 = (src.r0 + nb - 1) / src.nband;
+    blocks_y = (int)(k1 - k0 + 1) * ceil_div(src.nband, TC);
   }
-  __syncthreads();
-  const int b = blockIdx.y * CT + threadIdx.x;
-  if (b >= nb) return;
-  const float2 *x = X + (long long)b * xstride + cc.x_off;
-  float2 *o = partial + (long long)b * ptot + cc.part_off;
-  if (nl == 8)
-    chunk_body<8>(cc, ts, shift, x, o);
-  else if (nl == 18)
-    chunk_body<18>(cc, ts, shift, x, o);
-  else
-    chunk_body<32>(cc, ts, shift, x, o);
+  dim3 grid(nchunks, blocks_y);
+  PAWPY_LAUNCH("sphere_contract",
+               (k_contract_staged<NL, GATHER><<<grid, TC, smem, stream()>>>(chunks, src, partial, ptot, nb)));
 }
 
-void launch_chunk_contract(const ChunkContract *chunks, int nchunks, int max_total, const float2 *X,
-                           long long xstride, float2 *partial, int ptot, int nb) {
+void launch_contract_staged(const ChunkContract *chunks, int nchunks, int max_total, const ContractSource &src,
+                            float2 *partial, int ptot, int nb, long long npts) {
   if (nchunks <= 0 || nb <= 0) return;
+  note_work("sphere_contract", 8.0 * (double)npts * nb);
   if (max_total > 32) throw Error(ERR_UNSUPPORTED, "more than 32 projector channels on one site");
-  PAWPY_REQUIRE(xstride % 2 == 0, "picked-point rows must be 16-byte aligned");
-  const int nl = max_total <= 8 ? 8 : max_total <= 18 ? 18 : 32;
-  const size_t smem = sizeof(float2) * (size_t)nl * TSTRIDE;
-  allow_dynamic_smem((const void *)k_chunk_contract, smem);
-  dim3 grid(nchunks, ceil_div(nb, CT));
-  PAWPY_LAUNCH("sphere_contract",
-               k_chunk_contract<<<grid, CT, smem, stream()>>>(chunks, X, xstride, partial, ptot, nb));
+  const bool gather = src.grid != nullptr;
+  PAWPY_REQUIRE(gather || src.X, "contraction without a source");
+  PAWPY_REQUIRE(!gather || src.nband > 0, "contraction source without a band count");
+  if (max_total <= 8)
+    gather ? contract_staged<8, true>(chunks, nchunks, src, partial, ptot, nb)
+           : contract_staged<8, false>(chunks, nchunks, src, partial, ptot, nb);
+  else if (max_total <= 18)
+    gather ? contract_staged<18, true>(chunks, nchunks, src, partial, ptot, nb)
+           : contract_staged<18, false>(chunks, nchunks, src, partial, ptot, nb);
+  else
+    gather ? contract_staged<32, true>(chunks, nchunks, src, partial, ptot, nb)
+           : contract_staged<32, false>(chunks, nchunks, src, partial, ptot, nb);
+}
+
+// gcell[xo] = (i N2 + j) N3 + k and gphase[kq][xo] = the segment's Bloch phase, for every point xo
+// of the merged point space (segment si lies in plane seg_j[si] of the second axis)
+__global__ void k_point_index(const GatherSeg *__restrict__ segs, const int *__restrict__ seg_j, int N2, int N3,
+                              int nkp, long long Q, int *__restrict__ gcell, float2 *__restrict__ gphase) {
+  const GatherSeg sg = segs[blockIdx.x];
+  const int j = seg_j[blockIdx.x];
+  for (int p = threadIdx.x; p < sg.npts; p += blockDim.x) {
+    const int c = sg.idx[p], i = c / N3, k = c - i * N3;
+    const long long xo = sg.x_off + p;
+    gcell[xo] = (i * N2 + j) * N3 + k;
+    for (int q = 0; q < nkp; q++) gphase[q * Q + xo] = sg.phase[q * sg.phase_stride + p];
+  }
+}
+
+void launch_point_index(const GatherSeg *segs, const int *seg_j, int nsegs, int N2, int N3, int nkp, long long Q,
+                        int *gcell, float2 *gphase) {
+  if (nsegs <= 0) return;
+  PAWPY_LAUNCH("pick_list", k_point_index<<<nsegs, 128, 0, stream()>>>(segs, seg_j, N2, N3, nkp, Q, gcell, gphase));
 }
 
 // P[(band_base + b) * Ptot + o] = sum over the chunks c < n of the column's
