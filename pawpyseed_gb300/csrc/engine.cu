@@ -182,6 +182,11 @@ struct PairState {
   int cross_prec[2] = {-1, -1};
 };
 
+// Overlaps are between wavefunction bands: a noncollinear band is two consecutive
+// device bands (its spinor halves), so its overlap rows are twice as long.
+static int host_bands(const DevWF &d) { return d.ncl ? d.nband / 2 : d.nband; }
+static int spinor_factor(const DevWF &d) { return d.ncl ? 2 : 1; }
+
 static std::recursive_mutex g_mu;
 static std::map<const pswf_t *, std::unique_ptr<DevWF>> g_wfs;
 static std::map<std::pair<const pswf_t *, const pswf_t *>, std::unique_ptr<PairState>> g_pairs;
@@ -1167,10 +1172,10 @@ static PairState &pair_state(pswf_t *R, pswf_t *S) {
   auto &ptr = g_pairs[key];
   if (!ptr) {
     DevWF &r = mirror(R), &s = mirror(S);
-    // the reference computes no overlaps of noncollinear wavefunctions (projector.py:74-75)
-    if (r.ncl || s.ncl) {
+    // a noncollinear wavefunction overlaps only with another one (spinor against spinor)
+    if (r.ncl != s.ncl) {
       g_pairs.erase(key);
-      throw Error(ERR_UNSUPPORTED, "overlaps of noncollinear wavefunctions are not part of the projection path");
+      throw Error(ERR_UNSUPPORTED, "overlaps between a noncollinear and a collinear wavefunction are not defined");
     }
     ptr = std::make_unique<PairState>();
     ptr->R = &r;
@@ -1289,7 +1294,8 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   free_wave_projections(wf_S);
   wf_R->wp_num = nNS;
   wf_S->wp_num = nNR;
-  if (g_host_proj) {
+  // host wave_projections have the reference's collinear layout (none for spinor bands)
+  if (g_host_proj && !R.ncl) {
     for (int side = 0; side < 2; side++) {
       DevWF &W = side == 0 ? S : R;
       SphereSet &sm = side == 0 ? ps.sm_NR : ps.sm_NS;
@@ -1510,7 +1516,7 @@ static void do_overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, const int *labels
   free_wave_projections(wf_S);
   wf_R->wp_num = nNS;
   wf_S->wp_num = nNR;
-  if (g_host_proj) {
+  if (g_host_proj && !R.ncl) {
     if (!ps.N_R.empty()) publish_recip_coefficients(R, ps.CA_R);
     if (!ps.N_S.empty()) publish_recip_coefficients(S, ps.CA_S);
   }
@@ -1552,6 +1558,7 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   std::vector<GemmBatch> hb(nk);
   int maxK = 0;
   const bool recip = ps.recip && what != Contraction::kPseudo;
+  const int NR = host_bands(R), NS = host_bands(S);
   const bool haveCA_R = recip && !ps.N_R.empty(), haveCA_S = recip && !ps.N_S.empty();
   for (int k = 0; k < nk; k++) {
     int kR = flip_k(R, k, flip);
@@ -1565,16 +1572,19 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
     };
     std::vector<Seg> segs;
     const float2 *CR = coeffs(R, kR), *CS = coeffs(S, k);
-    const long long w = qR.Wpad;
+    // a noncollinear band's two spinor halves are consecutive rows: one row of twice the length
+    const int f = spinor_factor(R);
+    const long long w = (long long)f * qR.Wpad, kc = (long long)f * ps.Kcpad;
+    const int K = f * qR.Wpad;
     if (what == Contraction::kCross) {
-      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, qR.Wpad});
-      if (haveCA_S) segs.push_back({CR, ps.CA_S.p + qS.c_off, w, w, qR.Wpad});
+      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, K});
+      if (haveCA_S) segs.push_back({CR, ps.CA_S.p + qS.c_off, w, w, K});
     } else {
-      segs.push_back({CR, haveCA_S ? ps.D_S.p + qS.c_off : CS, w, w, qR.Wpad});
-      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, qR.Wpad});
+      segs.push_back({CR, haveCA_S ? ps.D_S.p + qS.c_off : CS, w, w, K});
+      if (haveCA_R) segs.push_back({ps.CA_R.p + qR.c_off, CS, w, w, K});
       if (B32 && what == Contraction::kAugmented)
-        segs.push_back({ps.A32.p + (size_t)kR * R.nband * ps.Kcpad, B32 + (size_t)k * S.nband * ps.Kcpad,
-                        ps.Kcpad, ps.Kcpad, ps.Kcpad});
+        segs.push_back({ps.A32.p + (size_t)kR * R.nband * ps.Kcpad, B32 + (size_t)k * S.nband * ps.Kcpad, kc, kc,
+                        (int)kc});
     }
     GemmBatch &g = hb[k];
     g.A1 = g.B1 = g.A2 = g.B2 = nullptr;
@@ -1589,26 +1599,26 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
     if (segs.size() > 2) {
       g.A3 = segs[2].A, g.B3 = segs[2].B, g.lda3 = segs[2].lda, g.ldb3 = segs[2].ldb, g.K3 = segs[2].K;
     }
-    g.out = out + (size_t)k * S.nband * R.nband;
+    g.out = out + (size_t)k * NS * NR;
     maxK = std::max(maxK, g.K1 + g.K2 + g.K3);
   }
   if (maxK == 0) {
-    PAWPY_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * (size_t)nk * S.nband * R.nband, stream()));
+    PAWPY_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * (size_t)nk * NS * NR, stream()));
     return;
   }
   DevBuf<GemmBatch> db(nk);
   db.upload(hb.data(), nk);
   double flops = 0;  // useful flops: 8 per complex multiply-add of every K segment
-  for (const GemmBatch &g : hb) flops += 8.0 * R.nband * S.nband * (double)(g.K1 + g.K2 + g.K3);
+  for (const GemmBatch &g : hb) flops += 8.0 * NR * NS * (double)(g.K1 + g.K2 + g.K3);
   note_work(prec == PAWPY_GPU_BF16X3 ? "gemm_bf16x3" : prec == PAWPY_GPU_TF32 ? "gemm_tf32" : "gemm_f32", flops);
   if (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32) {
-    launch_zgemm_tc(db.p, hb, R.nband, S.nband, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+    launch_zgemm_tc(db.p, hb, NR, NS, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
     return;
   }
-  int splits = choose_splits(R.nband, S.nband, nk, maxK);
+  int splits = choose_splits(NR, NS, nk, maxK);
   DevBuf<float2> ws;
-  if (splits > 1) ws.alloc((size_t)splits * nk * S.nband * R.nband);
-  launch_zgemm_f32(db.p, nk, R.nband, S.nband, splits, ws.p);
+  if (splits > 1) ws.alloc((size_t)splits * nk * NS * NR);
+  launch_zgemm_f32(db.p, nk, NR, NS, splits, ws.p);
 }
 
 static void ensure_pseudo(PairState &ps, int flip) {
@@ -1616,7 +1626,7 @@ static void ensure_pseudo(PairState &ps, int flip) {
   const int prec = g_precision.load();
   if (ps.pseudo_ready[f] && ps.pseudo_prec[f] == prec) return;
   DevWF &R = *ps.R, &S = *ps.S;
-  ps.pseudo[f].alloc((size_t)S.nk * S.nband * R.nband);
+  ps.pseudo[f].alloc((size_t)S.nk * host_bands(S) * host_bands(R));
   overlap_gemm(ps, f, nullptr, ps.pseudo[f].p, prec, Contraction::kPseudo);
   ps.pseudo_ready[f] = true;
   ps.pseudo_prec[f] = prec;
@@ -1628,7 +1638,7 @@ static void ensure_cross(PairState &ps, int flip) {
   const int prec = g_precision.load();
   if (ps.cross_ready[f] && ps.cross_prec[f] == prec) return;
   DevWF &R = *ps.R, &S = *ps.S;
-  ps.cross[f].alloc((size_t)S.nk * S.nband * R.nband);
+  ps.cross[f].alloc((size_t)S.nk * host_bands(S) * host_bands(R));
   overlap_gemm(ps, f, nullptr, ps.cross[f].p, prec, Contraction::kCross);
   ps.cross_ready[f] = true;
   ps.cross_prec[f] = prec;
@@ -1913,8 +1923,8 @@ void pseudoprojection(pawpy_c128 *projections, pswf_t *wf_ref, pswf_t *wf_proj, 
   ensure_pseudo(ps, flip_spin);
   DevWF &R = *ps.R, &S = *ps.S;
   int f = flip_spin ? 1 : 0;
-  DevBuf<double2> col((size_t)R.nband * S.nk);
-  launch_extract_band(ps.pseudo[f].p, S.nk, S.nband, R.nband, BAND_NUM, col.p);
+  DevBuf<double2> col((size_t)host_bands(R) * S.nk);
+  launch_extract_band(ps.pseudo[f].p, S.nk, host_bands(S), host_bands(R), BAND_NUM, col.p);
   col.download(reinterpret_cast<double2 *>(projections), col.n);
   sync();
   PAWPY_API_END()
@@ -1939,31 +1949,34 @@ static void do_compensation_terms(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_
   ensure_aug(ps, lists, flip_spin);
   DevWF &R = *ps.R, &S = *ps.S;
   int nk = S.nk, npairs = (int)ps.N_RS_R.size();
-  DevBuf<double2> B64((size_t)nk * std::max(1, ps.Kc));
-  launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, BAND_NUM, 1, nk, ps.b_ptr.p, ps.b_col.p,
+  // a noncollinear band's two spinor halves are consecutive device bands: their columns form
+  // one row of f Kc values (the PAW terms summed over both components)
+  const int f = spinor_factor(S), NR = host_bands(R), NS = host_bands(S), kc = f * ps.Kc;
+  DevBuf<double2> B64((size_t)nk * std::max(1, kc));
+  launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, f * BAND_NUM, f, nk, ps.b_ptr.p, ps.b_col.p,
                ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kc, B64.p, nullptr);
-  DevBuf<double2> acc((size_t)nk * R.nband);
+  DevBuf<double2> acc((size_t)nk * NR);
   acc.zero();
   for (int k = 0; k < nk; k++) {
     int kR = flip_k(R, k, flip_spin);
     if (ps.Kc > 0)
-      launch_zgemv_f64(ps.A64.p + (size_t)kR * R.nband * ps.Kc, ps.Kc, R.nband, ps.Kc, B64.p + (size_t)k * ps.Kc,
-                       acc.p + (size_t)k * R.nband);
+      launch_zgemv_f64(ps.A64.p + (size_t)kR * R.nband * ps.Kc, kc, NR, kc, B64.p + (size_t)k * kc,
+                       acc.p + (size_t)k * NR);
   }
   std::vector<double2> h(acc.n), hx;
   acc.download(h.data(), h.size());
   if (recip) {
     // cross terms of this band, col[bR][k]
     ensure_cross(ps, flip_spin);
-    DevBuf<double2> col((size_t)R.nband * nk);
-    launch_extract_band(ps.cross[flip_spin ? 1 : 0].p, nk, S.nband, R.nband, BAND_NUM, col.p);
+    DevBuf<double2> col((size_t)NR * nk);
+    launch_extract_band(ps.cross[flip_spin ? 1 : 0].p, nk, NS, NR, BAND_NUM, col.p);
     hx.resize(col.n);
     col.download(hx.data(), hx.size());
   }
   sync();
-  for (int b = 0; b < R.nband; b++)
+  for (int b = 0; b < NR; b++)
     for (int k = 0; k < nk; k++) {
-      double2 v = h[(size_t)k * R.nband + b];
+      double2 v = h[(size_t)k * NR + b];
       overlap[(size_t)b * nk + k] += pawpy_c128(v.x, v.y);
       if (recip) {
         double2 x = hx[(size_t)b * nk + k];
@@ -2025,7 +2038,7 @@ static void full_overlap(PairState &ps, const std::vector<int> lists[6], int fli
   DevBuf<float2> B32((size_t)nk * S.nband * std::max(16, ps.Kcpad));
   launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, 0, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
                ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
-  Smat.alloc((size_t)nk * S.nband * R.nband);
+  Smat.alloc((size_t)nk * host_bands(S) * host_bands(R));
   overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p, g_precision.load());
 }
 
@@ -2044,10 +2057,10 @@ int pawpy_gpu_project_all(pawpy_c128 *out, pswf_t *wf_R, pswf_t *wf_S, int num_M
   const int nk = S.nk;
   if (pageable_access()) {
     // the device writes the caller's (pageable) array through the host page tables
-    launch_to_host_layout(Smat.p, nk, S.nband, R.nband, reinterpret_cast<double2 *>(out));
+    launch_to_host_layout(Smat.p, nk, host_bands(S), host_bands(R), reinterpret_cast<double2 *>(out));
   } else {
     DevBuf<double2> o64(Smat.n);
-    launch_to_host_layout(Smat.p, nk, S.nband, R.nband, o64.p);
+    launch_to_host_layout(Smat.p, nk, host_bands(S), host_bands(R), o64.p);
     o64.download(reinterpret_cast<double2 *>(out), o64.n);
   }
   sync();
@@ -2067,11 +2080,11 @@ int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, i
   DevBuf<float2> Smat;
   full_overlap(ps, lists, flip_spin, Smat);
   DevWF &R = *ps.R, &S = *ps.S;
-  const int nk = S.nk, nw = (int)((size_t)R.nband * nk);
-  DevBuf<double> wv(nw), wc(nw), dv((size_t)S.nband * nch), dc((size_t)S.nband * nch);
+  const int nk = S.nk, nw = (int)((size_t)host_bands(R) * nk);
+  DevBuf<double> wv(nw), wc(nw), dv((size_t)host_bands(S) * nch), dc((size_t)host_bands(S) * nch);
   wv.upload(w_v, nw);
   wc.upload(w_c, nw);
-  launch_band_character(Smat.p, nk, S.nband, R.nband, wv.p, wc.p, S.nwk, nch, dv.p, dc.p);
+  launch_band_character(Smat.p, nk, host_bands(S), host_bands(R), wv.p, wc.p, S.nwk, nch, dv.p, dc.p);
   dv.download(v, dv.n);
   dc.download(c, dc.n);
   sync();

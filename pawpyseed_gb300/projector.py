@@ -20,14 +20,18 @@ from .wavefunction import Timer, Wavefunction
 class Projector:
     METHODS = ["pseudo", "realspace", "aug_recip", "aug_real"]
 
-    def __init__(self, wf, basis, unsym_basis=False, unsym_wf=False, method="aug_real"):
+    def __init__(self, wf, basis, unsym_basis=False, unsym_wf=False, method="aug_real", noncollinear=False):
+        """noncollinear (an extension; the reference refuses spinor wavefunctions,
+        projector.py:74-75): with two noncollinear wavefunctions, the overlaps are the sums over
+        both spinor components, <psi_R|psi_S> = sum_s <psi_R^s|psi_S^s>, each component with its
+        own PAW terms."""
         self.method = method
         if method not in self.METHODS:
             raise PAWpyError("method not recognized for Projector")
         if method == "realspace":
             raise PAWpyError("method %r is not part of this library's projection path; "
                              "use 'aug_real' (the reference default), 'aug_recip' or 'pseudo'" % method)
-        if wf.ncl or basis.ncl:
+        if (wf.ncl or basis.ncl) and not (noncollinear and wf.ncl and basis.ncl):
             raise PAWpyError("Projection not supported for noncollinear case!")
         if unsym_basis or unsym_wf:
             raise PAWpyError("k-point desymmetrization is not part of this library; "

@@ -1,8 +1,10 @@
-"""Noncollinear projections: setup_projections on a spinor wavefunction fills
+"""Noncollinear projections and overlaps. setup_projections on a spinor wavefunction fills
 every band's up_projections and down_projections (onto_projector_ncl,
 projector.c:359-392) — the two halves share the G list. Checked against the
 FP64 oracle run on each half as a collinear wavefunction; tolerance 1e-5
-relative to the largest coefficient (as the collinear projector test)."""
+relative to the largest coefficient (as the collinear projector test). The
+spinor overlaps (an extension: the reference refuses them) are checked against
+the sum of the oracle's overlaps of the two halves."""
 
 import os
 import sys
@@ -51,16 +53,61 @@ def test_ncl_projections_match_oracle_on_each_half():
                 assert np.abs(mine - ref[b]).max() <= 1e-5 * scale
 
 
-def test_ncl_overlaps_are_refused():
+def ncl_pair(nband=4, nk=2):
+    """A noncollinear basis and defect of the 8-atom cell (atom 0 moved 0.1 A)."""
+    from pawpyseed_gb300 import synth, vaspio
+
+    w = synth.small_workload(0, nband=nband, nk=nk)
+    bs, ds = synth.structures(0)
+    cr = vaspio.CoreRegion(synth.potcar_text(["A"]))
+    return bs, ds, cr, w, synth.wavefunction_data(bs, w, 78, ncl=True), synth.wavefunction_data(ds, w, 79, ncl=True)
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
+def test_ncl_overlaps_match_fp64_sum_over_spinor_halves(precision):
+    """Spinor overlaps <psi_R|psi_S> = sum over the up and down components of the PAW overlap of
+    each component (pseudo overlap + O_M + O_R + O_S + O_N). The reference defines no overlap of
+    noncollinear wavefunctions (projector.py:74-75), so the truth is the FP64 oracle's collinear
+    overlaps of each half, summed; tolerance 1e-5. The per-band entry points (pseudoprojection +
+    compensation_terms) must give the batched matrix's rows."""
+    import oracle as orc
+
     from pawpyseed_gb300 import _lib
+    from pawpyseed_gb300.projector import Projector
     from pawpyseed_gb300.wavefunction import NCLWavefunction
+
+    bs, ds, cr, w, bd, dd = ncl_pair()
+    basis = NCLWavefunction.from_arrays(bs, cr, w["dim"], bd)
+    wf = NCLWavefunction.from_arrays(ds, cr, w["dim"], dd)
+    prec0 = _lib.get_precision()
+    _lib.set_precision(precision)
+    try:
+        pr = Projector(wf, basis, noncollinear=True)
+        full = pr.project_all()
+        rows = np.array([pr.single_band_projection(b) for b in range(wf.nband)])
+    finally:
+        _lib.set_precision(prec0)
+    truth = 0
+    for h in (0, 1):
+        ob = orc.OracleWavefunction(data=half(bd, h), struct=bs, cr=cr, dim=w["dim"])
+        ow = orc.OracleWavefunction(data=half(dd, h), struct=ds, cr=cr, dim=w["dim"])
+        op = orc.OracleProjector(ow, ob)
+        truth = truth + np.array([op.band_vector(op.full(), b) for b in range(ow.nband)])
+    assert full.shape == truth.shape == (wf.nband, basis.nband * basis.nwk * basis.nspin)
+    assert np.abs(full - truth).max() <= 1e-5
+    assert np.abs(rows - full).max() <= 1e-6
+
+
+def test_mixed_collinear_noncollinear_overlaps_are_refused():
+    from pawpyseed_gb300 import _lib, synth
+    from pawpyseed_gb300.wavefunction import NCLWavefunction, Wavefunction
 
     bs, cr, w, data = ncl_case(nband=2, nk=1)
     a = NCLWavefunction.from_arrays(bs, cr, w["dim"], data)
-    b = NCLWavefunction.from_arrays(bs, cr, w["dim"], data)
+    b = Wavefunction.from_arrays(bs, cr, w["dim"], synth.wavefunction_data(bs, w, 5))
     a.check_c_projectors()
     b.check_c_projectors()
     res = np.zeros(b.nband * b.nwk * b.nspin, np.complex128)
     _lib.lib().pseudoprojection(res, b.wf_ptr, a.wf_ptr, 0, 0)
-    with pytest.raises(_lib.PAWpyGPUError):
+    with pytest.raises(_lib.PAWpyGPUError, match="noncollinear"):
         _lib.check()
