@@ -274,9 +274,15 @@ void pawpy_gpu_clear_error(void);
 /* Overlap precision for the device overlap matrices (default FP32). */
 void pawpy_gpu_set_precision(int precision);
 int pawpy_gpu_get_precision(void);
-/* K split of the tensor-core overlap contraction (0 = chosen from the SM
- * count, the default). No counterpart in the reference. */
+/* K split of the tensor-core overlap contraction (0 = chosen with the tile
+ * width, the default). No counterpart in the reference. */
 void pawpy_gpu_set_tc_splits(int splits);
+/* Tile width of the tensor-core overlap contraction: 128 or 64 defect bands
+ * per tile (64: two CTAs per SM, for few defect bands), or 0 (the default) to
+ * time the candidate widths and split counts once per problem shape and keep
+ * the fastest (PAWPY_GPU_TUNE_VERBOSE=1 prints each decision). No counterpart
+ * in the reference. */
+void pawpy_gpu_set_tc_tile(int bn);
 
 /* Batched overlap matrices of host arrays, no counterpart in the reference
  * (pseudoprojection's contraction, pseudoprojector.c:63-90, on raw matrices):

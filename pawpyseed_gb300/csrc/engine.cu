@@ -1793,6 +1793,7 @@ void pawpy_gpu_set_precision(int precision) {
 int pawpy_gpu_get_precision(void) { return g_precision; }
 void pawpy_gpu_set_tc_splits(int splits) { g_tc_splits = splits < 0 ? 0 : splits; }
 void pawpy_gpu_set_element_cache(int on) { set_projector_list_cache(on != 0); }
+void pawpy_gpu_set_tc_tile(int bn) { set_tc_tile(bn); }
 
 int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
                              pawpy_c64 *out, int precision) {

@@ -165,8 +165,10 @@ void launch_zgemm_f32(const GemmBatch *batches_dev, int nz, int M, int N, int sp
 // 3-term (tf32 false) or TF32 operands, FP32 accumulation. hb is the host copy
 // of batches_dev. splits_hint <= 0 picks the K split from the SM count.
 // A pipeline wait of the kernel that ran out makes the next sync() throw.
+// Tile width of the tensor-core contraction: 64 or 128 defect bands, 0 = timed per shape.
+void set_tc_tile(int bn);
 struct TcGemmInfo {
-  int splits = 0, Kc = 0, ctas = 0;
+  int splits = 0, Kc = 0, ctas = 0, bn = 0;  // bn: defect bands per tile
 };
 void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
                      int splits_hint, TcGemmInfo *info);

@@ -11,8 +11,9 @@
 //               lo = bf16(x - hi); products hi*hi + hi*lo + lo*hi (lo*lo,
 //               about 2^-18 of |a||b|, is dropped), FP32 accumulation;
 //   TF32:       re, im in FP32 read as TF32 by the tensor core.
-// One CTA computes a 128 (basis bands) x 128 (defect bands) tile of one
-// k-point over a K range (split-K). A single thread issues TMA copies of
+// One CTA computes a 128 (basis bands) x BN (defect bands, BN = 128 or 64) tile
+// of one k-point over a K range (split-K); the tile width and the split count
+// are chosen per problem shape by timing the candidates once (run_tc). A single thread issues TMA copies of
 // 64-byte-wide K blocks (64-byte swizzle) into a ring of shared-memory stages,
 // a second issues tcgen05.mma from them into TMEM, and eight warps drain the
 // accumulators into registers (see k_tc_zgemm). Partial sums over K ranges
@@ -27,6 +28,12 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+
 #include "kernels.h"
 
 namespace pawpy {
@@ -34,26 +41,28 @@ namespace pawpy {
 namespace {
 
 constexpr int TM = 128;          // basis bands per tile (TMEM lanes)
-constexpr int TN = 128;          // defect bands per tile (TMEM columns per accumulator)
+constexpr int BN_MAX = 128;      // widest defect-band tile; operand B rows are padded to it
 constexpr int ROWB = 64;         // bytes of one K block row (64-byte swizzle span)
 constexpr int DRAIN_WARPS = 8;   // warps 2..9
 constexpr int NTHREADS = 32 * (2 + DRAIN_WARPS);
-constexpr int TMEM_COLS = 4 * TN;  // two sets of (re, im)
 constexpr int FLUSH = 4;         // K blocks per accumulation interval
 constexpr unsigned long long kWaitNs = 4000000000ull;
 
-template <bool TF32>
+// BN defect bands per tile (TMEM columns per accumulator): 128, or 64 with two CTAs per SM
+// (half the TMEM columns and fewer stages, so that two fit in TMEM and shared memory).
+template <bool TF32, int BN>
 struct Prec {
   static constexpr int NPL = TF32 ? 2 : 4;            // planes per operand
   static constexpr int ESZ = TF32 ? 4 : 2;            // bytes per element
   static constexpr int KB = ROWB / ESZ;               // elements per K block
   static constexpr int KSTEPS = 2;                    // 32-byte MMA K steps per block
   static constexpr int A_PLANE = TM * ROWB;           // 8 KB
-  static constexpr int B_PLANE = TN * ROWB;           // 8 KB
+  static constexpr int B_PLANE = BN * ROWB;           // 8 or 4 KB
   static constexpr int STAGE = NPL * (A_PLANE + B_PLANE);
-  static constexpr int STAGES = TF32 ? 6 : 3;
+  static constexpr int STAGES = BN == 128 ? (TF32 ? 6 : 3) : (TF32 ? 4 : 2);
   static constexpr int SMEM = STAGES * STAGE + 1024;  // + alignment slack
   static constexpr int NTERMS = TF32 ? 4 : 12;
+  static constexpr int TMEM_COLS = 4 * BN;            // two sets of (re, im)
 };
 
 // Products of one K step: A plane | B plane << 4 | accumulator (0 re, 1 im)
@@ -133,10 +142,10 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
 }
 
 // Instruction descriptor of kind::f16 (BF16 inputs) or kind::tf32, FP32
-// accumulation, both operands K-major, M = TM (128), N = TN (128).
-__host__ __device__ constexpr uint32_t idesc(bool tf32, bool negA) {
+// accumulation, both operands K-major, M = TM (128), N = bn.
+__host__ __device__ constexpr uint32_t idesc(bool tf32, bool negA, int bn) {
   return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) | ((negA ? 1u : 0u) << 13) |
-         (static_cast<uint32_t>(TN >> 3) << 17) | (static_cast<uint32_t>(TM >> 4) << 24);
+         (static_cast<uint32_t>(bn >> 3) << 17) | (static_cast<uint32_t>(TM >> 4) << 24);
 }
 
 template <bool TF32>
@@ -187,12 +196,14 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 // FP32 accumulator at every instruction, an error biased towards zero that
 // grows with the magnitude it accumulates; draining keeps that magnitude to a
 // few K blocks, so the bias stays near 6 FLUSH 2^-24 |S| whatever K is.
-template <bool TF32>
-__global__ void __launch_bounds__(NTHREADS, 1)
+template <bool TF32, int BN>
+__global__ void __launch_bounds__(NTHREADS, (BN == 128 ? 1 : 2))  // CTAs per SM
     k_tc_zgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                const GemmBatch *__restrict__ batches, const int *__restrict__ kblocks, int M, int N, int Mpad,
                int Npad, int nz, int splits, float2 *__restrict__ ws, int *__restrict__ status) {
-  using P = Prec<TF32>;
+  using P = Prec<TF32, BN>;
+  constexpr int TN = BN;
+  constexpr int TMEM_COLS = P::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bar_full[P::STAGES], bar_empty[P::STAGES];
   __shared__ __align__(8) unsigned long long bar_accf[2], bar_acce[2], bar_drain;
@@ -272,7 +283,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       // MMA issuer
-      const uint32_t id_pos = idesc(TF32, false), id_neg = idesc(TF32, true);
+      const uint32_t id_pos = idesc(TF32, false, BN), id_neg = idesc(TF32, true, BN);
       int i = 0;
       bool stop = false;
       for (int q = 0; q < nq && !stop; q++) {
@@ -468,10 +479,45 @@ int sm_count() {
   return n;
 }
 
+// One launch of the contraction with tiles of bn defect bands and the given K split (plus
+// the fixed-order reduction of the split partial sums).
+template <bool TF32, int BN>
+void launch_tile(const CUtensorMap &ma, const void *pb, int Kc, const GemmBatch *batches_dev, const int *kb_dev,
+                 int M, int N, int Mpad, int Npad, int nz, int splits, float2 *ws, int *st) {
+  using P = Prec<TF32, BN>;
+  const CUtensorMap mb = plane_map(const_cast<void *>(pb), TF32, Kc, (long long)P::NPL * nz * Npad, BN);
+  allow_dynamic_smem((const void *)k_tc_zgemm<TF32, BN>, P::SMEM);
+  dim3 grid(Mpad / TM, ceil_div(N, BN), nz * splits);
+  PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
+               (k_tc_zgemm<TF32, BN><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev, M, N, Mpad,
+                                                                           Npad, nz, splits, ws, st)));
+  if (splits > 1) {
+    dim3 g2(ceil_div((long long)M * N, 256 * 4), nz);
+    PAWPY_LAUNCH("gemm_reduce", k_split_reduce<<<g2, 256, 0, stream()>>>(batches_dev, ws, M, N, splits, nz));
+  }
+}
+
+// Tile width and K split per problem shape, chosen once per process by timing the candidates
+// (PAWPY_GPU_TUNE_VERBOSE=1 prints each decision with the candidates' times). The key is the
+// precision (and a forced width), the basis band count, the defect band count in steps of 64,
+// the batch count and the K length in steps of 4096.
+struct TcChoice {
+  int bn = 128, splits = 1;
+};
+std::atomic<int> g_tc_tile{0};  // 0: tuned; 64 or 128: that tile width only
+std::mutex &tc_tune_mutex() {
+  static std::mutex m;
+  return m;
+}
+std::map<std::tuple<int, int, int, int, int>, TcChoice> &tc_tuned() {
+  static std::map<std::tuple<int, int, int, int, int>, TcChoice> m;
+  return m;
+}
+
 template <bool TF32>
 void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, int splits_hint,
             TcGemmInfo *info) {
-  using P = Prec<TF32>;
+  using P = Prec<TF32, BN_MAX>;
   HostPhase hp("tc_gemm");
   const int nz = (int)hb.size();
   int maxK = 0, minkb = 1 << 30;
@@ -483,10 +529,34 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
     minkb = std::min(minkb, kbl[z]);
   }
   const int Kc = ceil_div(std::max(maxK, 1), P::KB) * P::KB;
-  const int Mpad = ceil_div(M, TM) * TM, Npad = ceil_div(N, TN) * TN;
-  const int tiles = (Mpad / TM) * (Npad / TN) * nz;
-  int splits = splits_hint > 0 ? splits_hint : std::max(1, sm_count() / tiles);
-  splits = std::max(1, std::min(splits, std::max(1, minkb / 4)));
+  const int Mpad = ceil_div(M, TM) * TM, Npad = ceil_div(N, BN_MAX) * BN_MAX;
+  // K split for a tile width: enough CTAs for the SMs, at least 4 K blocks per split
+  auto splits_for = [&](int bn) {
+    const int tiles = (Mpad / TM) * ceil_div(N, bn) * nz;
+    int sp = splits_hint > 0 ? splits_hint : std::max(1, sm_count() * (bn == 128 ? 1 : 2) / tiles);
+    return std::max(1, std::min(sp, std::max(1, minkb / 4)));
+  };
+  std::vector<TcChoice> cands;
+  auto add = [&](int bn, int sp) {
+    sp = std::max(1, std::min(sp, std::max(1, minkb / 4)));
+    for (auto &c : cands)
+      if (c.bn == bn && c.splits == sp) return;
+    cands.push_back({bn, sp});
+  };
+  const int forced = g_tc_tile.load();
+  if (splits_hint > 0) {
+    add(forced == 64 ? 64 : 128, splits_for(forced == 64 ? 64 : 128));
+  } else {
+    for (int bn : {128, 64}) {
+      if (forced && bn != forced) continue;
+      const int s0 = splits_for(bn);
+      add(bn, s0);
+      add(bn, 2 * s0);
+      add(bn, s0 / 2);
+    }
+  }
+  int max_splits = 1;
+  for (auto &c : cands) max_splits = std::max(max_splits, c.splits);
 
   DevBuf<unsigned char> pa((size_t)P::NPL * nz * Mpad * Kc * P::ESZ);
   DevBuf<unsigned char> pb((size_t)P::NPL * nz * Npad * Kc * P::ESZ);
@@ -499,29 +569,73 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
     PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g2, 256, 0, stream()>>>(batches_dev, 1, N, Npad, Kc, nz, pb.p));
   }
   const CUtensorMap ma = plane_map(pa.p, TF32, Kc, (long long)P::NPL * nz * Mpad, TM);
-  const CUtensorMap mb = plane_map(pb.p, TF32, Kc, (long long)P::NPL * nz * Npad, TN);
-
   DevBuf<float2> ws;
-  if (splits > 1) ws.alloc((size_t)splits * nz * N * M);
+  if (max_splits > 1) ws.alloc((size_t)max_splits * nz * N * M);
   int *st = device_status();
-  allow_dynamic_smem((const void *)k_tc_zgemm<TF32>, P::SMEM);
-  dim3 grid(Mpad / TM, Npad / TN, nz * splits);
-  PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
-               k_tc_zgemm<TF32><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev.p, M, N, Mpad,
-                                                                       Npad, nz, splits, ws.p, st));
-  if (splits > 1) {
-    dim3 g2(ceil_div((long long)M * N, 256 * 4), nz);
-    PAWPY_LAUNCH("gemm_reduce", k_split_reduce<<<g2, 256, 0, stream()>>>(batches_dev, ws.p, M, N, splits, nz));
+  auto run = [&](const TcChoice &c) {
+    if (c.bn == 128)
+      launch_tile<TF32, 128>(ma, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
+    else
+      launch_tile<TF32, 64>(ma, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
+  };
+  TcChoice choice = cands[0];
+  if (cands.size() > 1) {
+    const auto key = std::make_tuple((TF32 ? 1 : 0) + 2 * forced, M, ceil_div(N, 64), nz, ceil_div(Kc, 4096));
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> lk(tc_tune_mutex());
+      auto it = tc_tuned().find(key);
+      if (it != tc_tuned().end()) {
+        choice = it->second;
+        have = true;
+      }
+    }
+    if (!have) {
+      // every candidate computes the full result; the chosen one runs again below
+      std::vector<cudaEvent_t> ev(cands.size() + 1);
+      for (auto &e : ev) PAWPY_CUDA(cudaEventCreate(&e));
+      PAWPY_CUDA(cudaEventRecord(ev[0], stream()));
+      for (size_t i = 0; i < cands.size(); i++) {
+        run(cands[i]);
+        PAWPY_CUDA(cudaEventRecord(ev[i + 1], stream()));
+      }
+      PAWPY_CUDA(cudaEventSynchronize(ev.back()));
+      float best = 1e30f;
+      std::string log;
+      for (size_t i = 0; i < cands.size(); i++) {
+        float ms = 0;
+        PAWPY_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+        char buf[64];
+        snprintf(buf, sizeof buf, " (%d,%d):%.4f", cands[i].bn, cands[i].splits, ms);
+        log += buf;
+        if (ms < best) {
+          best = ms;
+          choice = cands[i];
+        }
+      }
+      for (auto &e : ev) cudaEventDestroy(e);
+      status_readback(st, "tensor-core overlap: a pipeline wait timed out");
+      if (const char *v = getenv("PAWPY_GPU_TUNE_VERBOSE"))
+        if (v[0] == '1')
+          fprintf(stderr, "[pawpy tune] tc_gemm %s M=%d N=%d nz=%d Kc=%d (tile width, splits):ms%s -> (%d,%d)\n",
+                  TF32 ? "tf32" : "bf16x3", M, N, nz, Kc, log.c_str(), choice.bn, choice.splits);
+      std::lock_guard<std::mutex> lk(tc_tune_mutex());
+      tc_tuned()[key] = choice;
+    }
   }
+  run(choice);
   status_readback(st, "tensor-core overlap: a pipeline wait timed out");
   if (info) {
-    info->splits = splits;
+    info->splits = choice.splits;
     info->Kc = Kc;
-    info->ctas = grid.x * grid.y * grid.z;
+    info->ctas = (Mpad / TM) * ceil_div(N, choice.bn) * nz * choice.splits;
+    info->bn = choice.bn;
   }
 }
 
 }  // namespace
+
+void set_tc_tile(int bn) { g_tc_tile = (bn == 64 || bn == 128) ? bn : 0; }
 
 void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
                      int splits_hint, TcGemmInfo *info) {

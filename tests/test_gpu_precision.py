@@ -140,3 +140,29 @@ def test_projections_in_each_precision(name, workload_dirs, oracle_projectors):
                 assert np.abs(one - tv[-1]).max() <= TOL[prec]
     finally:
         _lib.set_precision("fp32")
+
+
+@pytest.mark.parametrize("tile", [64, 128, 0])
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("shape", SHAPES + [(300, 40, [5000, 4100]), (16, 100, [2048])],
+                         ids=lambda s: "%dx%dx%d" % (s[0], s[1], len(s[2])))
+def test_tensor_core_tile_widths(tile, prec, shape):
+    """Both tile widths of the tensor-core contraction (64 and 128 defect bands per tile, the
+    64-band tiles two CTAs per SM) and the tuner's choice (0) against FP64, on partial tiles and
+    uneven K; the tuner times every candidate once per shape, each computing the full result."""
+    from pawpyseed_gb300 import _lib
+
+    M, N, Ks = shape
+    rng = np.random.default_rng(M * 31 + N + 7 * tile)
+    As = [unit_rows(rng, M, k, scale_tail=True) for k in Ks]
+    Bs = [unit_rows(rng, N, k, scale_tail=True) for k in Ks]
+    L = _lib.lib()
+    L.pawpy_gpu_set_tc_tile(tile)
+    try:
+        s = _lib.overlap_matrix(As, Bs, prec)
+        s2 = _lib.overlap_matrix(As, Bs, prec)  # the tuned or cached choice again
+    finally:
+        L.pawpy_gpu_set_tc_tile(0)
+    t = truth(As, Bs)
+    assert np.abs(s - t).max() <= TOL[prec]
+    assert np.abs(s2 - t).max() <= TOL[prec]
