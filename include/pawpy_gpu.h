@@ -2,10 +2,11 @@
  *
  * Drop-in for the hot path of pawpyseed's C core: the structs below have the
  * binary layout of pawpyseed/core/utils.h:30-166 (the Cython layer reads
- * pswf_t members directly, e.g. pawpyc.pyx:537), and the nine entry points
- * in section 2 keep the exact names and signatures that pawpyc_extern.pxd
- * declares, so the Cython extension links against this library unchanged
- * (the aug_recip pair overlap_setup_recip / compensation_terms_recip included).
+ * pswf_t members directly, e.g. pawpyc.pyx:537), and the entry points in
+ * section 2 keep the exact names and signatures that pawpyc_extern.pxd
+ * declares, so the Cython extension links against this library unchanged:
+ * the aug_real path, the aug_recip pair overlap_setup_recip /
+ * compensation_terms_recip, and the real-space functions of density.c.
  * Section 3 adds batched entry points, status reporting and host helpers;
  * they use a pawpy_gpu_ prefix so that they never collide with reference
  * symbols.
@@ -247,6 +248,35 @@ void compensation_terms_recip(pawpy_c128 *overlap, int BAND_NUM, pswf_t *wf_S,
                               double *proj_coords, int *ref_labels, double *ref_coords,
                               int *fft_grid, int flip_spin);
 
+/* The 'realspace' method and all-electron densities (density.c; declared
+ * pawpyc_extern.pxd:252-262). All-electron wavefunction of band BAND_NUM,
+ * k-point KPOINT_NUM (spin-major) on the grid fftg:
+ *   x[(i N2 + j) N3 + k] = V^-1/2 sum_G C_G e^{iG.r} e^{2 pi i k.r}
+ *     + sum_sites sum_nlm <p_nlm|psi> (phi_nl - phit_nl)(|r-R|)/|r-R| Y_lm e^{2 pi i k.(R+T)}
+ * within the last radius of each element's partial-wave grid (realspace_state,
+ * density.c:245-310). Computed on the device (single precision grids; double
+ * precision sphere tables); the sphere terms of overlapping sites are added in
+ * site order. Needs setup_projections on wf; labels/coords are its sites. */
+void realspace_state(pawpy_c128 *x, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg,
+                     int *labels, double *coords);
+/* x *= exp(-2 pi i k.r) on the grid fftg (remove_phase, density.c:312-326). */
+void remove_phase(pawpy_c128 *x, int KPOINT_NUM, pswf_t *wf, int *fftg);
+/* P[i] += |realspace_state|^2 of one band (ae_state_density, density.c:27-37). */
+void ae_state_density(double *P, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg,
+                      int *labels, double *coords);
+/* P[i] += sum over k and occupied bands of |psi|^2 * k-weight * occupation *
+ * 2 / nspin (ae_chg_density, density.c:158-178); accumulated in double
+ * precision on the device. */
+void ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coords);
+/* projs[b*NK + k] = <psi_R,b,k|psi_S,BAND_NUM,k> of the all-electron
+ * real-space wavefunctions on fftg: the grid sum times V/N^3
+ * (project_realspace_state, density.c:206-243), the contraction in the
+ * overlap precision (pawpy_gpu_set_precision). wf = S (its sites labels/
+ * coords), wf_R = R (labels_R/coords_R). */
+void project_realspace_state(pawpy_c128 *projs, int BAND_NUM, pswf_t *wf, pswf_t *wf_R,
+                             int *fftg, int *labels, double *coords, int *labels_R,
+                             double *coords_R);
+
 /* Replaces fft3d (linalg.c:14-45; called from C only). x[i*N2*N3 + j*N3 + k] =
  * V^-1/2 sum_w Cs[w] exp(2 pi i (g1 i/N1 + g2 j/N2 + g3 k/N3)). The transform
  * runs on the device in single precision (|error| well below the 1e-5 that
@@ -326,6 +356,12 @@ int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, i
                              int num_N_R, int num_N_S, int num_N_RS, int *M_R, int *M_S,
                              int *N_R, int *N_S, int *N_RS_R, int *N_RS_S, const double *w_v,
                              const double *w_c, int nch, int flip_spin);
+
+/* project_realspace_state for every band of wf at once: out[bS*(NB_R*NK) +
+ * bR*NK + k], one contraction per k-point. No counterpart in the reference.
+ * Returns 0, or the status. */
+int pawpy_gpu_project_realspace_all(pawpy_c128 *out, pswf_t *wf, pswf_t *wf_R, int *fftg, int *labels,
+                                    double *coords, int *labels_R, double *coords_R);
 
 /* WAVECAR reader producing a pswf_t with the reference's layout and VASP plane-
  * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf. */

@@ -12,7 +12,9 @@ that reproduces the reference's Python-level flow:
   other structure's sites, their projections, the N_RS pair matrices
   ``conj(reciprocal_offsite_wave_overlap)`` (radial.c:116-196);
 * ``pseudoprojection`` (pseudoprojector.c:63-90) and ``compensation_terms``
-  (projector.c:850-963) for every defect band, as full matrices.
+  (projector.c:850-963) for every defect band, as full matrices;
+* ``realspace_state`` and ``ae_chg_density`` (density.c:158-310): all-electron
+  states and charge densities on a real-space grid.
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 bench.py use this module; the product path never imports it.  The
@@ -155,6 +157,10 @@ class OSpecies:
                                self.sdw_spl, self.kgrid, self.kwave, self.kwave_spl,
                                self.aeov, self.psov, self.diov)
         self.wave_rmax = float(wg[-1])
+        # all-electron minus pseudo partial wave per channel (projector.c:95-99)
+        self.diffwave = [np.asarray(a, dtype=np.float64) - np.asarray(b, dtype=np.float64)
+                         for a, b in zip(pp.aewaves, pp.pswaves)]
+        self._ae_spl = {}
         # (n, l, m) of each lm channel, in the order of setup_site (utils.c:622-635)
         self.nlm = [(n, int(l), m) for n, l in enumerate(pp.ls) for m in range(-int(l), int(l) + 1)]
         D = (self.aeov - self.psov).reshape(npj, npj)
@@ -253,6 +259,7 @@ class OracleWavefunction:
             vr = vaspio.Vasprun(os.path.join(path, "vasprun.xml"))
             dim = [vr.parameters[n] for n in ("NGX", "NGY", "NGZ")]
             data = vaspio.read_wavecar_numpy(os.path.join(path, "WAVECAR"))
+            data = dict(data, weights=vr.actual_kpoints_weights)
         self.struct, self.cr = struct, cr
         self.dim = np.array(dim, np.int32)
         self.data = data
@@ -294,6 +301,133 @@ class OracleWavefunction:
     def site_block(self, P, s):
         o = self.site_off[s]
         return P[:, o: o + self.tables.total[s]]
+
+    # -- all-electron real-space states (density.c) ------------------------------------------
+
+    def _ae_spline(self, e, n):
+        """Cubic-spline coefficients of diffwave channel n of species e on the log wave grid
+        (diffwave_spline, projector.c:111-112)."""
+        sp = self.species[e]
+        if n not in sp._ae_spl:
+            x = sp.wave_grid
+            f = np.ascontiguousarray(sp.diffwave[n][: len(x)])
+            b, c, d = np.zeros(len(x)), np.zeros(len(x)), np.zeros(len(x))
+            lib().oracle_spline_coeff(x, f, len(x), b, c, d)
+            sp._ae_spl[n] = (f, b, c, d)
+        return sp._ae_spl[n]
+
+    def _site_geometry(self, p, N):
+        """Grid points of site p within its last wave-grid radius on the grid N (the box and test of
+        realspace_state, density.c:267-296): flattened cell, periodic-image shift, radial values
+        per channel (wave_interpolate / max(r, x0), utils.c:477-489, 522-531) and Y_lm per (l, m)
+        with the angles of wave_value2 (utils.c:533-543). Cached per grid."""
+        key = (p, tuple(int(v) for v in N))
+        cache = self.__dict__.setdefault("_geom", {})
+        if key in cache:
+            return cache[key]
+        lat = self.lattice
+        vol = abs(np.linalg.det(lat))
+        e = int(self.nums[p])
+        sp = self.species[e]
+        wg = sp.wave_grid
+        rmax = float(wg[-1])
+        c = self.coords[p]
+        box = [int(np.linalg.norm(np.cross(lat[(a + 1) % 3], lat[(a + 2) % 3])) * rmax / vol * N[a]) + 1
+               for a in range(3)]
+        # C round(): halves away from zero
+        ctr = [int(math.copysign(math.floor(abs(c[a] * N[a]) + 0.5), c[a] * N[a])) for a in range(3)]
+        ax = [np.arange(ctr[a] - box[a], ctr[a] + box[a] + 1) for a in range(3)]
+        I, J, K = np.meshgrid(ax[0], ax[1], ax[2], indexing="ij")
+        ijk = np.stack([I.ravel(), J.ravel(), K.ravel()], axis=1)
+        cart = (ijk / N - c) @ lat
+        r = np.sqrt((cart ** 2).sum(axis=1))
+        keep = r < rmax
+        ijk, cart, r = ijk[keep], cart[keep], r[keep]
+        wrapped = np.mod(ijk, N)
+        shift = (wrapped - ijk) // N
+        with np.errstate(invalid="ignore", divide="ignore"):
+            theta = np.arccos(np.clip(cart[:, 2] / np.where(r > 0, r, 1), -1, 1))
+            rxy = np.sqrt(cart[:, 0] ** 2 + cart[:, 1] ** 2)
+            phi = np.where(r - np.abs(cart[:, 2]) == 0, 0.0,
+                           np.arccos(np.clip(cart[:, 0] / np.where(rxy > 0, rxy, 1), -1, 1)))
+        phi = np.where(cart[:, 1] < 0, 2 * np.pi - phi, phi)
+        theta = np.where(r == 0, 0.0, theta)
+        phi = np.where(r == 0, 0.0, phi)
+        lg = math.log(wg[1] / wg[0])
+        ind = np.minimum((np.log(np.maximum(r, wg[0]) / wg[0]) / lg).astype(np.int64), len(wg) - 2)
+        rem = r - wg[ind]
+        rads, ys = {}, {}
+        for n, l, m in sp.nlm:
+            if n not in rads:
+                f, sb, sc, sd = self._ae_spline(e, n)
+                rad = np.where(r < wg[0], f[0], f[ind] + rem * (sb[ind] + rem * (sc[ind] + rem * sd[ind])))
+                rads[n] = rad / np.maximum(r, wg[0])
+            if (l, m) not in ys:
+                ys[(l, m)] = ylm_c(l, m, theta, phi)
+        flat = (wrapped[:, 0] * N[1] + wrapped[:, 1]) * N[2] + wrapped[:, 2]
+        cache[key] = (flat, shift, rads, ys)
+        return cache[key]
+
+    def realspace_state(self, b, kidx, fftg):
+        """realspace_state (density.c:245-310): the pseudo wavefunction of band b at k-point
+        index kidx on the grid fftg (fft3d, linalg.c:14-45) times exp(2 pi i k.r), plus for every
+        site the partial-wave differences (phi - phit)(r)/r Y_lm weighted by <p|psi> on the grid
+        points within the last wave-grid radius, with the Bloch phase of the periodic image.
+        Needs setup_projectors. complex128 [N1, N2, N3]."""
+        L = lib()
+        N = np.asarray(fftg, dtype=np.int32)
+        lat = self.lattice
+        vol = abs(np.linalg.det(lat))
+        gs = np.ascontiguousarray(self.data["gs"][kidx], dtype=np.int32)
+        cs = np.ascontiguousarray(self.data["coeffs"][kidx][b], dtype=np.complex64)
+        xv = np.zeros(2 * int(np.prod(N)))
+        L.oracle_fft3d(xv, gs.reshape(-1), cs.view(np.float32), gs.shape[0], N, vol)
+        x = (xv[0::2] + 1j * xv[1::2]).reshape(tuple(N))
+        kf = self.kpts[kidx % self.nwk]
+        fr = [np.arange(N[a]) / N[a] for a in range(3)]
+        kdotr = kf[0] * fr[0][:, None, None] + kf[1] * fr[1][None, :, None] + kf[2] * fr[2][None, None, :]
+        x = x * np.exp(2j * np.pi * kdotr)
+        P = self.P[kidx]
+        xf = x.reshape(-1)
+        for p in range(len(self.struct)):
+            e = int(self.nums[p])
+            sp = self.species[e]
+            flat, shift, rads, ys = self._site_geometry(p, N)
+            phase = np.exp(2j * np.pi * ((self.coords[p] + shift) @ kf))
+            acc = np.zeros(flat.shape[0], np.complex128)
+            o = self.site_off[p]
+            for q, (n, l, m) in enumerate(sp.nlm):
+                acc += rads[n] * ys[(l, m)] * P[b, o + q]
+            np.add.at(xf, flat, acc * phase)
+        return x
+
+    def ae_chg_density(self, fftg):
+        """ae_chg_density (density.c:158-178): sum over k-points and occupied bands of
+        |realspace_state|^2 x k-point weight x occupation x 2/nspin."""
+        N = tuple(int(v) for v in fftg)
+        rho = np.zeros(N)
+        occ = np.asarray(self.occs, dtype=np.float64).reshape(self.nk, self.nband)
+        w = np.asarray(self.data["weights"], dtype=np.float64)
+        for k in range(self.nk):
+            for b in range(self.nband):
+                if occ[k, b] > 0:
+                    x = self.realspace_state(b, k, fftg)
+                    rho += (x.real ** 2 + x.imag ** 2) * w[k % self.nwk] * occ[k, b] * (2 / self.nspin)
+        return rho
+
+
+def ylm_c(l, m, theta, phi):
+    """Complex Y_lm (Condon-Shortley) of arrays of angles through the C restatement of Ylm
+    (utils.c)."""
+    L = lib()
+    th = np.atleast_1d(np.asarray(theta, dtype=np.float64))
+    ph = np.atleast_1d(np.asarray(phi, dtype=np.float64))
+    out = np.zeros(th.shape, np.complex128)
+    re, im = C.c_double(), C.c_double()
+    for i in range(th.size):
+        L.oracle_ylm(int(l), int(m), float(th.flat[i]), float(ph.flat[i]), C.byref(re), C.byref(im))
+        out.flat[i] = complex(re.value, im.value)
+    return out
 
 
 def band_subset(data, idx):

@@ -67,6 +67,13 @@ def _declare(L):
     L.pawpy_gpu_band_character.argtypes = [_dp, _dp, _wfp, _wfp, C.c_int, C.c_int, C.c_int, C.c_int,
                                            _vp, _vp, _vp, _vp, _vp, _vp, _dp, _dp, C.c_int, C.c_int]
     L.fft3d.argtypes = [_zp, _vp, _dp, _dp, _ip, _vp, C.c_int, _ip]
+    L.realspace_state.argtypes = [_zp, C.c_int, C.c_int, _wfp, _ip, _ip, _dp]
+    L.remove_phase.argtypes = [_zp, C.c_int, _wfp, _ip]
+    L.ae_state_density.argtypes = [_dp, C.c_int, C.c_int, _wfp, _ip, _ip, _dp]
+    L.ae_chg_density.argtypes = [_dp, _wfp, _ip, _ip, _dp]
+    L.project_realspace_state.argtypes = [_zp, C.c_int, _wfp, _wfp, _ip, _ip, _dp, _ip, _dp]
+    L.pawpy_gpu_project_realspace_all.restype = C.c_int
+    L.pawpy_gpu_project_realspace_all.argtypes = [_zp, _wfp, _wfp, _ip, _ip, _dp, _ip, _dp]
     L.onto_projector.argtypes = [C.POINTER(S.kpoint_t), C.c_int, C.POINTER(S.real_proj_site_t), C.c_int,
                                  _vp, _dp, _dp, C.c_int, _ip]
     L.pawpy_gpu_set_precision.argtypes = [C.c_int]

@@ -36,6 +36,11 @@ using cd = std::complex<double>;
 struct SpeciesTables {
   DevBuf<double> proj_f, proj_spl, smooth_f, smooth_spl;
   SpeciesDev proj{}, smooth{};
+  // (phi - phit) on the logarithmic partial-wave grid, for the all-electron real-space
+  // wavefunctions; ae_rmax = the grid's last point (the radius of those spheres)
+  DevBuf<double> ae_x, ae_f, ae_spl;
+  AeSpeciesDev ae{};
+  double ae_rmax = 0;
   int total = 0, nproj = 0;
   std::vector<int> lm_n, lm_l, lm_m;
   std::vector<double> D;  // total x total: (aeov - psov)[n_i][n_j] where (l,m) agree
@@ -55,6 +60,24 @@ struct SphereSet {
   DevBuf<SpeciesDev> species;
 };
 
+// Sphere tables of the all-electron real-space wavefunctions of one wavefunction on
+// one grid (realspace.cu): per site the points within its partial-wave grid's last
+// radius, (phi - phit)/r Y_lm there, exp(2 pi i k.(R + T)) per k-point, and the points
+// grouped per grid cell for the deterministic spread.
+struct AeTables {
+  int N[3] = {0, 0, 0};
+  std::vector<int> labels;
+  std::vector<double> coords;
+  long long npts = 0;
+  DevBuf<int> cell;
+  DevBuf<float2> val, phase;
+  DevBuf<int> ucell, ent_first, ent_site, site_npts, site_total, site_pcol;
+  DevBuf<long long> ent_pt, site_pt, site_val;
+  AeSpread view;
+  Radices r[3];
+  DevBuf<float2> tw[3];
+};
+
 struct DevKpt {
   int W = 0, Wpad = 0, g1min = 0, n1 = 0;
   int g2min = 0, n2 = 0, g3min = 0, n3 = 0;  // occupied ranges of the other two axes
@@ -64,6 +87,7 @@ struct DevKpt {
   std::vector<int> gsorted;  // [W][3] in sorted order
   DevBuf<int> perm_d, plane_start, plane_off;
   DevBuf<int> inv_d;  // invperm on the device (host-read upload)
+  DevBuf<int> gs_d;   // gsorted on the device (real-space wavefunctions)
   int off_N2 = 0, off_N3 = 0;
   size_t c_off = 0;
   double kfrac[3] = {0, 0, 0};
@@ -109,6 +133,7 @@ struct DevWF {
   bool p_ready = false;       // P holds <p|psi> of every band
   Radices r[3];
   DevBuf<float2> tw[3];
+  std::unique_ptr<AeTables> ae;  // real-space all-electron tables (last grid asked for)
   DevWF() = default;
   DevWF(const DevWF &) = delete;
   DevWF &operator=(const DevWF &) = delete;
@@ -576,6 +601,40 @@ static std::unique_ptr<SpeciesTables> species_tables(const ppot_t &pp) {
       }
       s.lm_coef[i] = c;
     }
+  }
+  {
+    const int ng = pp.wave_gridsize;
+    PAWPY_REQUIRE(ng >= 2 && pp.wave_grid[0] > 0, "partial-wave grid needs two positive points");
+    std::vector<double> af((size_t)np * ng), as((size_t)np * 3 * ng);
+    for (int k = 0; k < np; k++) {
+      const funcset_t &f = pp.funcs[k];
+      PAWPY_REQUIRE(f.diffwave && f.diffwave_spline, "element without (phi - phit) splines");
+      for (int j = 0; j < ng; j++) {
+        af[(size_t)k * ng + j] = f.diffwave[j];
+        for (int c = 0; c < 3; c++) as[((size_t)k * 3 + c) * ng + j] = f.diffwave_spline[c][j];
+      }
+    }
+    t->ae_x.alloc(ng);
+    t->ae_x.upload(pp.wave_grid, ng);
+    t->ae_f.alloc(af.size());
+    t->ae_f.upload(af.data(), af.size());
+    t->ae_spl.alloc(as.size());
+    t->ae_spl.upload(as.data(), as.size());
+    AeSpeciesDev &a = t->ae;
+    a.x = t->ae_x.p;
+    a.f = t->ae_f.p;
+    a.spl = t->ae_spl.p;
+    a.size = ng;
+    a.nfunc = np;
+    a.total = t->total;
+    a.logstep = std::log(pp.wave_grid[1] / pp.wave_grid[0]);
+    for (int i = 0; i < t->total; i++) {
+      a.lm_l[i] = t->proj.lm_l[i];
+      a.lm_m[i] = t->proj.lm_m[i];
+      a.lm_f[i] = t->proj.lm_f[i];
+      a.lm_coef[i] = t->proj.lm_coef[i];
+    }
+    t->ae_rmax = pp.wave_grid[ng - 1];
   }
   t->D.assign((size_t)t->total * t->total, 0.0);
   for (int i = 0; i < t->total; i++)
@@ -1524,6 +1583,199 @@ static void do_overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, const int *labels
   if (g_host_proj) sync();
 }
 
+
+// ============================================================= all-electron real-space wavefunctions
+
+// The real-space sphere tables of d's sites on grid N (built once per grid and site list).
+static AeTables &ae_tables(DevWF &d, const int *N, const int *labels, const double *coords) {
+  PAWPY_REQUIRE(d.tables_ready, "real-space wavefunctions need setup_projections first");
+  PAWPY_REQUIRE(!d.ncl, "real-space wavefunctions of noncollinear wavefunctions are not part of this library");
+  const int ns = (int)d.labels.size();
+  std::vector<int> lab(labels, labels + ns);
+  std::vector<double> crd(coords, coords + 3 * (size_t)ns);
+  if (d.ae && d.ae->N[0] == N[0] && d.ae->N[1] == N[1] && d.ae->N[2] == N[2] && d.ae->labels == lab &&
+      d.ae->coords == crd)
+    return *d.ae;
+  HostPhase hp("ae_tables");
+  auto t = std::make_unique<AeTables>();
+  for (int a = 0; a < 3; a++) {
+    PAWPY_REQUIRE(N[a] >= 1 && N[a] <= 4096, "bad FFT grid");
+    t->N[a] = N[a];
+    t->r[a] = make_radices(N[a]);
+    PAWPY_REQUIRE(t->r[a].ns >= 0, "FFT grid dimensions must factor into primes <= 13");
+    twiddles(N[a], t->tw[a]);
+  }
+  PAWPY_REQUIRE(3 * (size_t)std::max({N[0], N[1], N[2]}) * sizeof(float2) <= 227 * 1024,
+                "real-space grid lines do not fit in shared memory");
+  t->labels = lab;
+  t->coords = crd;
+  const double *lat = d.lattice;
+  auto cross = [](const double *a, const double *b, double *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  double c23[3], c13[3], c12[3];
+  cross(lat + 3, lat + 6, c23);
+  cross(lat + 0, lat + 6, c13);
+  cross(lat + 0, lat + 3, c12);
+  // boxes and cutoffs of realspace_state (density.c:269-287): half box (|a_j x a_k| rmax / V) N + 1
+  // around round(coord N), rmax the last point of the element's partial-wave grid
+  std::vector<SiteDesc> host(ns);
+  std::vector<int2> slabs;
+  std::vector<AeSpeciesDev> sd;
+  for (auto &sp : d.species) sd.push_back(sp->ae);
+  for (int s = 0; s < ns; s++) {
+    const int e = lab[s];
+    PAWPY_REQUIRE(e >= 0 && e < (int)d.species.size(), "site label out of range");
+    const double rmax = d.species[e]->ae_rmax;
+    SiteDesc &h = host[s];
+    for (int a = 0; a < 3; a++) h.coord[a] = crd[3 * s + a];
+    h.species = e;
+    h.g[0] = (int)(vnorm(c23) * rmax / d.vol * N[0]) + 1;
+    h.g[1] = (int)(vnorm(c13) * rmax / d.vol * N[1]) + 1;
+    h.g[2] = (int)(vnorm(c12) * rmax / d.vol * N[2]) + 1;
+    for (int a = 0; a < 3; a++) h.c[a] = (int)std::round(crd[3 * s + a] * N[a]);
+    h.R0 = rmax;
+    h.total = d.species[e]->total;
+    h.lm_off = d.site_lmoff[s];
+    for (int jb = 0; jb <= 2 * h.g[1]; jb++) slabs.push_back(make_int2(s, jb));
+  }
+  DevBuf<double> Ld(9);
+  Ld.upload(lat, 9);
+  DevBuf<int> Nd(3);
+  Nd.upload(N, 3);
+  DevBuf<SiteDesc> sites(std::max(1, ns));
+  sites.upload(host.data(), ns);
+  DevBuf<int2> slabs_d(std::max<size_t>(1, slabs.size()));
+  slabs_d.upload(slabs.data(), slabs.size());
+  DevBuf<int> counts(std::max<size_t>(1, slabs.size()));
+  launch_ae_count(sites.p, slabs_d.p, (int)slabs.size(), Ld.p, Nd.p, counts.p);
+  std::vector<int> hc(slabs.size());
+  counts.download(hc.data(), hc.size());
+  sync();
+  std::vector<long long> site_pt(ns, 0), site_val(ns, 0);
+  std::vector<int> site_npts(ns, 0), site_total(ns), site_pcol(ns);
+  for (size_t q = 0; q < slabs.size(); q++) site_npts[slabs[q].x] += hc[q];
+  long long pt = 0, val = 0;
+  for (int s = 0; s < ns; s++) {
+    site_pt[s] = pt;
+    site_val[s] = val;
+    site_total[s] = host[s].total;
+    site_pcol[s] = host[s].lm_off;
+    pt += site_npts[s];
+    val += (long long)site_npts[s] * host[s].total;
+  }
+  std::vector<SegFill> segs;
+  pt = 0;
+  for (size_t q = 0; q < slabs.size(); q++) {
+    if (hc[q] == 0) continue;
+    SegFill f;
+    f.site = slabs[q].x;
+    f.jb = slabs[q].y;
+    f.pt_off = pt;
+    f.npts = hc[q];
+    f.site_pt = site_pt[f.site];
+    f.site_npts = site_npts[f.site];
+    f.site_val = site_val[f.site];
+    segs.push_back(f);
+    pt += hc[q];
+  }
+  t->npts = pt;
+  std::vector<double> kf(3 * (size_t)d.nk);
+  for (int k = 0; k < d.nk; k++)
+    for (int a = 0; a < 3; a++) kf[3 * k + a] = d.kp[k].kfrac[a];
+  DevBuf<double> kfd(kf.size());
+  kfd.upload(kf.data(), kf.size());
+  DevBuf<AeSpeciesDev> spd(sd.size());
+  spd.upload(sd.data(), sd.size());
+  DevBuf<SegFill> segs_d(std::max<size_t>(1, segs.size()));
+  segs_d.upload(segs.data(), segs.size());
+  t->cell.alloc(std::max(1LL, pt));
+  t->val.alloc(std::max(1LL, val));
+  t->phase.alloc(std::max(1LL, pt * d.nk));
+  launch_ae_fill(sites.p, segs_d.p, (int)segs.size(), spd.p, Ld.p, Nd.p, kfd.p, d.nk, pt, t->cell.p, t->val.p,
+                 t->phase.p);
+  // the points of every cell, sites in order (segments are site-major)
+  std::vector<int> cell(std::max(1LL, pt));
+  t->cell.download(cell.data(), pt);
+  sync();
+  std::vector<int> site_of(std::max(1LL, pt));
+  for (const SegFill &f : segs)
+    for (int q = 0; q < f.npts; q++) site_of[f.pt_off + q] = f.site;
+  std::vector<long long> ord(pt);
+  std::iota(ord.begin(), ord.end(), 0LL);
+  std::stable_sort(ord.begin(), ord.end(), [&](long long a, long long b) { return cell[a] < cell[b]; });
+  std::vector<int> ucell, ent_first(1, 0), ent_site;
+  std::vector<long long> ent_pt;
+  for (size_t e = 0; e < ord.size(); e++) {
+    const long long o = ord[e];
+    if (e > 0 && cell[o] != cell[ord[e - 1]]) ent_first.push_back((int)e);
+    if (e == 0 || cell[o] != cell[ord[e - 1]]) ucell.push_back(cell[o]);
+    ent_pt.push_back(o);
+    ent_site.push_back(site_of[o]);
+  }
+  if (pt > 0) ent_first.push_back((int)pt);
+  auto up_i = [](DevBuf<int> &b, const std::vector<int> &h) {
+    b.alloc(std::max<size_t>(1, h.size()));
+    b.upload(h.data(), h.size());
+  };
+  auto up_l = [](DevBuf<long long> &b, const std::vector<long long> &h) {
+    b.alloc(std::max<size_t>(1, h.size()));
+    b.upload(h.data(), h.size());
+  };
+  up_i(t->ucell, ucell);
+  up_i(t->ent_first, ent_first);
+  up_i(t->ent_site, ent_site);
+  up_l(t->ent_pt, ent_pt);
+  up_l(t->site_pt, site_pt);
+  up_l(t->site_val, site_val);
+  up_i(t->site_npts, site_npts);
+  up_i(t->site_total, site_total);
+  up_i(t->site_pcol, site_pcol);
+  AeSpread &v = t->view;
+  v.ncell = (int)ucell.size();
+  v.ucell = t->ucell.p;
+  v.ent_first = t->ent_first.p;
+  v.ent_site = t->ent_site.p;
+  v.ent_pt = t->ent_pt.p;
+  v.site_pt = t->site_pt.p;
+  v.site_val = t->site_val.p;
+  v.site_npts = t->site_npts.p;
+  v.site_total = t->site_total.p;
+  v.site_pcol = t->site_pcol.p;
+  v.val = t->val.p;
+  v.phase = t->phase.p;
+  v.npts = pt;
+  d.ae = std::move(t);
+  return *d.ae;
+}
+
+// All-electron real-space wavefunctions of bands [b0, b0 + nb) of k-point kq on the grid of t:
+// grid[b][N1][N2][N3] (realspace_state, density.c:245-310).
+static void ae_grids(DevWF &d, AeTables &t, int kq, int b0, int nb, float2 *grid) {
+  ensure_projections(d);
+  DevKpt &q = d.kp[kq];
+  const float2 *C = coeffs(d, kq);
+  if (!q.gs_d.p) {
+    q.gs_d.alloc(std::max<size_t>(3, q.gsorted.size()));
+    q.gs_d.upload(q.gsorted.data(), q.gsorted.size());
+  }
+  const int *N = t.N;
+  const long long n3d = (long long)N[0] * N[1] * N[2];
+  launch_scatter_bands(C + (size_t)b0 * q.Wpad, q.Wpad, q.gs_d.p, q.W, N[0], N[1], N[2], grid, nb);
+  for (int a = 2; a >= 0; a--) launch_fft_axis(grid, nb, N[0], N[1], N[2], a, t.r[a], t.tw[a].p);
+  launch_bloch(grid, N[0], N[1], N[2], q.kfrac, std::pow(d.vol, -0.5), nb);
+  const int Pt = d.proj.Ptot;
+  launch_ae_add(t.view, d.P.p + ((size_t)kq * d.nband + b0) * Pt, Pt, kq, grid, n3d, nb);
+}
+
+// Bands per batch of real-space grids (about 1 GiB of grids).
+static int ae_batch(const AeTables &t) {
+  const long long n3d = (long long)t.N[0] * t.N[1] * t.N[2];
+  return (int)std::max(1LL, (1LL << 30) / (n3d * (long long)sizeof(float2)));
+}
+
 // ============================================================= overlap matrices
 
 static int flip_k(const DevWF &R, int k, int flip) {
@@ -2089,6 +2341,199 @@ int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, i
   dv.download(v, dv.n);
   dc.download(c, dc.n);
   sync();
+  return 0;
+  PAWPY_API_END(pawpy_gpu_last_error())
+}
+
+}  // extern "C"
+
+// out[n][m] = sum_k conj(A[m][k]) B[n][k] over K (a multiple of 16), in the overlap precision.
+static void grid_overlaps(const float2 *A, int M, const float2 *B, int N, long long K, float2 *out) {
+  PAWPY_REQUIRE(K % 16 == 0 && K < (1LL << 31), "grid contraction length");
+  std::vector<GemmBatch> hb(1);
+  GemmBatch &g = hb[0];
+  g.A1 = A;
+  g.B1 = B;
+  g.lda1 = g.ldb1 = K;
+  g.K1 = (int)K;
+  g.A2 = g.B2 = nullptr;
+  g.lda2 = g.ldb2 = 0;
+  g.K2 = 0;
+  g.out = out;
+  DevBuf<GemmBatch> db(1);
+  db.upload(hb.data(), 1);
+  const int prec = g_precision.load();
+  if (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32) {
+    launch_zgemm_tc(db.p, hb, M, N, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+    return;
+  }
+  int splits = choose_splits(M, N, 1, (int)K);
+  DevBuf<float2> ws;
+  if (splits > 1) ws.alloc((size_t)splits * M * N);
+  launch_zgemm_f32(db.p, 1, M, N, splits, ws.p);
+}
+
+// Real-space grids of bands [b0, b0 + nb) at k-point kq, rows of ld >= n3d values (zero past n3d).
+static void ae_grid_rows(DevWF &d, AeTables &t, int kq, int b0, int nb, float2 *rows, long long ld) {
+  const long long n3d = (long long)t.N[0] * t.N[1] * t.N[2];
+  if (ld == n3d) {
+    ae_grids(d, t, kq, b0, nb, rows);
+    return;
+  }
+  DevBuf<float2> tmp((size_t)nb * n3d);
+  ae_grids(d, t, kq, b0, nb, tmp.p);
+  PAWPY_CUDA(cudaMemsetAsync(rows, 0, sizeof(float2) * (size_t)nb * ld, stream()));
+  PAWPY_CUDA(cudaMemcpy2DAsync(rows, sizeof(float2) * ld, tmp.p, sizeof(float2) * n3d, sizeof(float2) * n3d, nb,
+                               cudaMemcpyDeviceToDevice, stream()));
+}
+
+// <psi_R,bR,k|psi_S,bS,k> of the all-electron real-space wavefunctions on grid fftg for the
+// defect bands [s0, s0 + ns): out[(bS - s0)][bR * nk + k] (project_realspace_state,
+// density.c:206-243: the grid sum times V / N^3).
+static void realspace_overlaps(pswf_t *wf_S, pswf_t *wf_R, const int *fftg, const int *labels, const double *coords,
+                               const int *labels_R, const double *coords_R, int s0, int ns, pawpy_c128 *out) {
+  DevWF &S = mirror(wf_S);
+  DevWF &R = mirror(wf_R);
+  PAWPY_REQUIRE(S.nk == R.nk, "basis and defect differ in k-points");
+  PAWPY_REQUIRE(s0 >= 0 && ns >= 1 && s0 + ns <= S.nband, "band index out of range");
+  AeTables &tS = ae_tables(S, fftg, labels, coords);
+  AeTables &tR = ae_tables(R, fftg, labels_R, coords_R);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2], ld = (n3d + 15) / 16 * 16;
+  const int nk = S.nk, nbR = R.nband;
+  const double scale = S.vol / (double)n3d;
+  DevBuf<float2> gS((size_t)ns * ld), gR((size_t)nbR * ld), o((size_t)ns * nbR);
+  std::vector<float2> h((size_t)ns * nbR);
+  for (int k = 0; k < nk; k++) {
+    ae_grid_rows(S, tS, k, s0, ns, gS.p, ld);
+    const int bb = ae_batch(tR);
+    for (int b0 = 0; b0 < nbR; b0 += bb)
+      ae_grid_rows(R, tR, k, b0, std::min(bb, nbR - b0), gR.p + (size_t)b0 * ld, ld);
+    grid_overlaps(gR.p, nbR, gS.p, ns, ld, o.p);
+    o.download(h.data(), h.size());
+    sync();
+    for (int b = 0; b < ns; b++)
+      for (int r = 0; r < nbR; r++) {
+        const float2 v = h[(size_t)b * nbR + r];
+        out[(size_t)b * nbR * nk + (size_t)r * nk + k] = pawpy_c128(v.x * scale, v.y * scale);
+      }
+  }
+}
+
+extern "C" {
+
+void realspace_state(pawpy_c128 *x, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg, int *labels,
+                     double *coords) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("realspace_state");
+  PAWPY_REQUIRE(x && wf && fftg && labels && coords, "realspace_state: NULL argument");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < d.nband && KPOINT_NUM >= 0 && KPOINT_NUM < d.nk,
+                "realspace_state: band or k-point index out of range");
+  AeTables &t = ae_tables(d, fftg, labels, coords);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  DevBuf<float2> g(n3d);
+  ae_grids(d, t, KPOINT_NUM, BAND_NUM, 1, g.p);
+  DevBuf<double2> o(n3d);
+  launch_scale_to_c128(g.p, n3d, 1.0, o.p);
+  o.download(reinterpret_cast<double2 *>(x), n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+void remove_phase(pawpy_c128 *x, int KPOINT_NUM, pswf_t *wf, int *fftg) {
+  PAWPY_API_BEGIN
+  PAWPY_REQUIRE(x && wf && fftg, "remove_phase: NULL argument");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(KPOINT_NUM >= 0 && KPOINT_NUM < d.nk, "remove_phase: k-point index out of range");
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  DevBuf<double2> g(n3d);
+  g.upload(reinterpret_cast<const double2 *>(x), n3d);
+  launch_remove_phase(g.p, fftg[0], fftg[1], fftg[2], d.kp[KPOINT_NUM].kfrac);
+  g.download(reinterpret_cast<double2 *>(x), n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+void ae_state_density(double *P, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg, int *labels,
+                      double *coords) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("ae_state_density");
+  PAWPY_REQUIRE(P && wf && fftg && labels && coords, "ae_state_density: NULL argument");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < d.nband && KPOINT_NUM >= 0 && KPOINT_NUM < d.nk,
+                "ae_state_density: band or k-point index out of range");
+  AeTables &t = ae_tables(d, fftg, labels, coords);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  DevBuf<float2> g(n3d);
+  ae_grids(d, t, KPOINT_NUM, BAND_NUM, 1, g.p);
+  DevBuf<double> rho(n3d), w(1);
+  const double one = 1.0;
+  w.upload(&one, 1);
+  rho.upload(P, n3d);
+  launch_density(g.p, w.p, 1, n3d, rho.p);
+  rho.download(P, n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+void ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coords) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("ae_chg_density");
+  PAWPY_REQUIRE(P && wf && fftg && labels && coords, "ae_chg_density: NULL argument");
+  DevWF &d = mirror(wf);
+  AeTables &t = ae_tables(d, fftg, labels, coords);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  const int bb = ae_batch(t);
+  DevBuf<float2> g((size_t)std::min(bb, d.nband) * n3d);
+  DevBuf<double> rho(n3d), w((size_t)d.nband);
+  rho.upload(P, n3d);
+  // occupied bands of every k-point, weight x occupation x 2 / nspin (density.c:158-178)
+  const double spin_mult = 2.0 / d.nspin;
+  for (int k = 0; k < d.nk; k++) {
+    std::vector<int> occ;
+    std::vector<double> wk;
+    for (int b = 0; b < d.nband; b++) {
+      const band_t *bd = wf->kpts[k]->bands[b];
+      if (bd->occ > 0) {
+        occ.push_back(b);
+        wk.push_back(wf->kpts[k]->weight * bd->occ * spin_mult);
+      }
+    }
+    // runs of consecutive occupied bands in batches
+    size_t i = 0;
+    while (i < occ.size()) {
+      size_t j = i + 1;
+      while (j < occ.size() && occ[j] == occ[j - 1] + 1 && (int)(j - i) < bb) j++;
+      const int nb = (int)(j - i);
+      ae_grids(d, t, k, occ[i], nb, g.p);
+      w.upload(wk.data() + i, nb);
+      launch_density(g.p, w.p, nb, n3d, rho.p);
+      i = j;
+    }
+  }
+  rho.download(P, n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+void project_realspace_state(pawpy_c128 *projs, int BAND_NUM, pswf_t *wf, pswf_t *wf_R, int *fftg, int *labels,
+                             double *coords, int *labels_R, double *coords_R) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("project_realspace_state");
+  PAWPY_REQUIRE(projs && wf && wf_R && fftg && labels && coords && labels_R && coords_R,
+                "project_realspace_state: NULL argument");
+  realspace_overlaps(wf, wf_R, fftg, labels, coords, labels_R, coords_R, BAND_NUM, 1, projs);
+  PAWPY_API_END()
+}
+
+int pawpy_gpu_project_realspace_all(pawpy_c128 *out, pswf_t *wf, pswf_t *wf_R, int *fftg, int *labels,
+                                    double *coords, int *labels_R, double *coords_R) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("pawpy_gpu_project_realspace_all");
+  PAWPY_REQUIRE(out && wf && wf_R && fftg && labels && coords && labels_R && coords_R,
+                "pawpy_gpu_project_realspace_all: NULL argument");
+  DevWF &S = mirror(wf);
+  realspace_overlaps(wf, wf_R, fftg, labels, coords, labels_R, coords_R, 0, S.nband, out);
   return 0;
   PAWPY_API_END(pawpy_gpu_last_error())
 }

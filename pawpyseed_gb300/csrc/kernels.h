@@ -208,6 +208,45 @@ void launch_recip_planes_pick(const float2 *H, const PlaneGeom &g, const int *ps
                               const Radices &r2, const Radices &r3, const float2 *tw2, const float2 *tw3,
                               const float2 *C, int Wpad, float2 *CA, float2 *D, int nb);
 
+// ---- all-electron real-space wavefunctions (realspace.cu) ----
+struct AeSpeciesDev {    // (phi - phit)(r) of one element on its logarithmic grid, device pointers
+  const double *x;       // [size] the grid
+  const double *f;       // [nfunc][size]
+  const double *spl;     // [nfunc][3][size] spline b, c, d
+  int size, nfunc, total;
+  double logstep;        // log(x[1] / x[0])
+  int lm_l[32], lm_m[32], lm_f[32];
+  double lm_coef[32];    // as SpeciesDev
+};
+// The sphere points of a wavefunction's sites grouped per grid cell: cells ucell[u] (global
+// (i N2 + j) N3 + k), each summing entries [ent_first[u], ent_first[u+1]) in site order.
+struct AeSpread {
+  int ncell = 0;
+  const int *ucell = nullptr, *ent_first = nullptr, *ent_site = nullptr;
+  const long long *ent_pt = nullptr;
+  const long long *site_pt = nullptr, *site_val = nullptr;
+  const int *site_npts = nullptr, *site_total = nullptr, *site_pcol = nullptr;
+  const float2 *val = nullptr;    // [total][site points] per site: (phi - phit)/r Y_lm
+  const float2 *phase = nullptr;  // [nkp][npts] exp(2 pi i k.(R + T))
+  long long npts = 0;
+};
+void launch_ae_count(const SiteDesc *sites, const int2 *slabs, int nslabs, const double *lattice, const int *fftg,
+                     int *counts);
+void launch_ae_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const AeSpeciesDev *species,
+                    const double *lattice, const int *fftg, const double *kfrac, int nkp, long long npts, int *cell,
+                    float2 *val, float2 *phase);
+// nb zeroed grids [b][N1][N2][N3] with C[b][t] at the wrapped plane-wave indices gsorted[3t..3t+2]
+void launch_scatter_bands(const float2 *C, int Wpad, const int *gsorted, int W, int N1, int N2, int N3,
+                          float2 *grid, int nb);
+// every grid point times scale exp(2 pi i k.(i/N1, j/N2, k/N3))
+void launch_bloch(float2 *grid, int N1, int N2, int N3, const double *kfrac, double scale, int nb);
+// the sphere terms of every band's projector coefficients (rows P[b][Pstride], k-point kq) added per cell
+void launch_ae_add(const AeSpread &c, const float2 *P, int Pstride, int kq, float2 *grid, long long n3d, int nb);
+// rho[i] += sum_b w[b] |grid[b][i]|^2 (double precision)
+void launch_density(const float2 *grid, const double *w, int nb, long long n3d, double *rho);
+// x[i] *= exp(-2 pi i k.r_frac) on a host-layout double grid
+void launch_remove_phase(double2 *x, int N1, int N2, int N3, const double *kfrac);
+
 // ---- augmentation columns of the PAW terms ----
 // A[kslice][b][c] = src[c] < Pt ? P[kslice][b][src[c]] : WP[kslice][b][src[c]-Pt]; zero for c >= Kc
 void launch_aug_a(const float2 *P, int Pt, const float2 *WP, int Pw, int nb, int nk, const int *src, int Kc,

@@ -1,8 +1,8 @@
 """``Projector``: PAW band projections of a defect wavefunction onto a basis.
 
 Mirrors ``pawpyseed.core.projector.Projector`` (projector.py:10-503) and its
-Cython base ``CProjector`` (pawpyc.pyx:628-721) for the ``aug_real``,
-``aug_recip`` and ``pseudo`` methods: site classification (``make_site_lists``), the overlap
+Cython base ``CProjector`` (pawpyc.pyx:628-737) for the ``aug_real``,
+``aug_recip``, ``realspace`` and ``pseudo`` methods: site classification (``make_site_lists``), the overlap
 setup, ``single_band_projection``, ``proportion_conduction`` and
 ``defect_band_analysis``. ``project_all`` adds the batched form: every defect
 band against every basis band in one device contraction.
@@ -28,9 +28,6 @@ class Projector:
         self.method = method
         if method not in self.METHODS:
             raise PAWpyError("method not recognized for Projector")
-        if method == "realspace":
-            raise PAWpyError("method %r is not part of this library's projection path; "
-                             "use 'aug_real' (the reference default), 'aug_recip' or 'pseudo'" % method)
         if (wf.ncl or basis.ncl) and not (noncollinear and wf.ncl and basis.ncl):
             raise PAWpyError("Projection not supported for noncollinear case!")
         if unsym_basis or unsym_wf:
@@ -47,6 +44,7 @@ class Projector:
         if self.method != "pseudo":
             basis.check_c_projectors()
             wf.check_c_projectors()
+        if "aug" in self.method:
             self.setup_overlap()
 
     # -- site classification ----------------------------------------------
@@ -131,7 +129,21 @@ class Projector:
             return self._single_band_projection_pseudo(band_num, flip_spin)
         if self.method == "aug_recip":
             return self._single_band_projection_aug_recip(band_num, flip_spin)
+        if self.method == "realspace":
+            return self._single_band_projection_realspace(band_num)
         return self._single_band_projection_aug_real(band_num, flip_spin)
+
+    def _single_band_projection_realspace(self, band_num, dim=None):
+        """All-electron projection with both wavefunctions evaluated on a real-space grid
+        (projector.py:199-208 with project_realspace_state, density.c:206-243), by default twice
+        the defect's FFT grid. (The reference's Cython layer compares that grid with None and
+        fails; the grid is passed here as three integers.)"""
+        g = np.ascontiguousarray(self.wf.dim * 2 if dim is None else dim, dtype=np.int32)
+        res = np.zeros(self.basis.nband * self.basis.nwk * self.basis.nspin, dtype=np.complex128)
+        _lib.lib().project_realspace_state(res, int(band_num), self.wf.wf_ptr, self.basis.wf_ptr, g, self.wf.nums,
+                                           self.wf.coords, self.basis.nums, self.basis.coords)
+        _lib.check()
+        return res
 
     def _single_band_projection_aug_recip(self, band_num, flip_spin=False):
         """All-electron projection with the augmentation evaluated in reciprocal space
@@ -153,6 +165,14 @@ class Projector:
         if self.method == "pseudo":
             return np.array([self.single_band_projection(b, flip_spin) for b in range(self.wf.nband)])
         nk = self.basis.nwk * self.basis.nspin
+        if self.method == "realspace":
+            out = np.zeros((self.wf.nband, self.basis.nband * nk), dtype=np.complex128)
+            g = np.ascontiguousarray(self.wf.dim * 2, dtype=np.int32)
+            _lib.lib().pawpy_gpu_project_realspace_all(out.reshape(-1), self.wf.wf_ptr, self.basis.wf_ptr, g,
+                                                       self.wf.nums, self.wf.coords, self.basis.nums,
+                                                       self.basis.coords)
+            _lib.check()
+            return out
         out = np.zeros((self.wf.nband, self.basis.nband * nk), dtype=np.complex128)
         L = _lib.lib()
         L.pawpy_gpu_project_all(out.reshape(-1), self.basis.wf_ptr, self.wf.wf_ptr, len(self.M_R),

@@ -237,6 +237,118 @@ class Wavefunction:
             self._make_c_projectors()
             Timer.setup_time(time.monotonic() - start)
 
+    # -- all-electron real-space wavefunctions (wavefunction.py:431-590, pawpyc.pyx:425-523) --------
+    #
+    # The grid is given explicitly (dim); the reference sets it through update_dim, which also
+    # changes the wavefunction's own grid. States default to the wavefunction's grid, densities
+    # to the doubled grid, as there.
+
+    def _grid(self, dim, fine):
+        g = self.dim * (2 if fine else 1) if dim is None else np.asarray(dim)
+        return np.ascontiguousarray(g, dtype=np.int32)
+
+    def _check_bks(self, b, k, s):
+        if b < 0 or b >= self.nband:
+            raise ValueError("Invalid band choice")
+        if k < 0 or k >= self.nwk:
+            raise ValueError("Invalid k-point choice")
+        if s < 0 or s >= self.nspin:
+            raise ValueError("Invalid spin choice")
+
+    def get_state_realspace(self, b, k, s, dim=None, remove_phase=False):
+        """All-electron wavefunction of band b, k-point k, spin s on the grid dim (default the
+        wavefunction's own): complex128 [N1, N2, N3] (realspace_state, density.c:245-310). With
+        remove_phase the exp(2 pi i k.r) factor is divided out."""
+        self.check_c_projectors()
+        self._check_bks(b, k, s)
+        g = self._grid(dim, False)
+        res = np.zeros(int(np.prod(g)), dtype=np.complex128)
+        L = _lib.lib()
+        L.realspace_state(res, int(b), int(k + s * self.nwk), self._ptr, g, self.nums, self.coords)
+        _lib.check()
+        if remove_phase:
+            L.remove_phase(res, int(k + s * self.nwk), self._ptr, g)
+            _lib.check()
+        return res.reshape(tuple(g))
+
+    def get_state_realspace_density(self, b, k, s, dim=None):
+        """|psi|^2 of one band on the grid dim (default twice the wavefunction's grid)
+        (ae_state_density, density.c:27-37)."""
+        self.check_c_projectors()
+        self._check_bks(b, k, s)
+        g = self._grid(dim, True)
+        res = np.zeros(int(np.prod(g)), dtype=np.float64)
+        _lib.lib().ae_state_density(res, int(b), int(k + s * self.nwk), self._ptr, g, self.nums, self.coords)
+        _lib.check()
+        return res.reshape(tuple(g))
+
+    def get_realspace_density(self, dim=None, bands=None):
+        """All-electron charge density on the grid dim (default twice the wavefunction's grid):
+        every occupied band (ae_chg_density, density.c:158-178), or with bands (an int or a list)
+        those bands weighted by k-point weight / nspin (pawpyc.pyx:455-494)."""
+        self.check_c_projectors()
+        g = self._grid(dim, True)
+        n = int(np.prod(g))
+        L = _lib.lib()
+        res = np.zeros(n, dtype=np.float64)
+        if bands is None:
+            L.ae_chg_density(res, self._ptr, g, self.nums, self.coords)
+            _lib.check()
+        else:
+            for b in ([bands] if isinstance(bands, (int, np.integer)) else list(bands)):
+                if b < 0 or b >= self.nband:
+                    raise ValueError("Invalid band choice")
+                for k in range(self.nwk * self.nspin):
+                    work = np.zeros(n, dtype=np.float64)
+                    L.ae_state_density(work, int(b), int(k), self._ptr, g, self.nums, self.coords)
+                    _lib.check()
+                    res += work * self.kws[k % self.nwk] / self.nspin
+        return res.reshape(tuple(g))
+
+    def _write_volumetric(self, filename, values, dim, scale):
+        """A VASP volumetric file: the structure header of _convert_to_vasp_volumetric
+        (wavefunction.py:481-510), the grid dimensions, then the values times scale with the
+        first index fastest, five per line, as write_volumetric (density.c:461-477) prints them."""
+        st = self.structure
+        syms, counts = [], []
+        for sp in st.species:
+            if syms and syms[-1] == sp:
+                counts[-1] += 1
+            else:
+                syms.append(sp)
+                counts.append(1)
+        lines = [filename, "   1.00000000000000"]
+        for row in np.asarray(st.lattice).reshape(3, 3):
+            lines.append(" %12.6f%12.6f%12.6f" % tuple(row))
+        lines.append("".join("%5s" % x for x in syms))
+        lines.append("".join("%6d" % x for x in counts))
+        lines.append("Direct")
+        for fc in st.frac_coords:
+            lines.append("%10.6f%10.6f%10.6f" % tuple(fc))
+        lines.append(" ")
+        lines.append("%d %d %d" % tuple(int(x) for x in dim))
+        vals = (np.asarray(values).reshape(tuple(dim)).transpose(2, 1, 0).ravel() * scale)
+        body = []
+        for i in range(0, vals.size, 5):
+            body.append("".join("%E   " % v for v in vals[i:i + 5]))
+        with open(filename, "w") as fh:
+            fh.write("\n".join(lines) + "\n" + "\n".join(body) + ("\n" if body else ""))
+
+    def write_state_realspace(self, b, k, s, fileprefix="", dim=None, scale=1, remove_phase=False):
+        """Writes the real and imaginary parts of one band to <prefix>B<b>K<k>S<s>_REAL.vasp and
+        _IMAG.vasp (wavefunction.py:512-555); returns the complex grid."""
+        res = self.get_state_realspace(b, k, s, dim, remove_phase)
+        base = "%sB%dK%dS%d" % (fileprefix, b, k, s)
+        self._write_volumetric("%s_REAL.vasp" % base, np.real(res), res.shape, scale)
+        self._write_volumetric("%s_IMAG.vasp" % base, np.imag(res), res.shape, scale)
+        return res
+
+    def write_density_realspace(self, filename="PYAECCAR.vasp", dim=None, scale=1, bands=None):
+        """Writes the all-electron charge density (wavefunction.py:557-590); returns it."""
+        res = self.get_realspace_density(dim, bands)
+        self._write_volumetric(filename, res, res.shape, scale)
+        return res
+
     def pseudoprojection(self, band_num, basis, flip_spin=False):
         """<psi~_basis,b,k|psi~_self,band_num,k> for all basis bands b and k (pawpyc.pyx:311-325)."""
         res = np.zeros(basis.nband * basis.nwk * basis.nspin, dtype=np.complex128)

@@ -67,6 +67,14 @@ def workload_dirs(tmp_path_factory):
 
 
 @pytest.fixture(scope="session")
+def realspace_dirs(tmp_path_factory):
+    """The 64-atom workload reduced to 4 bands and 2 k-points (the real-space golden fixture's)."""
+    from pawpyseed_gb300 import synth
+
+    return synth.write_workload(str(tmp_path_factory.mktemp("realspace")), 0, nband=4, nk=2)
+
+
+@pytest.fixture(scope="session")
 def golden():
     def get(name):
         return np.load(os.path.join(GOLDEN, name + ".npz"))

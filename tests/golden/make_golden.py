@@ -21,10 +21,17 @@ Fixtures:
   ``aug_recip`` method (``recip_total_*``) with the augmentation coefficients
   band->CAs of band 0 of each side that has them, per k-point, first 4096
   plane waves in file order (``recip_CA_<side>_k<k>``).
+* ``realspace_cfg0.npz`` -- the real-space functions of density.c on the
+  64-atom workload reduced to 4 bands and 2 k-points, on the defect's grid:
+  ``realspace_state`` of band 1 at k-point 1 (``state_b1_k1``),
+  ``ae_chg_density`` of the defect (``rho``), and
+  ``project_realspace_state`` of every defect band onto the basis (``proj``,
+  [band][basis band * nk + k]).
 
 The reference tree is read from $PAWPY_REFERENCE (default /root/reference).
 """
 
+import ctypes as C
 import hashlib
 import os
 import shutil
@@ -41,6 +48,11 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from pawpyseed_gb300 import synth, vaspio  # noqa: E402
 
 REFERENCE = os.environ.get("PAWPY_REFERENCE", "/root/reference")
+
+# realspace_state adds the sites' partial waves from an OpenMP loop over sites whose
+# updates of shared grid cells are unsynchronised (density.c:265-306); one thread makes
+# the sums deterministic.
+os.environ["OMP_NUM_THREADS"] = "1"
 
 CASES = {
     # name: (workload, nband, nk, flips)
@@ -132,10 +144,53 @@ def case_fixture(name, cfg, nband, nk, flips):
         shutil.rmtree(tmp)
 
 
+def realspace_fixture():
+    import ref_harness as rh
+
+    lib = rh.load_ref()
+    zp = np.ctypeslib.ndpointer(dtype=np.complex128, flags="C_CONTIGUOUS")
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+    wfp = C.POINTER(rh.S.pswf_t)
+    lib.realspace_state.argtypes = [zp, C.c_int, C.c_int, wfp, ip, ip, dp]
+    lib.ae_chg_density.argtypes = [dp, wfp, ip, ip, dp]
+    lib.project_realspace_state.argtypes = [zp, C.c_int, wfp, wfp, ip, ip, dp, ip, dp]
+    tmp = tempfile.mkdtemp()
+    try:
+        paths = synth.write_workload(tmp, 0, nband=4, nk=2)
+        b = rh.RefWavefunction(lib, paths["basis"])
+        d = rh.RefWavefunction(lib, paths["defect"])
+        b.setup_projectors()
+        d.setup_projectors()
+        fftg = np.ascontiguousarray(d.dim, dtype=np.int32)
+        n = int(np.prod(fftg))
+        x = np.zeros(n, np.complex128)
+        lib.realspace_state(x, 1, 1, d.ptr, fftg, d.nums, d.coords)
+        rho = np.zeros(n)
+        lib.ae_chg_density(rho, d.ptr, fftg, d.nums, d.coords)
+        nk = d.nwk * d.nspin
+        proj = np.zeros((d.nband, b.nband * nk), np.complex128)
+        for band in range(d.nband):
+            row = np.zeros(b.nband * nk, np.complex128)
+            lib.project_realspace_state(row, band, d.ptr, b.ptr, fftg, d.nums, d.coords, b.nums, b.coords)
+            proj[band] = row
+        out = dict(fp_basis=fingerprint(paths["basis"]), fp_defect=fingerprint(paths["defect"]),
+                   fftg=fftg, state_b1_k1=x.reshape(tuple(fftg)), rho=rho.reshape(tuple(fftg)), proj=proj)
+        np.savez_compressed(os.path.join(HERE, "realspace_cfg0.npz"), **out)
+        print("realspace_cfg0 written: grid", tuple(fftg), "sum rho dV =",
+              rho.sum() * abs(np.linalg.det(d.struct.lattice)) / n)
+        b.free()
+        d.free()
+    finally:
+        shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["fft"] + list(CASES)
+    which = sys.argv[1:] or ["fft"] + list(CASES) + ["realspace"]
     for w in which:
         if w == "fft":
             fft_fixture()
+        elif w == "realspace":
+            realspace_fixture()
         else:
             case_fixture(w, *CASES[w])

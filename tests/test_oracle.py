@@ -150,3 +150,31 @@ def test_oracle_recip_matches_reference(name, workload_dirs, golden, oracle_proj
         ref = g[key]
         mine = CA[int(k)][0][: ref.shape[0]]
         assert np.abs(mine - ref).max() <= (1e-6 if same else 1e-5) * np.abs(ref).max()
+
+
+def test_oracle_realspace_matches_reference(realspace_dirs, golden):
+    """realspace_state, ae_chg_density and project_realspace_state (density.c:27-310) of the
+    oracle against the reference on the same inputs, to rounding."""
+    import oracle as orc
+
+    g = golden("realspace_cfg0")
+    same = same_golden_inputs(realspace_dirs, g, "realspace_cfg0")
+    tol = 1e-12 if same else 1e-5
+    w = orc.OracleWavefunction(realspace_dirs["defect"])
+    b = orc.OracleWavefunction(realspace_dirs["basis"])
+    w.setup_projectors()
+    b.setup_projectors()
+    N = g["fftg"]
+    x = w.realspace_state(1, 1, N)
+    assert np.abs(x - g["state_b1_k1"]).max() <= tol
+    rho = w.ae_chg_density(N)
+    assert np.abs(rho - g["rho"]).max() <= tol
+    nk = w.nk
+    vol = abs(np.linalg.det(w.lattice))
+    n3 = int(np.prod(N))
+    proj = np.zeros_like(g["proj"])
+    for k in range(nk):
+        S = np.array([w.realspace_state(bb, k, N).ravel() for bb in range(w.nband)])
+        R = np.array([b.realspace_state(bb, k, N).ravel() for bb in range(b.nband)])
+        proj[:, k::nk] = S @ R.conj().T * vol / n3
+    assert np.abs(proj - g["proj"]).max() <= tol
