@@ -332,7 +332,8 @@ def roofline(stats, w, basis, wf, lists, cr):
     for name, (ms, n, work) in stats.items():
         if name.startswith("host."):
             continue
-        key = "fft" if name in ("fft_planes", "fft_x_pick") else name
+        key = "fft" if name in ("fft_planes", "fft_x_pick") else (
+            "sphere_contract" if name.startswith("sphere_contract") else name)
         a = fams.setdefault(key, [0.0, 0, 0.0, []])
         a[0] += ms
         a[1] += n

@@ -313,6 +313,12 @@ void pawpy_gpu_set_tc_splits(int splits);
  * the fastest (PAWPY_GPU_TUNE_VERBOSE=1 prints each decision). No counterpart
  * in the reference. */
 void pawpy_gpu_set_tc_tile(int bn);
+/* Form of the sphere contraction (the projections <p|psi> of
+ * onto_projector_helper, projector.c:223-274): 1 (the default) on the tensor
+ * cores (split-BF16) whenever the precision is a tensor-core one, FP32 CUDA
+ * cores otherwise; 0 always the FP32 CUDA-core form; 2 always the tensor-core
+ * form. No counterpart in the reference. */
+void pawpy_gpu_set_sphere_contraction(int mode);
 
 /* Batched overlap matrices of host arrays, no counterpart in the reference
  * (pseudoprojection's contraction, pseudoprojector.c:63-90, on raw matrices):

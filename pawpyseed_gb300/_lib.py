@@ -80,6 +80,7 @@ def _declare(L):
     L.pawpy_gpu_get_precision.restype = C.c_int
     L.pawpy_gpu_set_tc_splits.argtypes = [C.c_int]
     L.pawpy_gpu_set_tc_tile.argtypes = [C.c_int]
+    L.pawpy_gpu_set_sphere_contraction.argtypes = [C.c_int]
     L.pawpy_gpu_set_element_cache.argtypes = [C.c_int]
     L.pawpy_gpu_prepare_basis.restype = C.c_int
     L.pawpy_gpu_prepare_basis.argtypes = [_wfp, C.c_int]

@@ -217,6 +217,12 @@ static std::map<const pswf_t *, std::unique_ptr<DevWF>> g_wfs;
 static std::map<std::pair<const pswf_t *, const pswf_t *>, std::unique_ptr<PairState>> g_pairs;
 // process-wide switches; serving threads read them while a caller may set them
 static std::atomic<int> g_precision{PAWPY_GPU_FP32};
+// sphere contraction on the tensor cores: 1 with the tensor-core precisions, 0 never, 2 always
+static std::atomic<int> g_sphere_tc{1};
+static bool sphere_tc_enabled() {
+  const int m = g_sphere_tc.load(), prec = g_precision.load();
+  return m == 2 || (m == 1 && (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32));
+}
 static std::atomic<int> g_tc_splits{0};  // K split of the tensor-core contraction, 0 = from the SM count
 static std::atomic<bool> g_host_proj{true};
 
@@ -976,6 +982,51 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     mdev[i].alloc(col.size());
     mdev[i].upload(col.data(), col.size());
   }
+  // tensor-core form: one site per z, table planes built once per call
+  const bool tc = sphere_tc_enabled() && max_total > 0;
+  std::vector<TcSite> tsites;
+  std::vector<TcTable> ttabs;
+  int tc_bn = 0, tc_brows = 0, tc_maxkb = 0;
+  long long tc_lb = 0;
+  DevBuf<TcSite> tsites_d;
+  DevBuf<unsigned char> tc_planes;
+  if (tc) {
+    tc_bn = tc_sphere_width(max_total);
+    long long xo = 0;
+    for (size_t i = 0; i < sets.size(); i++) {
+      const SphereSet &S = *sets[i];
+      for (int s = 0; s < S.nsites; s++) {
+        const long long x_off = xo + S.site_pt[s];
+        const int lead = (int)(x_off & 1), n = S.site_npts[s];
+        TcSite ts;
+        ts.a_x = x_off - lead;
+        ts.nkb = (lead + n + 15) / 16;
+        ts.b_row = (int)tsites.size() * tc_bn;
+        ts.total = S.host[s].total;
+        ts.ld = S.Ptot;
+        ts.out = outs[i] + S.host[s].lm_off;
+        TcTable tt;
+        tt.tab = S.tab.p + S.site_val[s];
+        tt.npts = n;
+        tt.lead = lead;
+        tt.total = ts.total;
+        tt.nkb = ts.nkb;
+        tt.b_row = ts.b_row;
+        tc_maxkb = std::max(tc_maxkb, ts.nkb);
+        tsites.push_back(ts);
+        ttabs.push_back(tt);
+      }
+      xo += S.npts;
+    }
+    tc_brows = (int)tsites.size() * tc_bn;
+    tc_lb = (long long)std::max(1, tc_maxkb) * 32;
+    tc_planes.alloc((size_t)2 * tc_brows * tc_lb * 2);
+    tsites_d.alloc(std::max<size_t>(1, tsites.size()));
+    tsites_d.upload(tsites.data(), tsites.size());
+    DevBuf<TcTable> ttabs_d(std::max<size_t>(1, ttabs.size()));
+    ttabs_d.upload(ttabs.data(), ttabs.size());
+    launch_tc_tables(ttabs_d.p, (int)ttabs.size(), tc_maxkb, tc_bn, tc_brows, tc_lb, tc_planes.p);
+  }
   int maxn1 = 0;
   for (auto &q : d.kp) maxn1 = std::max(maxn1, q.n1);
   // FFT sub-batch: the plane-FFT intermediate H of a sub-batch stays within L2
@@ -990,7 +1041,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   // A wavefunction held in real space skips X: the contraction gathers its grid values.
   const bool gather = d.grid_ready;
   const long long xstride = (xtot + 3) / 4 * 4;
-  const long long per_row = ((gather ? 0 : xstride) + ptot) * (long long)sizeof(float2);
+  const long long per_row = ((gather ? 0 : xstride) + (tc ? 0 : ptot)) * (long long)sizeof(float2);
   const long long rows = (long long)d.nk * d.nband;
   const long long cbatch =
       std::min({rows, 32768LL, std::max<long long>(fbatch, (2LL << 30) / std::max(1LL, per_row))});
@@ -1019,7 +1070,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     src.X = X.p;
     src.xstride = xstride;
   }
-  DevBuf<float2> partial((size_t)cbatch * std::max(1, ptot));
+  DevBuf<float2> partial(tc ? 1 : (size_t)cbatch * std::max(1, ptot));
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<char> fast(d.nk);
   for (int k = 0; k < d.nk; k++) fast[k] = plane_geom(d, k, geo[k]);
@@ -1055,6 +1106,10 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     }
     const int cn = (int)(r1 - r0);
     src.r0 = r0;
+    if (tc) {
+      launch_tc_sphere(tsites_d.p, (int)tsites.size(), tc_bn, tc_planes.p, tc_brows, tc_lb, src, cn, xtot, xtot);
+      continue;
+    }
     launch_contract_staged(ch_d.p, (int)chunks.size(), max_total, src, partial.p, ptot, cn, xtot);
     for (size_t i = 0; i < sets.size(); i++) {
       const SphereSet &S = *sets[i];
@@ -2046,6 +2101,7 @@ int pawpy_gpu_get_precision(void) { return g_precision; }
 void pawpy_gpu_set_tc_splits(int splits) { g_tc_splits = splits < 0 ? 0 : splits; }
 void pawpy_gpu_set_element_cache(int on) { set_projector_list_cache(on != 0); }
 void pawpy_gpu_set_tc_tile(int bn) { set_tc_tile(bn); }
+void pawpy_gpu_set_sphere_contraction(int mode) { g_sphere_tc = (mode >= 0 && mode <= 2) ? mode : 1; }
 
 int pawpy_gpu_overlap_matrix(const pawpy_c64 *A, const pawpy_c64 *B, int M, int N, int nz, const int *K,
                              pawpy_c64 *out, int precision) {

@@ -125,6 +125,28 @@ struct ContractSource {
 // npts (the merged point space) sizes the declared work
 void launch_contract_staged(const ChunkContract *chunks, int nchunks, int max_total, const ContractSource &src,
                             float2 *partial, int ptot, int nb, long long npts);
+// Tensor-core form of the contraction (sphere_tc.cu). One site of one set: its K range
+// starts at the even point a_x of the merged point space and spans nkb blocks of 16 points;
+// its table occupies rows [b_row, b_row + width) of the table planes; P of row R (global
+// (k-point, band) row) is written to out[R * ld + c] for channels c < total.
+struct TcSite {
+  long long a_x = 0;
+  int nkb = 0, b_row = 0, total = 0, ld = 0;
+  float2 *out = nullptr;
+};
+// Source of one site's table planes: tab[c][npts] (site_npts stride), shifted by lead points.
+struct TcTable {
+  const float2 *tab = nullptr;
+  int npts = 0, lead = 0, total = 0, nkb = 0, b_row = 0;
+};
+// table width (2 x channels, padded) for the widest site: 32, 48 or 64
+int tc_sphere_width(int max_total);
+// BF16 hi/lo table planes [2][brows][lb] of every site
+void launch_tc_tables(const TcTable *tabs_dev, int nsites, int max_nkb, int bn, int brows, long long lb,
+                      void *planes);
+// P of every site for the rows [r0, r0 + nb) of src (picked rows: xtot points per row)
+void launch_tc_sphere(const TcSite *sites_dev, int nsites, int bn, const void *planes, int brows, long long lb,
+                      const ContractSource &src, int nb, long long npts, long long xtot);
 // the global cell and Bloch phase of every point of the merged point space
 void launch_point_index(const GatherSeg *segs, const int *seg_j, int nsegs, int N2, int N3, int nkp, long long Q,
                         int *gcell, float2 *gphase);

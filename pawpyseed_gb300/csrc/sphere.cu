@@ -50,6 +50,45 @@ __device__ __forceinline__ bool slab_point(const SiteDesc &s, int jb, int q, con
   return s_norm(path) < s.R0;
 }
 
+// Single-precision pre-test of slab_point: the displacement in grid units times the
+// lattice rows over N, squared length against R0^2 widened by a relative margin of 1e-4
+// (far above the single-precision error, about 1e-6 here). 1: inside, 0: outside, -1:
+// within the margin (slab_point decides).
+struct FastTest {
+  float lf[9];   // L[a][c] / N[a]
+  float cn[3];   // site position in grid units
+  float r2lo, r2hi;
+  __device__ void init(const SiteDesc &s, const double *L, const int *N) {
+    for (int a = 0; a < 3; a++) {
+      cn[a] = (float)(s.coord[a] * N[a]);
+      for (int c = 0; c < 3; c++) lf[3 * a + c] = (float)(L[3 * a + c] / N[a]);
+    }
+    const double r2 = s.R0 * s.R0;
+    r2lo = (float)(r2 * (1.0 - 1e-4));
+    r2hi = (float)(r2 * (1.0 + 1e-4));
+  }
+  __device__ int test(const int *ijk) const {
+    const float u0 = (float)ijk[0] - cn[0], u1 = (float)ijk[1] - cn[1], u2 = (float)ijk[2] - cn[2];
+    const float x = u0 * lf[0] + u1 * lf[3] + u2 * lf[6];
+    const float y = u0 * lf[1] + u1 * lf[4] + u2 * lf[7];
+    const float z = u0 * lf[2] + u1 * lf[5] + u2 * lf[8];
+    const float r2 = x * x + y * y + z * z;
+    return r2 < r2lo ? 1 : (r2 > r2hi ? 0 : -1);
+  }
+};
+
+// slab_point's verdict through the pre-test; the FP64 path only within the margin
+__device__ __forceinline__ bool slab_inside(const SiteDesc &s, const FastTest &ft, int jb, int q, const double *L,
+                                            const int *N) {
+  const int w2 = 2 * s.g[2] + 1;
+  const int ijk[3] = {box_i(s, 0, q / w2), box_i(s, 1, jb), box_i(s, 2, q % w2)};
+  const int v = ft.test(ijk);
+  if (v >= 0) return v == 1;
+  int ijk2[3];
+  double path[3];
+  return slab_point(s, jb, q, L, N, ijk2, path);
+}
+
 __global__ void k_slab_count(const SiteDesc *__restrict__ sites, const int2 *__restrict__ slabs,
                              const double *__restrict__ Lg, const int *__restrict__ Ng, int *__restrict__ counts) {
   __shared__ int total;
@@ -58,14 +97,13 @@ __global__ void k_slab_count(const SiteDesc *__restrict__ sites, const int2 *__r
   double L[9];
   int N[3] = {Ng[0], Ng[1], Ng[2]};
   for (int i = 0; i < 9; i++) L[i] = Lg[i];
+  FastTest ft;
+  ft.init(s, L, N);
   if (threadIdx.x == 0) total = 0;
   __syncthreads();
   int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1), c = 0;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    int ijk[3];
-    double path[3];
-    if (slab_point(s, sl.y, q, L, N, ijk, path)) c++;
-  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x)
+    if (slab_inside(s, ft, sl.y, q, L, N)) c++;
   atomicAdd(&total, c);
   __syncthreads();
   if (threadIdx.x == 0) counts[blockIdx.x] = total;
@@ -94,6 +132,8 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
   int N[3] = {Ng[0], Ng[1], Ng[2]};
   for (int i = 0; i < 9; i++) L[i] = Lg[i];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  FastTest ft;
+  ft.init(s, L, N);
   if (threadIdx.x == 0) base_s = 0;
   __syncthreads();
   const int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1);
@@ -101,7 +141,8 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
     int q = start + threadIdx.x;
     int ijk[3];
     double path[3];
-    bool in = q < n && slab_point(s, sg.jb, q, L, N, ijk, path);
+    bool in = q < n && slab_inside(s, ft, sg.jb, q, L, N);
+    if (in) slab_point(s, sg.jb, q, L, N, ijk, path);  // the exact displacement of an inside point
     unsigned m = __ballot_sync(0xffffffffu, in);
     if (lane == 0) warp_cnt[wid] = __popc(m);
     __syncthreads();
