@@ -77,6 +77,67 @@ void launch_aug_b(const float2 *P, int Pt, const float2 *WP, int Pw, int nbtot, 
                                                         npairs, Kc, Kcpad, B64, B32));
 }
 
+// The FP32 form of k_aug_b for the batched contraction (its B columns are FP32): val32[k][e]
+// holds the entry times the column's pair phase. One thread per column and four bands.
+__global__ void k_aug_b32(const float2 *__restrict__ P, int Pt, const float2 *__restrict__ WP, int Pw, int nbtot,
+                          int nb, const int *__restrict__ ptr, const int *__restrict__ col,
+                          const float2 *__restrict__ val32, int nent, int Kc, int Kcpad,
+                          float2 *__restrict__ B32) {
+  constexpr int NBT = 4;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bb = blockIdx.y * NBT, k = blockIdx.z;
+  if (c >= Kcpad) return;
+  float re[NBT], im[NBT];
+#pragma unroll
+  for (int u = 0; u < NBT; u++) re[u] = im[u] = 0.f;
+  if (c < Kc) {
+    const float2 *vk = val32 + (long long)k * nent;
+    for (int e = ptr[c]; e < ptr[c + 1]; e++) {
+      const int s = col[e];
+      const float2 w = vk[e];
+#pragma unroll
+      for (int u = 0; u < NBT; u++) {
+        if (bb + u < nb) {
+          const long long row = (long long)k * nbtot + bb + u;
+          const float2 x = s < Pt ? P[row * Pt + s] : WP[row * Pw + (s - Pt)];
+          re[u] = fmaf(w.x, x.x, fmaf(-w.y, x.y, re[u]));
+          im[u] = fmaf(w.x, x.y, fmaf(w.y, x.x, im[u]));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NBT; u++)
+    if (bb + u < nb) B32[((long long)k * nb + bb + u) * Kcpad + c] = make_float2(re[u], im[u]);
+}
+
+__global__ void k_aug_val32(const double2 *__restrict__ val, const int *__restrict__ e_pair, int n, int ne,
+                            const double2 *__restrict__ phase, int npairs, float2 *__restrict__ val32) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  if (e >= ne) return;
+  double2 v = e < n ? val[e] : make_double2(0.0, 0.0);
+  if (e < n && e_pair[e] >= 0) {
+    const double2 f = phase[(long long)k * npairs + e_pair[e]];
+    v = make_double2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
+  }
+  val32[(long long)k * ne + e] = make_float2((float)v.x, (float)v.y);
+}
+
+void launch_aug_val32(const double2 *val, const int *e_pair, int n, int ne, const double2 *phase, int npairs, int nk,
+                      float2 *val32) {
+  if (ne <= 0 || nk <= 0) return;
+  dim3 g(ceil_div(ne, 256), nk);
+  PAWPY_LAUNCH("aug_setup", k_aug_val32<<<g, 256, 0, stream()>>>(val, e_pair, n, ne, phase, npairs, val32));
+}
+
+void launch_aug_b32(const float2 *P, int Pt, const float2 *WP, int Pw, int nbtot, int nb, int nk, const int *ptr,
+                    const int *col, const float2 *val32, int nent, int Kc, int Kcpad, float2 *B32) {
+  if (Kcpad <= 0 || nb <= 0 || nk <= 0) return;
+  dim3 g(ceil_div(Kcpad, 128), ceil_div(nb, 4), nk);
+  PAWPY_LAUNCH("aug_b", k_aug_b32<<<g, 128, 0, stream()>>>(P, Pt, WP, Pw, nbtot, nb, ptr, col, val32, nent, Kc,
+                                                          Kcpad, B32));
+}
+
 __global__ void k_to_host_layout(const float2 *__restrict__ S, int nk, int nbS, int nbR, double2 *__restrict__ out) {
   long long n = (long long)nk * nbS * nbR;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {

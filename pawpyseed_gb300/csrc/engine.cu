@@ -196,6 +196,7 @@ struct PairState {
   DevBuf<int> a_src, b_ptr, b_col, b_pair;
   DevBuf<double2> b_val;
   DevBuf<double2> pair_phase;  // [nk][npairs]
+  DevBuf<float2> b_val32;      // [nk][entries]: b_val times the column's pair phase, FP32
   // aug_recip: set by overlap_setup_recip (the overlaps then follow that method). The
   // augmentation coefficients of R's bands on its N_R sites and of S's bands on its N_S
   // sites, [nk][nband][Wpad] in the sorted plane-wave order (empty when the list is);
@@ -219,6 +220,8 @@ static std::map<std::pair<const pswf_t *, const pswf_t *>, std::unique_ptr<PairS
 static std::atomic<int> g_precision{PAWPY_GPU_FP32};
 // sphere contraction on the tensor cores: 1 with the tensor-core precisions, 0 never, 2 always
 static std::atomic<int> g_sphere_tc{1};
+// picked-point rows per batch of the tensor-core sphere contraction, in bytes
+constexpr long long kTcPickBatchBytes = 12LL << 30;
 static bool sphere_tc_enabled() {
   const int m = g_sphere_tc.load(), prec = g_precision.load();
   return m == 2 || (m == 1 && (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32));
@@ -996,8 +999,9 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     for (size_t i = 0; i < sets.size(); i++) {
       const SphereSet &S = *sets[i];
       for (int s = 0; s < S.nsites; s++) {
+        // K ranges start on a multiple of 4 points (16-byte TMA coordinates of the split rows)
         const long long x_off = xo + S.site_pt[s];
-        const int lead = (int)(x_off & 1), n = S.site_npts[s];
+        const int lead = (int)(x_off & 3), n = S.site_npts[s];
         TcSite ts;
         ts.a_x = x_off - lead;
         ts.nkb = (lead + n + 15) / 16;
@@ -1043,8 +1047,11 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   const long long xstride = (xtot + 3) / 4 * 4;
   const long long per_row = ((gather ? 0 : xstride) + (tc ? 0 : ptot)) * (long long)sizeof(float2);
   const long long rows = (long long)d.nk * d.nband;
+  // (the tensor-core form keeps no partial sums and reads the rows once: a larger batch, fewer launches)
+  const long long xcap = tc ? kTcPickBatchBytes : (2LL << 30);
   const long long cbatch =
-      std::min({rows, 32768LL, std::max<long long>(fbatch, (2LL << 30) / std::max(1LL, per_row))});
+      std::min({rows, 32768LL, std::max<long long>(fbatch, xcap / std::max(1LL, per_row))});
+  const bool split_x = tc && !gather;  // pass B writes the split BF16 rows the tensor cores read
   const bool early = d.h_ready && !d.grid_ready;
   DevBuf<float2> H(d.grid_ready || early ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
   DevBuf<float2> X(gather ? 1 : (size_t)cbatch * std::max(1LL, xstride));
@@ -1069,7 +1076,9 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   } else {
     src.X = X.p;
     src.xstride = xstride;
+    src.xrows = split_x ? cbatch : 0;
   }
+  const long long lo_words = split_x ? cbatch * xstride : 0;
   DevBuf<float2> partial(tc ? 1 : (size_t)cbatch * std::max(1, ptot));
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<char> fast(d.nk);
@@ -1086,21 +1095,25 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       const int step = early ? std::max(1, bhi - blo) : fbatch;
       for (int b0 = blo; b0 < bhi; b0 += step) {
         const int nb = std::min(step, bhi - b0);
-        float2 *xb = gather ? nullptr : X.p + ((long long)k * d.nband + b0 - r0) * xstride;
+        // first row of the sub-batch (in 32-bit words of the hi plane for the split rows)
+        const long long roff = (long long)k * d.nband + b0 - r0;
+        float2 *xb = gather   ? nullptr
+                     : split_x ? reinterpret_cast<float2 *>(reinterpret_cast<uint32_t *>(X.p) + roff * xstride)
+                               : X.p + roff * xstride;
         if (early) {
           PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
           launch_fft_x_pick_fast(d.Hall.p + d.hoff[k] + (size_t)b0 * q.n1 * d.N[1] * d.N[2], g, plist, k, xb,
-                                 xstride, nb);
+                                 xstride, nb, lo_words);
         } else if (gather) {
           // resident real-space wavefunctions: the contraction reads them directly
         } else if (fast[k]) {
           launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                                  H.p, nb);
-          launch_fft_x_pick_fast(H.p, g, plist, k, xb, xstride, nb);
+          launch_fft_x_pick_fast(H.p, g, plist, k, xb, xstride, nb, lo_words);
         } else {
           launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, xstride, nb);
+          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, xstride, nb, lo_words);
         }
       }
     }
@@ -2062,6 +2075,18 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
   ps.b_pair.upload(b_pair.data(), b_pair.size());
   ps.pair_phase.alloc(ph.size());
   ps.pair_phase.upload(ph.data(), ph.size());
+  {
+    // FP32 entries with the pair phase of their column folded in, per k-point (on the device)
+    const size_t ne = std::max<size_t>(1, b_val.size());
+    std::vector<int> e_pair(ne, -1);
+    for (size_t c = 0; c + 1 < b_ptr.size(); c++)
+      for (int e = b_ptr[c]; e < b_ptr[c + 1]; e++) e_pair[e] = b_pair[c];
+    DevBuf<int> e_pair_d(ne);
+    e_pair_d.upload(e_pair.data(), ne);
+    ps.b_val32.alloc((size_t)S.nk * ne);
+    launch_aug_val32(ps.b_val.p, e_pair_d.p, (int)b_val.size(), (int)ne, ps.pair_phase.p, std::max(1, npairs), S.nk,
+                     ps.b_val32.p);
+  }
   // basis-side columns for every k-slice of R
   ps.A64.alloc(std::max<size_t>(1, (size_t)R.nk * R.nband * ps.Kc));
   ps.A32.alloc(std::max<size_t>(1, (size_t)R.nk * R.nband * ps.Kcpad));
@@ -2345,8 +2370,9 @@ static void full_overlap(PairState &ps, const std::vector<int> lists[6], int fli
   DevWF &R = *ps.R, &S = *ps.S;
   int nk = S.nk, npairs = (int)ps.N_RS_R.size();
   DevBuf<float2> B32((size_t)nk * S.nband * std::max(16, ps.Kcpad));
-  launch_aug_b(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, 0, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
-               ps.b_val.p, ps.b_pair.p, ps.pair_phase.p, std::max(1, npairs), ps.Kc, ps.Kcpad, nullptr, B32.p);
+  (void)npairs;
+  launch_aug_b32(S.P.p, S.proj.Ptot, ps.WP_S.p, ps.sm_NR.Ptot, S.nband, S.nband, nk, ps.b_ptr.p, ps.b_col.p,
+                 ps.b_val32.p, (int)(ps.b_val32.n / std::max(1, nk)), ps.Kc, ps.Kcpad, B32.p);
   Smat.alloc((size_t)nk * host_bands(S) * host_bands(R));
   overlap_gemm(ps, flip_spin, ps.Kcpad > 0 ? B32.p : nullptr, Smat.p, g_precision.load());
 }

@@ -16,6 +16,8 @@
 // first batch (the results do not depend on it).
 #pragma once
 
+#include "bf16split.cuh"
+
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -255,12 +257,44 @@ __global__ void __launch_bounds__(FT) k_planes_direct(const float2 *__restrict__
 // the plane's H rows of the current and the next band (cp.async), tile
 // [N1][LD] the transformed plane and, when the plane has at most pts_cap
 // points, a copy of its pick list (the same for every band).
+// The pick of one plane: value at tile cell times the point's Bloch phase, to its position in
+// the picked-point row of band b. The lists are read from global memory (L2) U points per
+// thread at a time, all loads in flight before the stores.
+template <int N3, int LD>
+__device__ __forceinline__ void pick_plane(const float2 *tile, const int *__restrict__ cell,
+                                           const int *__restrict__ xo, const float2 *__restrict__ phase, int npj,
+                                           int t0, int nt, float2 *X, long long b, long long xstride,
+                                           long long lo_words) {
+  constexpr int U = 8;
+  for (int q0 = t0; q0 < npj; q0 += nt * U) {
+    int c[U], o[U];
+    float2 f[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * nt;
+      if (q < npj) {
+        c[u] = __ldg(cell + q);
+        o[u] = __ldg(xo + q);
+        f[u] = __ldg(phase + q);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * nt;
+      if (q < npj) {
+        const int xr = c[u] / N3, z = c[u] - xr * N3;
+        put_picked(X, b, xstride, lo_words, o[u], cmul(tile[xr * LD + z], f[u]));
+      }
+    }
+  }
+}
+
 template <int N1, int N3>
 __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H, int nb, PlaneGeom g,
                                                    const int *__restrict__ plane_first,
                                                    const int *__restrict__ cell, const int *__restrict__ xo,
                                                    const float2 *__restrict__ phase, int pts_cap,
-                                                   float2 *__restrict__ X, long long xstride) {
+                                                   float2 *__restrict__ X, long long xstride, long long lo_words) {
   constexpr int LD = padded(N3);
   constexpr int T1 = reg::lanes_for(N1), L1 = N1 / T1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -325,14 +359,12 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
       }
     }
     __syncthreads();
-    float2 *xb = X + (long long)b * xstride;
     if (staged) {
-      for (int q = threadIdx.x; q < npj; q += blockDim.x) xb[pxo[q]] = cmul(tile[pto[q]], pph[q]);
+      for (int q = threadIdx.x; q < npj; q += blockDim.x)
+        put_picked(X, b, xstride, lo_words, pxo[q], cmul(tile[pto[q]], pph[q]));
     } else {
-      for (int q = threadIdx.x; q < npj; q += blockDim.x) {
-        const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
-        xb[xo[pf + q]] = cmul(tile[xr * LD + z], phase[pf + q]);
-      }
+      pick_plane<N3, LD>(tile, cell + pf, xo + pf, phase + pf, npj, threadIdx.x, blockDim.x, X, b, xstride,
+                         lo_words);
     }
   }
 }
@@ -348,7 +380,7 @@ __global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ 
                                                      const int *__restrict__ plane_first,
                                                      const int *__restrict__ cell, const int *__restrict__ xo,
                                                      const float2 *__restrict__ phase, float2 *__restrict__ X,
-                                                     long long xstride) {
+                                                     long long xstride, long long lo_words) {
   constexpr int LD = padded(N3), L1 = N1 / T1;
   constexpr int TPB = 32 * ((N3 * T1 + 31) / 32) < FT ? 32 * ((N3 * T1 + 31) / 32) : FT;  // threads per band
   constexpr int BPC = FT / TPB;
@@ -385,11 +417,7 @@ __global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ 
   __syncthreads();
   if (!band_ok) return;
   const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
-  float2 *xb = X + (long long)b * xstride;
-  for (int q = gt; q < npj; q += TPB) {
-    const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
-    xb[xo[pf + q]] = cmul(tile[xr * LD + z], phase[pf + q]);
-  }
+  pick_plane<N3, LD>(tile, cell + pf, xo + pf, phase + pf, npj, gt, TPB, X, b, xstride, lo_words);
 }
 
 // Pass B writing whole grids (resident real-space wavefunctions): grid

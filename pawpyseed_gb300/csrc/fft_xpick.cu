@@ -6,10 +6,10 @@ namespace pawpy {
 namespace {
 
 using PickFn = void (*)(const float2 *, int, PlaneGeom, const int *, const int *, const int *, const float2 *, int,
-                       float2 *, long long);
+                       float2 *, long long, long long);
 
 using DirectFn = void (*)(const float2 *, int, PlaneGeom, const int *, const int *, const int *, const float2 *,
-                         float2 *, long long);
+                         float2 *, long long, long long);
 
 PickFn find_pick(int n1, int n3) {
 #define X(a, b) \
@@ -53,7 +53,7 @@ bool fft_fast_supported(const PlaneGeom &g) {
 }
 
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
-                            long long xstride, int nb) {
+                            long long xstride, int nb, long long lo_words) {
   using namespace fftfast;
   if (nb <= 0) return;
   PickFn fn = find_pick(g.N1, g.N3);
@@ -73,15 +73,15 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
     if (mult == 0) {
       dim3 grid(ceil_div(nb, bpc), g.N2);
       PAWPY_LAUNCH("fft_x_pick", dfn<<<grid, FT, dsmem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, X,
-                                                                    xstride));
+                                                                    xstride, lo_words));
       return;
     }
     const int G = std::max(1, std::min(nb, ceil_div((long long)waves * mult, g.N2)));
     dim3 grid(g.N2, G);
     PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, cap, X,
-                                                                xstride));
+                                                                xstride, lo_words));
   };
-  int mult = tune(std::make_tuple(1, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
+  int mult = tune(std::make_tuple(lo_words ? 3 : 1, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
   run(mult);
   note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }

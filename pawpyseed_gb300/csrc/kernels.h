@@ -45,8 +45,10 @@ struct PickList {
   long long npts = 0;
   int max_plane_pts = 0;
 };
+// lo_words > 0: the rows are written in the split BF16 form (bf16split.cuh), lo plane lo_words
+// 32-bit words after the hi plane
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
-                            long long xstride, int nb);
+                            long long xstride, int nb, long long lo_words = 0);
 // pass B writing whole grids: grid[b] = [N1][N2][N3] real-space values of band b (register sizes only)
 void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb);
 // fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
@@ -115,6 +117,7 @@ struct ChunkContract {
 struct ContractSource {
   const float2 *X = nullptr;
   long long xstride = 0;
+  long long xrows = 0;  // split form (tensor-core contraction): rows per plane of X
   const float2 *grid = nullptr;
   long long n3d = 0, r0 = 0, npts = 0;
   int nband = 1;
@@ -161,7 +164,8 @@ void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const
 // x-axis transform of each plane j of nb bands, then X[b][x_off + p] = u(point p) exp(i k.path_p) for
 // the segments of plane j (segs sorted by plane; plane_start[N2+1])
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
-                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb);
+                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb,
+                       long long lo_words = 0);
 // P[(band_base + b)*Ptot + o] = sum over c < col[o].y of partial[b][col[o].x + c*col[o].z]: the
 // chunks of column o's site, in chunk order
 void launch_chunk_reduce(const float2 *partial, int ptot, const int4 *col, float2 *P, int Ptot, int nb,
@@ -277,6 +281,12 @@ void launch_aug_a(const float2 *P, int Pt, const float2 *WP, int Pw, int nb, int
 void launch_aug_b(const float2 *P, int Pt, const float2 *WP, int Pw, int nbtot, int b0, int nb, int nk,
                   const int *ptr, const int *col, const double2 *val, const int *pair, const double2 *phase,
                   int npairs, int Kc, int Kcpad, double2 *B64, float2 *B32);
+// val32[k][e] = val[e] (times phase[k][e_pair[e]] where e_pair[e] >= 0) in FP32, e < ne (zero from n on)
+void launch_aug_val32(const double2 *val, const int *e_pair, int n, int ne, const double2 *phase, int npairs, int nk,
+                      float2 *val32);
+// FP32 form for the batched contraction: val32 [nk][nent] = entries times their column's pair phase
+void launch_aug_b32(const float2 *P, int Pt, const float2 *WP, int Pw, int nbtot, int nb, int nk, const int *ptr,
+                    const int *col, const float2 *val32, int nent, int Kc, int Kcpad, float2 *B32);
 // out[bS][bR][k] = (complex double) S[k][bS][bR]
 void launch_to_host_layout(const float2 *S, int nk, int nbS, int nbR, double2 *out);
 // out[bR][k] = S[k][band][bR]

@@ -18,6 +18,7 @@
 // register-blocked complex product over (bands x lm channels).
 #include <cuda_runtime.h>
 
+#include "bf16split.cuh"
 #include "fft_tmpl.cuh"
 #include "kernels.h"
 
@@ -59,9 +60,11 @@ struct FastTest {
   float cn[3];   // site position in grid units
   float r2lo, r2hi;
   __device__ void init(const SiteDesc &s, const double *L, const int *N) {
+    // single precision throughout (every thread runs this; FP64 division is slow on this part)
     for (int a = 0; a < 3; a++) {
       cn[a] = (float)(s.coord[a] * N[a]);
-      for (int c = 0; c < 3; c++) lf[3 * a + c] = (float)(L[3 * a + c] / N[a]);
+      const float inv = 1.0f / (float)N[a];
+      for (int c = 0; c < 3; c++) lf[3 * a + c] = (float)L[3 * a + c] * inv;
     }
     const double r2 = s.R0 * s.R0;
     r2lo = (float)(r2 * (1.0 - 1e-4));
@@ -125,6 +128,7 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
                            float2 *__restrict__ phase) {
   __shared__ int warp_cnt[32];
   __shared__ int base_s;
+  __shared__ double invN[3];
   const SegFill sg = segs[blockIdx.x];
   const SiteDesc s = sites[sg.site];
   const SpeciesDev &sp = species[s.species];
@@ -134,15 +138,27 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   FastTest ft;
   ft.init(s, L, N);
-  if (threadIdx.x == 0) base_s = 0;
+  if (threadIdx.x == 0) {
+    base_s = 0;
+    for (int a = 0; a < 3; a++) invN[a] = 1.0 / N[a];
+  }
   __syncthreads();
   const int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1);
+  const int w2 = 2 * s.g[2] + 1;
   for (int start = 0; start < n; start += blockDim.x) {
     int q = start + threadIdx.x;
     int ijk[3];
     double path[3];
     bool in = q < n && slab_inside(s, ft, sg.jb, q, L, N);
-    if (in) slab_point(s, sg.jb, q, L, N, ijk, path);  // the exact displacement of an inside point
+    if (in) {
+      // the displacement of an inside point (its membership was decided exactly above)
+      ijk[0] = box_i(s, 0, q / w2);
+      ijk[1] = box_i(s, 1, sg.jb);
+      ijk[2] = box_i(s, 2, q % w2);
+      const double fr[3] = {ijk[0] * invN[0] - s.coord[0], ijk[1] * invN[1] - s.coord[1],
+                            ijk[2] * invN[2] - s.coord[2]};
+      s_to_cart(fr, L, path);
+    }
     unsigned m = __ballot_sync(0xffffffffu, in);
     if (lane == 0) warp_cnt[wid] = __popc(m);
     __syncthreads();
@@ -185,8 +201,7 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
       // Y_lm(theta, phi) of the displacement t without transcendental calls:
       // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
       // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
-      // (FP64 division is slow on this part: one reciprocal each for r and rho, and the
-      // recurrence divisors as constant multipliers; the table is rounded to FP32 after)
+      // (FP64 division is slow on this part: one reciprocal each for r and rho)
       double ct = 1.0, cp = 1.0, sp_ = 0.0;
       if (r != 0) {
         ct = t[2] * (1.0 / r);
@@ -197,44 +212,49 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
           sp_ = t[1] * irho;
         }
       }
-      double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+      // The channel values in single precision (the table is stored in single precision; the
+      // geometry above and the spline index below stay in double precision)
+      const float ctf = (float)ct, cpf = (float)cp, spf = (float)sp_;
+      const float stf = sqrtf(fmaxf(0.f, (float)(1.0 - ct * ct)));
       // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence:
       // P_l^m = ((2l-1) ct P_{l-1}^m - (l+m-1) P_{l-2}^m) / (l-m)
-      double P[4][4];
-      P[0][0] = 1.0;
-      for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * st * P[m - 1][m - 1];
-      for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ct * P[m][m];
-      P[2][0] = (3.0 * ct * P[1][0] - 1.0 * P[0][0]) * 0.5;
-      P[3][0] = (5.0 * ct * P[2][0] - 2.0 * P[1][0]) * (1.0 / 3.0);
-      P[3][1] = (5.0 * ct * P[2][1] - 3.0 * P[1][1]) * 0.5;
-      double er[4] = {1.0, cp, 0, 0}, ei[4] = {0.0, sp_, 0, 0};
+      float P[4][4];
+      P[0][0] = 1.f;
+      for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * stf * P[m - 1][m - 1];
+      for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ctf * P[m][m];
+      P[2][0] = (3.f * ctf * P[1][0] - 1.f * P[0][0]) * 0.5f;
+      P[3][0] = (5.f * ctf * P[2][0] - 2.f * P[1][0]) * (1.f / 3.f);
+      P[3][1] = (5.f * ctf * P[2][1] - 3.f * P[1][1]) * 0.5f;
+      float er[4] = {1.f, cpf, 0.f, 0.f}, ei[4] = {0.f, spf, 0.f, 0.f};
       for (int m = 2; m <= 3; m++) {
-        er[m] = er[m - 1] * cp - ei[m - 1] * sp_;
-        ei[m] = er[m - 1] * sp_ + ei[m - 1] * cp;
+        er[m] = er[m - 1] * cpf - ei[m - 1] * spf;
+        ei[m] = er[m - 1] * spf + ei[m - 1] * cpf;
       }
       // linear-grid spline interpolation (proj_interpolate, utils.c:461-475); x_j = rmax/size*j
       double xlast = sp.h * (sp.size - 1);
       int ind = (int)(r * sp.inv_h);
       if (ind > sp.size - 2) ind = sp.size - 2;
-      double dd = r - sp.h * ind;
-      double rad = 0.0;
+      const float dd = (float)(r - sp.h * ind);
+      const float ws = (float)wscale;
+      float rad = 0.f;
       int last_f = -1;
       for (int lm = 0; lm < sp.total; lm++) {
         int l = sp.lm_l[lm], mm = sp.lm_m[lm], fi = sp.lm_f[lm];
         if (fi != last_f) {
           const double *f = sp.f + (long long)fi * sp.size;
           const double *sb = sp.spl + (long long)fi * 3 * sp.size;
-          rad = r > xlast ? 0.0 : f[ind] + dd * (sb[ind] + dd * (sb[sp.size + ind] + dd * sb[2 * sp.size + ind]));
+          rad = r > xlast ? 0.f
+                          : (float)f[ind] + dd * ((float)sb[ind] + dd * ((float)sb[sp.size + ind] +
+                                                                          dd * (float)sb[2 * sp.size + ind]));
           last_f = fi;
         }
         int am = mm < 0 ? -mm : mm;
-        double plm = l <= 3 ? P[l][am] : 0.0;
+        float plm = l <= 3 ? P[l][am] : 0.f;
         // lm_coef carries the m < 0 factor of P_l^{-|m|} (utils.c:379-380)
-        double y = sp.lm_coef[lm] * plm * rad * wscale;
-        double cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
+        float y = (float)sp.lm_coef[lm] * plm * rad * ws;
+        float cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
         // conj(radial * Y_lm) * dV * V^-1/2
-        tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] =
-            make_float2((float)(y * cs), (float)(-y * sn));
+        tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] = make_float2(y * cs, -y * sn);
       }
       // exp(i k.path): the argument in units of pi reduced to [-1, 1] in double precision,
       // then the single-precision sincospi (the phase is stored in single precision)
@@ -268,7 +288,7 @@ __global__ void __launch_bounds__(256) k_fft_x_pick(const float2 *__restrict__ H
                                                     const float2 *__restrict__ tw1g,
                                                     const GatherSeg *__restrict__ segs,
                                                     const int *__restrict__ plane_start, int kq,
-                                                    float2 *__restrict__ X, long long xstride) {
+                                                    float2 *__restrict__ X, long long xstride, long long lo_words) {
   extern __shared__ float2 sm[];
   const int tile = g.N1 * g.N3;
   float2 *a = sm, *b = sm + tile, *tw1 = sm + 2 * tile;
@@ -285,23 +305,24 @@ __global__ void __launch_bounds__(256) k_fft_x_pick(const float2 *__restrict__ H
   __syncthreads();
   const float2 *u = block_fft_any<1, false>(a, b, r1, g.N3, 1, g.N3, tw1);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  float2 *xb = X + (long long)band * xstride;
   for (int si = plane_start[j] + warp; si < plane_start[j + 1]; si += nwarp) {
     const GatherSeg sg = segs[si];
     const float2 *ph = sg.phase + (long long)kq * sg.phase_stride;
-    for (int p = lane; p < sg.npts; p += 32) xb[sg.x_off + p] = cmul(u[sg.idx[p]], ph[p]);
+    for (int p = lane; p < sg.npts; p += 32)
+      put_picked(X, band, xstride, lo_words, (int)(sg.x_off + p), cmul(u[sg.idx[p]], ph[p]));
   }
 }
 
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
-                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb) {
+                       const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb,
+                       long long lo_words) {
   if (nb <= 0) return;
   size_t smem = sizeof(float2) * (2 * (size_t)g.N1 * g.N3 + g.N1);
   PAWPY_REQUIRE(smem <= 227 * 1024, "FFT tile does not fit in shared memory");
   allow_dynamic_smem((const void *)k_fft_x_pick, smem);
   dim3 grid(g.N2, nb);
   PAWPY_LAUNCH("fft_x_pick", k_fft_x_pick<<<grid, 256, smem, stream()>>>(H, g, r1, tw1, segs, plane_start, kq, X,
-                                                                        xstride));
+                                                                        xstride, lo_words));
   note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 

@@ -17,15 +17,17 @@
 // hi*hi + hi*lo + lo*hi are accumulated in FP32 in TMEM, drained every FLUSH K
 // blocks into FP32 running sums (as in tc_gemm.cu).
 //
-// Warp roles: warp 0 issues TMA copies (table planes; with picked rows also the
-// FP32 rows into a staging ring), warp 1 the MMAs, CONV converter warps write
-// the A planes (split to BF16, 64-byte swizzle) from the staging ring or from
-// the gathered grid values, and 4 warps drain the accumulators. Every wait is
-// bounded; a wait that runs out records a status word and the CTA winds down.
+// Warp roles: warp 0 issues TMA copies (table planes; with picked rows, which
+// pass B writes already split, also the A planes), warp 1 the MMAs, and 4 warps
+// drain the accumulators; for grid values, 8 converter warps gather them with
+// cp.async into a staging ring, apply the Bloch phase, split them and write the
+// A planes (64-byte swizzle). Every mbarrier wait is bounded; a wait that runs
+// out records a status word and the CTA winds down.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "bf16split.cuh"
 #include "kernels.h"
 #include "tc_ptx.cuh"
 
@@ -38,23 +40,30 @@ namespace {
 constexpr int STM = 128;     // rows per tile (TMEM lanes)
 constexpr int KPTS = 16;     // points per K block
 constexpr int KELEM = 32;    // BF16 elements per K block row (64 bytes)
-constexpr int STAGES = 4;    // A/B plane stages
-constexpr int STG = 4;       // FP32 staging stages (picked rows)
 constexpr int FLUSH = 4;     // K blocks per accumulation interval
 constexpr int DRAIN = 4;     // drain warps
 
+// GATHER = false: the picked rows are already split (bf16split.cuh), so a K block of A is
+// two TMA boxes and the pipeline is TMA -> MMA only (4-5 stages, two CTAs per SM).
+// GATHER = true: CONV converter warps gather the grid values with cp.async into a ring of
+// STG FP32 staging slots (STG - 1 K blocks in flight), apply the Bloch phase, split and
+// write the A planes of an MMA stage.
 template <int BN, bool GATHER>
 struct SphCfg {
-  static constexpr int CONV = GATHER ? 8 : 4;  // converter warps
+  static constexpr int CONV = GATHER ? 8 : 0;
   static constexpr int NTHREADS = 32 * (2 + CONV + DRAIN);
-  static constexpr int RPW = STM / CONV;       // rows per converter warp
-  static constexpr int A_PLANE = STM * 64;     // 8 KB
+  static constexpr int RPW = GATHER ? STM / CONV : 1;  // rows per converter warp
+  static constexpr int STAGES = GATHER ? 4 : (BN <= 48 ? 5 : 4);  // picked rows: two CTAs per SM
+  static constexpr int STG = GATHER ? 6 : 0;
+  static constexpr int A_PLANE = STM * 64;  // 8 KB
   static constexpr int B_PLANE = BN * 64;
   static constexpr int STAGE = 2 * A_PLANE + 2 * B_PLANE;
   static constexpr int STG_BYTES = STM * KPTS * 8;  // 16 KB of FP32 (re, im) pairs
-  static constexpr int SMEM = STAGES * STAGE + (GATHER ? 0 : STG * STG_BYTES) + 1024;
+  static constexpr int PH_BYTES = KPTS * 8;         // the slot's Bloch phases
+  static constexpr int SMEM = STAGES * STAGE + STG * (STG_BYTES + PH_BYTES) + 1024;
   static constexpr int TMEM_COLS = 2 * BN <= 64 ? 64 : 128;  // two accumulator sets
-  static constexpr int SETC = TMEM_COLS / 2;                      // columns between the sets
+  static constexpr int SETC = TMEM_COLS / 2;                  // columns between the sets
+  static constexpr int MIN_CTAS = GATHER ? 1 : 2;
 };
 
 // kind::f16 with BF16 inputs, FP32 accumulation, both operands K-major, M = 128, N = bn
@@ -63,32 +72,34 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int bn) {
          (static_cast<uint32_t>(STM >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
-  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
-
-__device__ __forceinline__ void split2(float2 v, uint32_t &hi, uint32_t &lo) {
-  const __nv_bfloat16 hr = __float2bfloat16_rn(v.x), hi_ = __float2bfloat16_rn(v.y);
-  const __nv_bfloat16 lr = __float2bfloat16_rn(v.x - __bfloat162float(hr));
-  const __nv_bfloat16 li = __float2bfloat16_rn(v.y - __bfloat162float(hi_));
-  hi = pack_bf16(hr, hi_);
-  lo = pack_bf16(lr, li);
-}
-
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 8-byte cp.async; src_bytes 0 fills the destination with zeros
+__device__ __forceinline__ void cpa8z(uint32_t dst, const void *src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void conv_barrier(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
 
 }  // namespace
 
 // grid (row tiles, sites); see the file comment. With GATHER, a row tile never
 // crosses a k-point (the Bloch phase of a point depends on the k-point).
+// tmA (picked rows): BF16 words, hi rows [0, arows), lo rows [arows, 2 arows).
 template <int BN, bool GATHER>
-__global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
-    k_tc_sphere(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int brows,
-                const TcSite *__restrict__ sites, ContractSource src, int nb, int *__restrict__ status) {
+__global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHER>::MIN_CTAS)
+    k_tc_sphere(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int arows,
+                int brows, const TcSite *__restrict__ sites, ContractSource src, int nb, int *__restrict__ status) {
   using C = SphCfg<BN, GATHER>;
+  constexpr int STAGES = C::STAGES;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long b_full[STAGES], conv_full[STAGES], mma_empty[STAGES];
-  __shared__ __align__(8) unsigned long long stg_full[STG], stg_empty[STG];
+  __shared__ __align__(8) unsigned long long full[STAGES], conv_full[STAGES], mma_empty[STAGES];
   __shared__ __align__(8) unsigned long long bar_accf[2], bar_acce[2], bar_drain;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
@@ -116,19 +127,16 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   const uint32_t stg_base = sbase + STAGES * C::STAGE;
+  const uint32_t ph_base = stg_base + C::STG * C::STG_BYTES;
   auto a_plane = [&](int s, int p) { return sbase + s * C::STAGE + p * C::A_PLANE; };
   auto b_plane = [&](int s, int p) { return sbase + s * C::STAGE + 2 * C::A_PLANE + p * C::B_PLANE; };
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
     for (int s = 0; s < STAGES; s++) {
-      mbar_init(smem_u32(&b_full[s]), 1);
-      mbar_init(smem_u32(&conv_full[s]), 32 * C::CONV);
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&conv_full[s]), GATHER ? 32 * C::CONV : 1);
       mbar_init(smem_u32(&mma_empty[s]), 1);
-    }
-    for (int s = 0; s < STG; s++) {
-      mbar_init(smem_u32(&stg_full[s]), 1);
-      mbar_init(smem_u32(&stg_empty[s]), 32 * C::CONV);
     }
     for (int s = 0; s < 2; s++) {
       mbar_init(smem_u32(&bar_accf[s]), 1);
@@ -154,11 +162,10 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
 
   if (warp == 0) {
     if (lane == 0 && nkb > 0) {
-      int last_b[STAGES], last_a[STG];
+      // TMA producer: table planes (and, for picked rows, the A planes) of each K block
+      int last[STAGES];
 #pragma unroll
-      for (int s = 0; s < STAGES; s++) last_b[s] = -1;
-#pragma unroll
-      for (int s = 0; s < STG; s++) last_a[s] = -1;
+      for (int s = 0; s < STAGES; s++) last[s] = -1;
       for (int i = 0; i < nkb; i++) {
         const int s = i % STAGES, r = i / STAGES;
         if (r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag)) {
@@ -166,30 +173,21 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
           break;
         }
         if (abort_flag) break;
-        const uint32_t bf = smem_u32(&b_full[s]);
-        mbar_expect_tx(bf, 2 * C::B_PLANE);
+        const uint32_t bf = smem_u32(&full[s]);
+        mbar_expect_tx(bf, 2 * C::B_PLANE + (GATHER ? 0 : 2 * C::A_PLANE));
         tma_load_2d(b_plane(s, 0), &tmB, bf, i * KELEM, st.b_row);
         tma_load_2d(b_plane(s, 1), &tmB, bf, i * KELEM, brows + st.b_row);
-        last_b[s] = r;
         if (!GATHER) {
-          const int t = i % STG, u = i / STG;
-          if (u > 0 && !mbar_wait(smem_u32(&stg_empty[t]), (u - 1) & 1, &abort_flag)) {
-            if (!abort_flag) fail(12);
-            break;
-          }
-          if (abort_flag) break;
-          const uint32_t af = smem_u32(&stg_full[t]);
-          mbar_expect_tx(af, C::STG_BYTES);
-          tma_load_2d(stg_base + t * C::STG_BYTES, &tmA, af, (int)(2 * (st.a_x + (long long)i * KPTS)), row0);
-          last_a[t] = u;
+          const int x = (int)(2 * (st.a_x + (long long)i * KPTS));
+          tma_load_2d(a_plane(s, 0), &tmA, bf, x, row0);
+          tma_load_2d(a_plane(s, 1), &tmA, bf, x, arows + row0);
         }
+        last[s] = r;
       }
       if (abort_flag) {
         // let the copies already issued land before the CTA's memory is released
         for (int s = 0; s < STAGES; s++)
-          if (last_b[s] >= 0) mbar_wait(smem_u32(&b_full[s]), last_b[s] & 1);
-        for (int s = 0; s < STG; s++)
-          if (last_a[s] >= 0) mbar_wait(smem_u32(&stg_full[s]), last_a[s] & 1);
+          if (last[s] >= 0) mbar_wait(smem_u32(&full[s]), last[s] & 1);
       }
     }
   } else if (warp == 1) {
@@ -208,8 +206,8 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
         const int iend = min(nkb, (q + 1) * FLUSH);
         for (; i < iend; i++) {
           const int s = i % STAGES, r = i / STAGES;
-          if (!mbar_wait(smem_u32(&b_full[s]), r & 1, &abort_flag) ||
-              !mbar_wait(smem_u32(&conv_full[s]), r & 1, &abort_flag)) {
+          if (!mbar_wait(smem_u32(&full[s]), r & 1, &abort_flag) ||
+              (GATHER && !mbar_wait(smem_u32(&conv_full[s]), r & 1, &abort_flag))) {
             if (!abort_flag) fail(14);
             stop = true;
             break;
@@ -233,56 +231,71 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, 1)
       }
       umma_commit(smem_u32(&bar_drain));
     }
-  } else if (warp < 2 + C::CONV) {
-    // converters: rows [cw RPW, (cw + 1) RPW); lane -> (row parity half, point p)
+  } else if (GATHER && warp < 2 + C::CONV) {
+    // converters: lane -> (row parity half, point p); rows cw RPW + 2 it + half. Every
+    // converter thread runs every iteration (the named barriers need all of them); after an
+    // abort the waits return at once and the conversions are skipped.
+    constexpr int NCT = 32 * C::CONV, STG = C::STG, D = STG - 1;
     const int cw = warp - 2, half = lane >> 4, p = lane & 15;
-    for (int i = 0; i < nkb; i++) {
-      const int s = i % STAGES, r = i / STAGES;
-      if (r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag)) {
-        if (!abort_flag) fail(15);
-        break;
-      }
-      float2 v[C::RPW / 2];
-      if (GATHER) {
-        const long long x = st.a_x + (long long)i * KPTS + p;
-        int cell = -1;
-        float2 ph = make_float2(0.f, 0.f);
-        if (x < src.npts) {
-          cell = __ldg(src.gcell + x);
-          ph = __ldg(src.gphase + kq * src.npts + x);
-        }
+    const float2 *gbase = src.grid + (src.r0 + row0) * src.n3d;
+    auto cell_of = [&](int i) {
+      const long long x = st.a_x + (long long)i * KPTS + p;
+      return (i < nkb && x < src.npts) ? __ldg(src.gcell + x) : -1;
+    };
+    int cell_next = cell_of(0);
+    auto issue = [&](int i) {
+      if (i < nkb) {
+        const int t = i % STG;
+        const int cell = cell_next;
+        cell_next = cell_of(i + 1);
+        const uint32_t slot = stg_base + t * C::STG_BYTES;
 #pragma unroll
         for (int it = 0; it < C::RPW / 2; it++) {
           const int row = cw * C::RPW + 2 * it + half;
-          float2 g = make_float2(0.f, 0.f);
-          if (cell >= 0 && row < nrows) g = __ldg(src.grid + (src.r0 + row0 + row) * src.n3d + cell);
-          v[it] = make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x);
+          const bool ok = cell >= 0 && row < nrows;
+          const float2 *g = ok ? gbase + (long long)row * src.n3d + cell : src.grid;
+          cpa8z(slot + (row * KPTS + p) * 8, g, ok ? 8 : 0);
         }
-      } else {
-        const int t = i % STG, u = i / STG;
-        if (!mbar_wait(smem_u32(&stg_full[t]), u & 1, &abort_flag)) {
-          if (!abort_flag) fail(16);
-          break;
+        if (cw == 0 && half == 0) {
+          const long long x = st.a_x + (long long)i * KPTS + p;
+          const bool ok = x < src.npts;
+          cpa8z(ph_base + (t * KPTS + p) * 8, ok ? src.gphase + kq * src.npts + x : src.gphase, ok ? 8 : 0);
         }
+      }
+      cpa_commit();
+    };
+    for (int i = 0; i < D; i++) issue(i);
+    for (int i = 0; i < nkb; i++) {
+      const int s = i % STAGES, r = i / STAGES, t = i % STG;
+      issue(i + D);
+      cpa_wait<D>();
+      conv_barrier(NCT);  // block i's values are in slot t for every converter thread
+      bool ok = !abort_flag;
+      if (ok && r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag)) {
+        if (!abort_flag) fail(15);
+        ok = false;
+      }
+      if (ok) {
         const float2 *sg = reinterpret_cast<const float2 *>(smem_raw + (stg_base + t * C::STG_BYTES - raw));
+        const float2 ph = reinterpret_cast<const float2 *>(smem_raw + (ph_base - raw))[t * KPTS + p];
+        unsigned char *ah = smem_raw + (a_plane(s, 0) - raw), *al = smem_raw + (a_plane(s, 1) - raw);
 #pragma unroll
-        for (int it = 0; it < C::RPW / 2; it++) v[it] = sg[(cw * C::RPW + 2 * it + half) * KPTS + p];
-        mbar_arrive(smem_u32(&stg_empty[t]));
+        for (int it = 0; it < C::RPW / 2; it++) {
+          const int row = cw * C::RPW + 2 * it + half;
+          const float2 g = sg[row * KPTS + p];
+          uint32_t h, l;
+          split_bf16x2(make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x), h, l);
+          const uint32_t off = sw64_offset(row, p >> 2) + 4 * (p & 3);
+          *reinterpret_cast<uint32_t *>(ah + off) = h;
+          *reinterpret_cast<uint32_t *>(al + off) = l;
+        }
+        fence_async_smem();
+        mbar_arrive(smem_u32(&conv_full[s]));
       }
-      unsigned char *ah = smem_raw + (a_plane(s, 0) - raw), *al = smem_raw + (a_plane(s, 1) - raw);
-#pragma unroll
-      for (int it = 0; it < C::RPW / 2; it++) {
-        const int row = cw * C::RPW + 2 * it + half;
-        uint32_t h, l;
-        split2(v[it], h, l);
-        const uint32_t off = sw64_offset(row, p >> 2) + 4 * (p & 3);
-        *reinterpret_cast<uint32_t *>(ah + off) = h;
-        *reinterpret_cast<uint32_t *>(al + off) = l;
-      }
-      fence_async_smem();
-      mbar_arrive(smem_u32(&conv_full[s]));
+      conv_barrier(NCT);  // slot t is read by every converter thread before it is refilled
     }
-  } else {
+    cpa_wait<0>();
+  } else if (warp >= 2 + C::CONV) {
     // drain warps: TMEM lane quarter (warp % 4), all BN columns
     const int quarter = warp & 3;
     float acc[BN];
@@ -345,7 +358,7 @@ __global__ void k_tc_tables(const TcTable *__restrict__ tabs, int brows, long lo
   if (c < t.total && p >= 0 && p < t.npts) v = __ldg(t.tab + (long long)c * t.npts + p);
   const float2 e = (n & 1) ? make_float2(v.y, v.x) : make_float2(v.x, -v.y);
   uint32_t h, l;
-  split2(e, h, l);
+  split_bf16x2(e, h, l);
   const long long off = (long long)(t.b_row + n) * lb + 2LL * j;
   *reinterpret_cast<uint32_t *>(planes + off) = h;
   *reinterpret_cast<uint32_t *>(planes + (long long)brows * lb + off) = l;
@@ -368,7 +381,7 @@ void launch_tc_tables(const TcTable *tabs_dev, int nsites, int max_nkb, int bn, 
 namespace {
 
 template <int BN, bool GATHER>
-void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int brows, const TcSite *sites, int nsites,
+void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int arows, int brows, const TcSite *sites, int nsites,
                const ContractSource &src, int nb, int *st) {
   using C = SphCfg<BN, GATHER>;
   allow_dynamic_smem((const void *)k_tc_sphere<BN, GATHER>, C::SMEM);
@@ -379,7 +392,7 @@ void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int brows, const Tc
   }
   dim3 grid(tiles, nsites);
   PAWPY_LAUNCH("sphere_contract_tc", (k_tc_sphere<BN, GATHER><<<grid, C::NTHREADS, C::SMEM, stream()>>>(
-                                         ma, mb, brows, sites, src, nb, st)));
+                                         ma, mb, arows, brows, sites, src, nb, st)));
 }
 
 }  // namespace
@@ -395,15 +408,19 @@ void launch_tc_sphere(const TcSite *sites_dev, int nsites, int bn, const void *p
   PAWPY_REQUIRE(bn == 32 || bn == 48 || bn == 64, "tensor-core contraction: table width must be 32, 48 or 64");
   const CUtensorMap mb = tensor_map_2d(const_cast<void *>(planes), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, lb,
                                        2LL * brows, lb * 2, KELEM, bn, CU_TENSOR_MAP_SWIZZLE_64B);
-  // picked rows as FP32 (re, im) pairs; points from xtot on read as zero
+  // picked rows in the split form: BF16 (re, im) words, hi plane rows [0, xrows), lo plane rows
+  // [xrows, 2 xrows); points from xtot on read as zero
   CUtensorMap ma = mb;
-  if (!gather)
-    ma = tensor_map_2d(const_cast<float2 *>(src.X), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 2 * std::max(1LL, xtot), nb,
-                       src.xstride * 8, 2 * KPTS, STM, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!gather) {
+    PAWPY_REQUIRE(src.xrows >= nb, "picked-point planes shorter than the batch");
+    ma = tensor_map_2d(const_cast<float2 *>(src.X), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, 2 * std::max(1LL, xtot),
+                       2 * src.xrows, src.xstride * 4, KELEM, STM, CU_TENSOR_MAP_SWIZZLE_64B);
+  }
+  const int arows = (int)src.xrows;
   int *st = device_status();
-#define PAWPY_TC_SPHERE(W)                                                 \
-  (gather ? tc_sphere<W, true>(ma, mb, brows, sites_dev, nsites, src, nb, st) \
-          : tc_sphere<W, false>(ma, mb, brows, sites_dev, nsites, src, nb, st))
+#define PAWPY_TC_SPHERE(W)                                                        \
+  (gather ? tc_sphere<W, true>(ma, mb, arows, brows, sites_dev, nsites, src, nb, st) \
+          : tc_sphere<W, false>(ma, mb, arows, brows, sites_dev, nsites, src, nb, st))
   if (bn == 32)
     PAWPY_TC_SPHERE(32);
   else if (bn == 48)
