@@ -15,8 +15,9 @@ __device__ __forceinline__ void split_bf16x2(float2 v, uint32_t &hi, uint32_t &l
   lo = (uint32_t)__bfloat16_as_ushort(lr) | ((uint32_t)__bfloat16_as_ushort(lm) << 16);
 }
 
-// Picked-point rows: complex64 X[row][xstride] (lo_words == 0) or the split form, BF16
-// (re, im) words hi[row][xstride] with lo at hi + lo_words.
+// Picked-point rows: complex64 X[row][xstride] (lo_words == 0), or the split form in K blocks
+// of 16 points: BF16 (re, im) words hi[point / 16][row][point % 16], xstride words from one
+// block to the next, lo at hi + lo_words.
 __device__ __forceinline__ void put_picked(float2 *X, long long row, long long xstride, long long lo_words, int pos,
                                            float2 v) {
   if (lo_words == 0) {
@@ -24,7 +25,7 @@ __device__ __forceinline__ void put_picked(float2 *X, long long row, long long x
   } else {
     uint32_t h, l;
     split_bf16x2(v, h, l);
-    uint32_t *w = reinterpret_cast<uint32_t *>(X) + row * xstride + pos;
+    uint32_t *w = reinterpret_cast<uint32_t *>(X) + (long long)(pos >> 4) * xstride + row * 16 + (pos & 15);
     w[0] = h;
     w[lo_words] = l;
   }

@@ -882,6 +882,27 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   long long xtot = 0;
   int ptot = 0, max_total = 0;
   const int CHUNK = CHUNK_PTS;
+  // The tensor-core form reads K blocks of 16 points per site: there every site of the merged
+  // point space starts on a multiple of 16 (the gaps are zero in the picked rows).
+  int set_max_total = 0;
+  for (const SphereSet *S : sets) set_max_total = std::max(set_max_total, S->max_total);
+  const bool tc = sphere_tc_enabled() && set_max_total > 0;
+  std::vector<std::vector<long long>> site_x(sets.size());  // first point of each site
+  for (size_t i = 0; i < sets.size(); i++) {
+    const SphereSet &S = *sets[i];
+    site_x[i].resize(S.nsites);
+    for (int s = 0; s < S.nsites; s++) {
+      if (tc) {
+        site_x[i][s] = xtot;
+        xtot += (S.site_npts[s] + 15) / 16 * 16;
+      } else {
+        site_x[i][s] = xtot + S.site_pt[s];
+      }
+    }
+    if (!tc) xtot += S.npts;
+  }
+  const long long xspace = xtot;
+  xtot = 0;
   for (size_t i = 0; i < sets.size(); i++) {
     const SphereSet &S = *sets[i];
     for (int q = 0; q < S.nseg; q++) {
@@ -890,7 +911,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
       g.idx = S.idx.p + f.pt_off;
       g.phase = S.phase.p + f.pt_off;
       g.phase_stride = S.npts;
-      g.x_off = xtot + f.pt_off;
+      g.x_off = site_x[i][f.site] + (f.pt_off - f.site_pt);
       g.npts = f.npts;
       segs.push_back(g);
       plane_of.push_back(S.seg_plane[q]);
@@ -925,6 +946,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     }
     xtot += S.npts;
   }
+  xtot = xspace;
   std::vector<int> order(segs.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return plane_of[a] < plane_of[b]; });
@@ -986,7 +1008,6 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     mdev[i].upload(col.data(), col.size());
   }
   // tensor-core form: one site per z, table planes built once per call
-  const bool tc = sphere_tc_enabled() && max_total > 0;
   std::vector<TcSite> tsites;
   std::vector<TcTable> ttabs;
   int tc_bn = 0, tc_brows = 0, tc_maxkb = 0;
@@ -995,16 +1016,14 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   DevBuf<unsigned char> tc_planes;
   if (tc) {
     tc_bn = tc_sphere_width(max_total);
-    long long xo = 0;
     for (size_t i = 0; i < sets.size(); i++) {
       const SphereSet &S = *sets[i];
       for (int s = 0; s < S.nsites; s++) {
-        // K ranges start on a multiple of 4 points (16-byte TMA coordinates of the split rows)
-        const long long x_off = xo + S.site_pt[s];
-        const int lead = (int)(x_off & 3), n = S.site_npts[s];
+        const long long x_off = site_x[i][s];  // a multiple of 16
+        const int lead = 0, n = S.site_npts[s];
         TcSite ts;
-        ts.a_x = x_off - lead;
-        ts.nkb = (lead + n + 15) / 16;
+        ts.a_x = x_off;
+        ts.nkb = (n + 15) / 16;
         ts.b_row = (int)tsites.size() * tc_bn;
         ts.total = S.host[s].total;
         ts.ld = S.Ptot;
@@ -1020,7 +1039,6 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
         tsites.push_back(ts);
         ttabs.push_back(tt);
       }
-      xo += S.npts;
     }
     tc_brows = (int)tsites.size() * tc_bn;
     tc_lb = (long long)std::max(1, tc_maxkb) * 32;
@@ -1066,6 +1084,8 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     seg_j_d.upload(seg_j.data(), seg_j.size());
     gcell.alloc(std::max(1LL, xtot));
     gphase.alloc(std::max(1LL, xtot * d.nk));
+    // gaps of the aligned point space: no cell
+    PAWPY_CUDA(cudaMemsetAsync(gcell.p, 0xFF, sizeof(int) * std::max(1LL, xtot), stream()));
     launch_point_index(segs_d.p, seg_j_d.p, (int)sorted.size(), d.N[1], d.N[2], d.nk, xtot, gcell.p, gphase.p);
     src.grid = d.grid.p;
     src.n3d = (long long)d.N[0] * d.N[1] * d.N[2];
@@ -1078,7 +1098,20 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     src.xstride = xstride;
     src.xrows = split_x ? cbatch : 0;
   }
+  // split rows: K blocks of 16 points, cbatch rows each (bf16split.cuh); the last block of a site
+  // whose point count is not a multiple of 16 is zeroed before each batch's pick
   const long long lo_words = split_x ? cbatch * xstride : 0;
+  const long long pick_stride = split_x ? cbatch * 16 : xstride;
+  DevBuf<long long> tail_blocks;
+  int ntail = 0;
+  if (split_x) {
+    std::vector<long long> tb;
+    for (const TcSite &ts : tsites)
+      if (ts.nkb > 0) tb.push_back(ts.a_x / 16 + ts.nkb - 1);
+    ntail = (int)tb.size();
+    tail_blocks.alloc(std::max<size_t>(1, tb.size()));
+    tail_blocks.upload(tb.data(), tb.size());
+  }
   DevBuf<float2> partial(tc ? 1 : (size_t)cbatch * std::max(1, ptot));
   std::vector<PlaneGeom> geo(d.nk);
   std::vector<char> fast(d.nk);
@@ -1086,6 +1119,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   if (xtot == 0) return;
   for (long long r0 = 0; r0 < rows; r0 += cbatch) {
     const long long r1 = std::min(rows, r0 + cbatch);
+    if (split_x) launch_zero_picked_blocks(X.p, tail_blocks.p, ntail, cbatch * 16, (int)(r1 - r0), lo_words);
     for (int k = (int)(r0 / d.nband); (long long)k * d.nband < r1; k++) {
       DevKpt &q = d.kp[k];
       const PlaneGeom &g = geo[k];
@@ -1098,22 +1132,22 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
         // first row of the sub-batch (in 32-bit words of the hi plane for the split rows)
         const long long roff = (long long)k * d.nband + b0 - r0;
         float2 *xb = gather   ? nullptr
-                     : split_x ? reinterpret_cast<float2 *>(reinterpret_cast<uint32_t *>(X.p) + roff * xstride)
+                     : split_x ? reinterpret_cast<float2 *>(reinterpret_cast<uint32_t *>(X.p) + roff * 16)
                                : X.p + roff * xstride;
         if (early) {
           PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
           launch_fft_x_pick_fast(d.Hall.p + d.hoff[k] + (size_t)b0 * q.n1 * d.N[1] * d.N[2], g, plist, k, xb,
-                                 xstride, nb, lo_words);
+                                 pick_stride, nb, lo_words);
         } else if (gather) {
           // resident real-space wavefunctions: the contraction reads them directly
         } else if (fast[k]) {
           launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                                  H.p, nb);
-          launch_fft_x_pick_fast(H.p, g, plist, k, xb, xstride, nb, lo_words);
+          launch_fft_x_pick_fast(H.p, g, plist, k, xb, pick_stride, nb, lo_words);
         } else {
           launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, xstride, nb, lo_words);
+          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, pick_stride, nb, lo_words);
         }
       }
     }

@@ -142,6 +142,10 @@ struct TcTable {
   const float2 *tab = nullptr;
   int npts = 0, lead = 0, total = 0, nkb = 0, b_row = 0;
 };
+// Zeroes K blocks blocks[0..nblocks) of the split picked rows (rows [0, nb), both planes;
+// kb_words 32-bit words from one block to the next).
+void launch_zero_picked_blocks(float2 *X, const long long *blocks, int nblocks, long long kb_words, int nb,
+                               long long lo_words);
 // table width (2 x channels, padded) for the widest site: 32, 48 or 64
 int tc_sphere_width(int max_total);
 // BF16 hi/lo table planes [2][brows][lb] of every site

@@ -91,11 +91,14 @@ __device__ __forceinline__ void conv_barrier(int nthreads) {
 
 // grid (row tiles, sites); see the file comment. With GATHER, a row tile never
 // crosses a k-point (the Bloch phase of a point depends on the k-point).
-// tmA (picked rows): BF16 words, hi rows [0, arows), lo rows [arows, 2 arows).
+// tmA (picked rows): 64-byte rows of one K block and one row each, K block b and row r at
+// row b arows + r of the hi plane and aplane + b arows + r of the lo plane. Sites start on
+// a multiple of 16 points.
 template <int BN, bool GATHER>
 __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHER>::MIN_CTAS)
     k_tc_sphere(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int arows,
-                int brows, const TcSite *__restrict__ sites, ContractSource src, int nb, int *__restrict__ status) {
+                int aplane, int brows, const TcSite *__restrict__ sites, ContractSource src, int nb,
+                int *__restrict__ status) {
   using C = SphCfg<BN, GATHER>;
   constexpr int STAGES = C::STAGES;
   extern __shared__ unsigned char smem_raw[];
@@ -178,9 +181,10 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
         tma_load_2d(b_plane(s, 0), &tmB, bf, i * KELEM, st.b_row);
         tma_load_2d(b_plane(s, 1), &tmB, bf, i * KELEM, brows + st.b_row);
         if (!GATHER) {
-          const int x = (int)(2 * (st.a_x + (long long)i * KPTS));
-          tma_load_2d(a_plane(s, 0), &tmA, bf, x, row0);
-          tma_load_2d(a_plane(s, 1), &tmA, bf, x, arows + row0);
+          // K block (a_x / 16 + i): rows [row0, row0 + 128) of the block, hi then lo plane
+          const int y = (int)((st.a_x / KPTS + i) * (long long)arows) + row0;
+          tma_load_2d(a_plane(s, 0), &tmA, bf, 0, y);
+          tma_load_2d(a_plane(s, 1), &tmA, bf, 0, aplane + y);
         }
         last[s] = r;
       }
@@ -257,8 +261,9 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
           cpa8z(slot + (row * KPTS + p) * 8, g, ok ? 8 : 0);
         }
         if (cw == 0 && half == 0) {
+          // gaps between sites have cell -1 (and no phase): zero
           const long long x = st.a_x + (long long)i * KPTS + p;
-          const bool ok = x < src.npts;
+          const bool ok = cell >= 0;
           cpa8z(ph_base + (t * KPTS + p) * 8, ok ? src.gphase + kq * src.npts + x : src.gphase, ok ? 8 : 0);
         }
       }
@@ -364,6 +369,22 @@ __global__ void k_tc_tables(const TcTable *__restrict__ tabs, int brows, long lo
   *reinterpret_cast<uint32_t *>(planes + (long long)brows * lb + off) = l;
 }
 
+__global__ void k_zero_picked_blocks(uint32_t *__restrict__ X, const long long *__restrict__ blocks,
+                                     long long kb_words, int nb, long long lo_words) {
+  uint32_t *w = X + blocks[blockIdx.x] * kb_words;
+  for (int e = threadIdx.x; e < nb * 16; e += blockDim.x) {
+    w[e] = 0u;
+    w[lo_words + e] = 0u;
+  }
+}
+
+void launch_zero_picked_blocks(float2 *X, const long long *blocks, int nblocks, long long kb_words, int nb,
+                               long long lo_words) {
+  if (nblocks <= 0 || nb <= 0) return;
+  PAWPY_LAUNCH("pick_list", k_zero_picked_blocks<<<nblocks, 256, 0, stream()>>>(reinterpret_cast<uint32_t *>(X),
+                                                                              blocks, kb_words, nb, lo_words));
+}
+
 int tc_sphere_width(int max_total) {
   if (max_total > 32) throw Error(ERR_UNSUPPORTED, "more than 32 projector channels on one site");
   return max_total <= 16 ? 32 : max_total <= 24 ? 48 : 64;
@@ -381,8 +402,8 @@ void launch_tc_tables(const TcTable *tabs_dev, int nsites, int max_nkb, int bn, 
 namespace {
 
 template <int BN, bool GATHER>
-void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int arows, int brows, const TcSite *sites, int nsites,
-               const ContractSource &src, int nb, int *st) {
+void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int arows, int aplane, int brows, const TcSite *sites,
+               int nsites, const ContractSource &src, int nb, int *st) {
   using C = SphCfg<BN, GATHER>;
   allow_dynamic_smem((const void *)k_tc_sphere<BN, GATHER>, C::SMEM);
   int tiles = ceil_div(nb, STM);
@@ -392,7 +413,7 @@ void tc_sphere(const CUtensorMap &ma, const CUtensorMap &mb, int arows, int brow
   }
   dim3 grid(tiles, nsites);
   PAWPY_LAUNCH("sphere_contract_tc", (k_tc_sphere<BN, GATHER><<<grid, C::NTHREADS, C::SMEM, stream()>>>(
-                                         ma, mb, arows, brows, sites, src, nb, st)));
+                                         ma, mb, arows, aplane, brows, sites, src, nb, st)));
 }
 
 }  // namespace
@@ -408,19 +429,22 @@ void launch_tc_sphere(const TcSite *sites_dev, int nsites, int bn, const void *p
   PAWPY_REQUIRE(bn == 32 || bn == 48 || bn == 64, "tensor-core contraction: table width must be 32, 48 or 64");
   const CUtensorMap mb = tensor_map_2d(const_cast<void *>(planes), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, lb,
                                        2LL * brows, lb * 2, KELEM, bn, CU_TENSOR_MAP_SWIZZLE_64B);
-  // picked rows in the split form: BF16 (re, im) words, hi plane rows [0, xrows), lo plane rows
-  // [xrows, 2 xrows); points from xtot on read as zero
+  // picked rows in the split form, K blocks of 16 points (bf16split.cuh): xrows rows per block,
+  // xtot / 16 blocks per plane; blocks from xtot / 16 on read as zero
   CUtensorMap ma = mb;
+  long long aplane = 0;
   if (!gather) {
-    PAWPY_REQUIRE(src.xrows >= nb, "picked-point planes shorter than the batch");
-    ma = tensor_map_2d(const_cast<float2 *>(src.X), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, 2 * std::max(1LL, xtot),
-                       2 * src.xrows, src.xstride * 4, KELEM, STM, CU_TENSOR_MAP_SWIZZLE_64B);
+    PAWPY_REQUIRE(src.xrows >= nb && xtot % KPTS == 0, "picked-point blocks do not match the batch");
+    aplane = xtot / KPTS * src.xrows;
+    PAWPY_REQUIRE(2 * aplane < (1LL << 31), "picked-point planes too large for 32-bit box coordinates");
+    ma = tensor_map_2d(const_cast<float2 *>(src.X), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, KELEM, 2 * aplane, 64, KELEM,
+                       STM, CU_TENSOR_MAP_SWIZZLE_64B);
   }
   const int arows = (int)src.xrows;
   int *st = device_status();
 #define PAWPY_TC_SPHERE(W)                                                        \
-  (gather ? tc_sphere<W, true>(ma, mb, arows, brows, sites_dev, nsites, src, nb, st) \
-          : tc_sphere<W, false>(ma, mb, arows, brows, sites_dev, nsites, src, nb, st))
+  (gather ? tc_sphere<W, true>(ma, mb, arows, (int)aplane, brows, sites_dev, nsites, src, nb, st) \
+          : tc_sphere<W, false>(ma, mb, arows, (int)aplane, brows, sites_dev, nsites, src, nb, st))
   if (bn == 32)
     PAWPY_TC_SPHERE(32);
   else if (bn == 48)
