@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--rate", type=float, default=200.0, help="mean request arrival rate (1/s)")
     ap.add_argument("--slots", type=int, default=4, help="requests in flight at once")
     ap.add_argument("--budget-gb", type=float, default=100.0, help="device-memory admission budget")
+    ap.add_argument("--cpu-report", action="store_true",
+                    help="the reference algorithm's CPU port per workload (0, 1, 2): defect setup, overlaps, "
+                         "pairs/s and its error against FP64, one JSON line each (no GPU work)")
     ap.add_argument("--precision-report", action="store_true",
                     help="overlap matrix of the workload in every precision against FP64 (error and time)")
     return ap.parse_args()
@@ -643,8 +646,38 @@ def measure(args, cfg, rank, world, local, pg, with_cpu):
     return res, work, acc, cpu
 
 
+def run_cpu_report(args):
+    """Per workload: the oracle port (the reference's algorithm, all host threads) on a band sample
+    (the whole 8-atom workload; 8 defect x 32 basis bands at every k-point of the others), the
+    band-independent setup timed once and the per-band phases extrapolated to the full workload,
+    and the error of its overlaps (single-precision pseudo overlap as the reference computes it,
+    FP64 PAW terms) against the FP64 evaluation of the same sample."""
+    for cfg in (0, 1, 2):
+        work = make_workload(cfg, None, None)
+        work = work + (site_lists(work[1], work[2], work[3]),)
+        w, basis_s, defect_s, cr, bd, dd, lists = work
+        full = cfg == 0
+        smp = OracleSample(work, dd["nband"] if full else 8, bd["nband"] if full else 32, seed=31 + cfg)
+        smp.run()
+        smp.run(fixed_once=True)
+        pps, secs = smp.extrapolate()
+        w_, NS, NR = smp.timings, dd["nband"], bd["nband"]
+        ns, nr = len(smp.sb), len(smp.rb)
+        setup = (sum(smp.fixed.values()) + (w_.get("project", 0.0) + w_.get("wp_defect", 0.0)) * NS / ns
+                 + w_.get("wp_basis", 0.0) * NR / nr)
+        overlaps = w_["pairs"] * (NS * NR) / (ns * nr)
+        err = np.abs(smp.p32 + smp.comp - smp.truth())
+        print(json.dumps(dict(workload=cfg, pairs=NS * NR * len(bd["coeffs"]), cores=threads_used(),
+                              defect_setup_s=setup, overlaps_s=overlaps, pairs_per_s=pps, extrapolated_s=secs,
+                              max_abs_err_vs_fp64=float(err.max()), rms_abs_err_vs_fp64=float(np.sqrt((err ** 2).mean())),
+                              sample=smp.describe())), flush=True)
+
+
 def main():
     args = parse()
+    if args.cpu_report:
+        run_cpu_report(args)
+        return
     rank, world, local, pg = dist_init(args.gpus)
     if args.precision_report:
         run_precision_report(args, local)

@@ -867,6 +867,11 @@ static void transform_planes_early(DevWF &d) {
   d.h_ready = true;
 }
 
+// values per k-point of the resident real-space wavefunctions (bands in tiles of 16)
+static size_t grid_kstride(const DevWF &d) {
+  return (size_t)ceil_div(d.nband, 16) * 16 * d.N[0] * d.N[1] * d.N[2];
+}
+
 static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
                           const std::vector<float2 *> &outs) {
   HostPhase hp("project_bands");
@@ -1067,8 +1072,9 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   const long long rows = (long long)d.nk * d.nband;
   // (the tensor-core form keeps no partial sums and reads the rows once: a larger batch, fewer launches)
   const long long xcap = tc ? kTcPickBatchBytes : (2LL << 30);
-  const long long cbatch =
-      std::min({rows, 32768LL, std::max<long long>(fbatch, xcap / std::max(1LL, per_row))});
+  long long cbatch = std::min({rows, 32768LL, std::max<long long>(fbatch, xcap / std::max(1LL, per_row))});
+  // the gathered tensor-core form reads whole tiles of 16 bands: batches start on a k-point
+  if (tc && gather) cbatch = std::min(rows, std::max(1LL, 32768LL / d.nband) * d.nband);
   const bool split_x = tc && !gather;  // pass B writes the split BF16 rows the tensor cores read
   const bool early = d.h_ready && !d.grid_ready;
   DevBuf<float2> H(d.grid_ready || early ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
@@ -1084,11 +1090,16 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     seg_j_d.upload(seg_j.data(), seg_j.size());
     gcell.alloc(std::max(1LL, xtot));
     gphase.alloc(std::max(1LL, xtot * d.nk));
-    // gaps of the aligned point space: no cell
+    // gaps of the aligned point space: no cell, and a zero phase (the tensor-core form reads a
+    // valid grid row there, zeroed by the phase)
     PAWPY_CUDA(cudaMemsetAsync(gcell.p, 0xFF, sizeof(int) * std::max(1LL, xtot), stream()));
+    PAWPY_CUDA(cudaMemsetAsync(gphase.p, 0, sizeof(float2) * std::max(1LL, xtot * d.nk), stream()));
     launch_point_index(segs_d.p, seg_j_d.p, (int)sorted.size(), d.N[1], d.N[2], d.nk, xtot, gcell.p, gphase.p);
     src.grid = d.grid.p;
     src.n3d = (long long)d.N[0] * d.N[1] * d.N[2];
+    src.gstride = (long long)grid_kstride(d);
+    src.gkp = d.nk;
+    src.grows = (long long)d.nk * src.gstride / 16;
     src.npts = xtot;
     src.nband = d.nband;
     src.gcell = gcell.p;
@@ -1192,7 +1203,7 @@ static bool build_grids(DevWF &d) {
     geo[k] = g;
     maxn1 = std::max(maxn1, q.n1);
   }
-  d.grid.alloc((size_t)d.nk * d.nband * n3d);
+  d.grid.alloc((size_t)d.nk * grid_kstride(d));
   const long long hband = (long long)maxn1 * d.N[1] * d.N[2] * (long long)sizeof(float2);
   const int fbatch = (int)std::max(1LL, std::min<long long>(d.nband, kFftBatchBytes / std::max(1LL, hband)));
   DevBuf<float2> H((size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
@@ -1202,7 +1213,7 @@ static bool build_grids(DevWF &d) {
       const int nb = std::min(fbatch, d.nband - b0);
       launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
                              H.p, nb);
-      launch_fft_x_grid(H.p, geo[k], d.grid.p + ((size_t)k * d.nband + b0) * n3d, nb);
+      launch_fft_x_grid(H.p, geo[k], d.grid.p + (size_t)k * grid_kstride(d), b0, nb);
     }
   }
   d.grid_ready = true;

@@ -423,10 +423,11 @@ __global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ 
 // Pass B writing whole grids (resident real-space wavefunctions): grid
 // (ceil(nb / BPC) band groups, N2 planes j), FT threads in BPC groups of TPB,
 // one band each; the first-axis transform of plane j goes straight from
-// registers to grid[b][(x N2 + j) N3 + z].
+// registers to the grid of band bb = b0 + b in tiles of 16 bands:
+// grid[((bb / 16) N1 N2 N3 + (x N2 + j) N3 + z) 16 + bb % 16] (grid_value_index).
 template <int N1, int N3, int T1>
 __global__ void __launch_bounds__(FT) k_xgrid(const float2 *__restrict__ H, int nb, PlaneGeom g,
-                                              float2 *__restrict__ grid) {
+                                              float2 *__restrict__ grid, int b0) {
   constexpr int L1 = N1 / T1;
   constexpr int TPB = 32 * ((N3 * T1 + 31) / 32) < FT ? 32 * ((N3 * T1 + 31) / 32) : FT;
   constexpr int BPC = FT / TPB;
@@ -439,7 +440,8 @@ __global__ void __launch_bounds__(FT) k_xgrid(const float2 *__restrict__ H, int 
   const int pstride = g.N2 * N3;
   const int h = lane / LPW, c = lane % LPW;
   const float2 *hb = H + ((long long)b * n1 * g.N2 + j) * N3;
-  float2 *gb = grid + (long long)b * N1 * g.N2 * N3 + (long long)j * N3;
+  const int bb = b0 + b;
+  float2 *gb = grid + ((long long)(bb >> 4) * N1 * g.N2 * N3 + (long long)j * N3) * 16 + (bb & 15);
   for (int g0 = warp * LPW; g0 < N3; g0 += (TPB / 32) * LPW) {
     const int z = g0 + c;
     const bool ok = z < N3;
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(FT) k_xgrid(const float2 *__restrict__ H, int 
     if (ok) {
       const int o = L1 * reg::bitrev(h, T1);
 #pragma unroll
-      for (int k = 0; k < L1; k++) gb[(long long)(o + k) * pstride + z] = x[k];
+      for (int k = 0; k < L1; k++) gb[((long long)(o + k) * pstride + z) * 16] = x[k];
     }
   }
 }

@@ -32,7 +32,7 @@ DirectFn find_direct(int n1, int n3, int *bpc) {
 
 }  // namespace
 
-using GridFn = void (*)(const float2 *, int, PlaneGeom, float2 *);
+using GridFn = void (*)(const float2 *, int, PlaneGeom, float2 *, int);
 
 GridFn find_xgrid(int n1, int n3, int *bpc) {
 #define X(a, b)                                 \
@@ -86,13 +86,13 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 
-void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb) {
+void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int b0, int nb) {
   if (nb <= 0) return;
   int bpc = 1;
   GridFn fn = find_xgrid(g.N1, g.N3, &bpc);
   PAWPY_REQUIRE(fn, "no register FFT for this grid");
   dim3 grd(ceil_div(nb, bpc), g.N2);
-  PAWPY_LAUNCH("fft_x_grid", fn<<<grd, FT, 0, stream()>>>(H, nb, g, grid));
+  PAWPY_LAUNCH("fft_x_grid", fn<<<grd, FT, 0, stream()>>>(H, nb, g, grid, b0));
   note_work("fft_x_grid", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 

@@ -49,8 +49,13 @@ struct PickList {
 // 32-bit words after the hi plane
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
                             long long xstride, int nb, long long lo_words = 0);
-// pass B writing whole grids: grid[b] = [N1][N2][N3] real-space values of band b (register sizes only)
-void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int nb);
+// Resident real-space wavefunctions of one k-point, bands in tiles of 16: the value of band b at
+// cell c (= (x N2 + y) N3 + z) is at grid_value_index(b, c, n3d).
+__host__ __device__ inline long long grid_value_index(int b, long long cell, long long n3d) {
+  return ((long long)(b >> 4) * n3d + cell) * 16 + (b & 15);
+}
+// pass B writing whole grids of bands [b0, b0 + nb) of one k-point (register sizes only)
+void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int b0, int nb);
 // fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
 void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).
@@ -118,8 +123,9 @@ struct ContractSource {
   const float2 *X = nullptr;
   long long xstride = 0;
   long long xrows = 0;  // split form (tensor-core contraction): rows per plane of X
-  const float2 *grid = nullptr;
-  long long n3d = 0, r0 = 0, npts = 0;
+  const float2 *grid = nullptr;  // k-point kq at grid + kq gstride, grid_value_index layout
+  long long n3d = 0, r0 = 0, npts = 0, gstride = 0;
+  long long grows = 0, gkp = 0;  // rows of 16 bands over all gkp k-points (gkp gstride / 16)
   int nband = 1;
   const int *gcell = nullptr;
   const float2 *gphase = nullptr;

@@ -412,8 +412,10 @@ __global__ void __launch_bounds__(TC) k_contract_staged(const ChunkContract *__r
       float2 *dst = xs + ((long long)buf * TP + pl) * XS;
       const int rfirst = warp * (32 / TP) + rsub;
       if (GATHER) {
-        const float2 *g = src.grid + (src.r0 + row0) * src.n3d + src.gcell[xo];
-        for (int r = rfirst; r < nrows; r += RSTEP) cpa8(dst + r, g + (long long)r * src.n3d);
+        const float2 *gk = src.grid + kq * src.gstride;
+        const int b0 = (int)(src.r0 + row0 - kq * src.nband);
+        const int cell = src.gcell[xo];
+        for (int r = rfirst; r < nrows; r += RSTEP) cpa8(dst + r, gk + grid_value_index(b0 + r, cell, src.n3d));
       } else {
         const float2 *x = src.X + (long long)row0 * src.xstride + xo;
         for (int r = rfirst; r < nrows; r += RSTEP) cpa8(dst + r, x + (long long)r * src.xstride);
