@@ -867,6 +867,9 @@ static void transform_planes_early(DevWF &d) {
   d.h_ready = true;
 }
 
+// the k-point is Gamma: its Bloch phases are all exactly 1
+static bool kpoint_is_gamma(const DevKpt &q) { return q.kfrac[0] == 0.0 && q.kfrac[1] == 0.0 && q.kfrac[2] == 0.0; }
+
 // values per k-point of the resident real-space wavefunctions (bands in tiles of 16)
 static size_t grid_kstride(const DevWF &d) {
   return (size_t)ceil_div(d.nband, 16) * 16 * d.N[0] * d.N[1] * d.N[2];
@@ -994,7 +997,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   plist.max_plane_pts = max_plane_pts;
   for (size_t i = 0; i < sets.size(); i++)
     PAWPY_REQUIRE(sets[i]->nkp == d.nk, "sphere tables and wavefunction differ in k-points");
-  launch_flatten_pick(segs_d.p, seg_base_d.p, (int)sorted.size(), d.nk, plist);
+  launch_flatten_pick(segs_d.p, seg_base_d.p, (int)sorted.size(), d.nk, d.N[2], plist);
   DevBuf<int> pstart_d(pstart.size());
   pstart_d.upload(pstart.data(), pstart.size());
   DevBuf<ChunkContract> ch_d(std::max<size_t>(1, chunks.size()));
@@ -1066,7 +1069,19 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   // launch covers several k-points (the tables do not depend on k; the Bloch
   // phase is applied at the pick); picked points and partial sums of up to 2 GiB.
   // A wavefunction held in real space skips X: the contraction gathers its grid values.
-  const bool gather = d.grid_ready;
+  std::vector<PlaneGeom> geo(d.nk);
+  std::vector<char> fast(d.nk);
+  bool all_fast = true;
+  for (int k = 0; k < d.nk; k++) {
+    fast[k] = plane_geom(d, k, geo[k]);
+    all_fast = all_fast && fast[k];
+  }
+  // The tensor-core form of a wavefunction not held in real space picks the sphere points into
+  // rows in pass B; with PAWPY_GPU_DEFECT_GRID=1 pass B writes the real-space grids of the batch
+  // instead (band-tiled, as a prepared basis holds them) and the contraction gathers from them.
+  const char *dg_env = getenv("PAWPY_GPU_DEFECT_GRID");
+  const bool dgrid_mode = tc && !d.grid_ready && all_fast && !generic_fft_forced() && dg_env && dg_env[0] == '1';
+  const bool gather = d.grid_ready || dgrid_mode;
   const long long xstride = (xtot + 3) / 4 * 4;
   const long long per_row = ((gather ? 0 : xstride) + (tc ? 0 : ptot)) * (long long)sizeof(float2);
   const long long rows = (long long)d.nk * d.nband;
@@ -1078,6 +1093,26 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   const bool split_x = tc && !gather;  // pass B writes the split BF16 rows the tensor cores read
   const bool early = d.h_ready && !d.grid_ready;
   DevBuf<float2> H(d.grid_ready || early ? 0 : (size_t)fbatch * maxn1 * d.N[1] * d.N[2]);
+  DevBuf<float2> dgrid;
+  if (dgrid_mode && xtot > 0) {
+    dgrid.alloc((size_t)d.nk * grid_kstride(d));
+    for (int k = 0; k < d.nk; k++) {
+      DevKpt &q = d.kp[k];
+      float2 *gk = dgrid.p + (size_t)k * grid_kstride(d);
+      if (early) {
+        PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
+        launch_fft_x_grid(d.Hall.p + d.hoff[k], geo[k], gk, 0, d.nband);
+        continue;
+      }
+      for (int b0 = 0; b0 < d.nband; b0 += fbatch) {
+        const int nb = std::min(fbatch, d.nband - b0);
+        launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
+                               H.p, nb);
+        launch_fft_x_grid(H.p, geo[k], gk, b0, nb);
+      }
+    }
+  }
+  const float2 *grid_src = dgrid_mode ? dgrid.p : d.grid.p;
   DevBuf<float2> X(gather ? 1 : (size_t)cbatch * std::max(1LL, xstride));
   ContractSource src;
   DevBuf<int> gcell, seg_j_d;
@@ -1090,16 +1125,13 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     seg_j_d.upload(seg_j.data(), seg_j.size());
     gcell.alloc(std::max(1LL, xtot));
     gphase.alloc(std::max(1LL, xtot * d.nk));
-    // gaps of the aligned point space: no cell, and a zero phase (the tensor-core form reads a
-    // valid grid row there, zeroed by the phase)
+    // gaps of the aligned point space: no cell and a zero phase
     PAWPY_CUDA(cudaMemsetAsync(gcell.p, 0xFF, sizeof(int) * std::max(1LL, xtot), stream()));
     PAWPY_CUDA(cudaMemsetAsync(gphase.p, 0, sizeof(float2) * std::max(1LL, xtot * d.nk), stream()));
     launch_point_index(segs_d.p, seg_j_d.p, (int)sorted.size(), d.N[1], d.N[2], d.nk, xtot, gcell.p, gphase.p);
-    src.grid = d.grid.p;
+    src.grid = grid_src;
     src.n3d = (long long)d.N[0] * d.N[1] * d.N[2];
     src.gstride = (long long)grid_kstride(d);
-    src.gkp = d.nk;
-    src.grows = (long long)d.nk * src.gstride / 16;
     src.npts = xtot;
     src.nband = d.nband;
     src.gcell = gcell.p;
@@ -1124,9 +1156,6 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     tail_blocks.upload(tb.data(), tb.size());
   }
   DevBuf<float2> partial(tc ? 1 : (size_t)cbatch * std::max(1, ptot));
-  std::vector<PlaneGeom> geo(d.nk);
-  std::vector<char> fast(d.nk);
-  for (int k = 0; k < d.nk; k++) fast[k] = plane_geom(d, k, geo[k]);
   if (xtot == 0) return;
   for (long long r0 = 0; r0 < rows; r0 += cbatch) {
     const long long r1 = std::min(rows, r0 + cbatch);
@@ -1145,16 +1174,16 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
         float2 *xb = gather   ? nullptr
                      : split_x ? reinterpret_cast<float2 *>(reinterpret_cast<uint32_t *>(X.p) + roff * 16)
                                : X.p + roff * xstride;
-        if (early) {
+        if (gather) {
+          // real-space wavefunctions (resident, or written above): the contraction reads them
+        } else if (early) {
           PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.h_ev[k], 0));
           launch_fft_x_pick_fast(d.Hall.p + d.hoff[k] + (size_t)b0 * q.n1 * d.N[1] * d.N[2], g, plist, k, xb,
-                                 pick_stride, nb, lo_words);
-        } else if (gather) {
-          // resident real-space wavefunctions: the contraction reads them directly
+                                 pick_stride, nb, lo_words, kpoint_is_gamma(q));
         } else if (fast[k]) {
           launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                                  H.p, nb);
-          launch_fft_x_pick_fast(H.p, g, plist, k, xb, pick_stride, nb, lo_words);
+          launch_fft_x_pick_fast(H.p, g, plist, k, xb, pick_stride, nb, lo_words, kpoint_is_gamma(q));
         } else {
           launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
@@ -1442,6 +1471,13 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   build_spheres(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, R.lattice, R.N, R.vol, R.kp, R.rec);
   ps.WP_S.alloc(std::max<size_t>(1, (size_t)S.nk * S.nband * ps.sm_NR.Ptot));
   ps.WP_R.alloc(std::max<size_t>(1, (size_t)R.nk * R.nband * ps.sm_NS.Ptot));
+  // The N_RS pair matrices depend only on the species and positions: their radial integrals run
+  // on the auxiliary stream (behind the first FFT pass at most) and the host assembles them
+  // while the projections below run on the device.
+  {
+    OnStream on(aux_stream());
+    pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
+  }
   // one FFT pass per wavefunction: pending <p|psi> and the smoothed-partial-wave projections together
   for (int side = 0; side < 2; side++) {
     DevWF &W = side == 0 ? S : R;
@@ -1460,7 +1496,6 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
     if (!sets.empty()) project_bands(W, sets, outs);
     if (!W.p_ready) W.p_ready = true;  // a prepared, shared basis is only read
   }
-  pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
   publish_pair_matrices(ps, wf_R, wf_S);
   free_wave_projections(wf_R);
   free_wave_projections(wf_S);

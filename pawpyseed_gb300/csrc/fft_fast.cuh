@@ -257,11 +257,11 @@ __global__ void __launch_bounds__(FT) k_planes_direct(const float2 *__restrict__
 // the plane's H rows of the current and the next band (cp.async), tile
 // [N1][LD] the transformed plane and, when the plane has at most pts_cap
 // points, a copy of its pick list (the same for every band).
-// The pick of one plane: value at tile cell times the point's Bloch phase, to its position in
-// the picked-point row of band b. The lists are read from global memory (L2) U points per
-// thread at a time, all loads in flight before the stores.
-template <int N3, int LD>
-__device__ __forceinline__ void pick_plane(const float2 *tile, const int *__restrict__ cell,
+// The pick of one plane: value at tile offset pto (row * LD + column of the transformed plane)
+// times the point's Bloch phase (phase == nullptr: the k-point is Gamma, the phase is 1), to its
+// position in the picked-point row of band b. The lists are read from global memory (L2) U
+// points per thread at a time, all loads in flight before the stores.
+__device__ __forceinline__ void pick_plane(const float2 *tile, const int *__restrict__ pto,
                                            const int *__restrict__ xo, const float2 *__restrict__ phase, int npj,
                                            int t0, int nt, float2 *X, long long b, long long xstride,
                                            long long lo_words) {
@@ -273,18 +273,15 @@ __device__ __forceinline__ void pick_plane(const float2 *tile, const int *__rest
     for (int u = 0; u < U; u++) {
       const int q = q0 + u * nt;
       if (q < npj) {
-        c[u] = __ldg(cell + q);
+        c[u] = __ldg(pto + q);
         o[u] = __ldg(xo + q);
-        f[u] = __ldg(phase + q);
+        if (phase) f[u] = __ldg(phase + q);
       }
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int q = q0 + u * nt;
-      if (q < npj) {
-        const int xr = c[u] / N3, z = c[u] - xr * N3;
-        put_picked(X, b, xstride, lo_words, o[u], cmul(tile[xr * LD + z], f[u]));
-      }
+      if (q < npj) put_picked(X, b, xstride, lo_words, o[u], phase ? cmul(tile[c[u]], f[u]) : tile[c[u]]);
     }
   }
 }
@@ -323,10 +320,9 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
   if (b < nb) prefetch(b, 0);
   if (staged)
     for (int q = threadIdx.x; q < npj; q += blockDim.x) {
-      const int c = cell[pf + q], xr = c / N3, z = c - xr * N3;
-      pto[q] = xr * LD + z;
+      pto[q] = cell[pf + q];
       pxo[q] = xo[pf + q];
-      pph[q] = phase[pf + q];
+      pph[q] = phase ? phase[pf + q] : make_float2(1.f, 0.f);
     }
   for (int it = 0; b < nb; it++, b += G) {
     if (b + G < nb) {
@@ -363,7 +359,7 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
       for (int q = threadIdx.x; q < npj; q += blockDim.x)
         put_picked(X, b, xstride, lo_words, pxo[q], cmul(tile[pto[q]], pph[q]));
     } else {
-      pick_plane<N3, LD>(tile, cell + pf, xo + pf, phase + pf, npj, threadIdx.x, blockDim.x, X, b, xstride,
+      pick_plane(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, threadIdx.x, blockDim.x, X, b, xstride,
                          lo_words);
     }
   }
@@ -375,8 +371,10 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
 // into registers (all loads of a lane in flight at once), transforms the
 // first axis into its shared tile [N1][LD] and picks from the flat list
 // through L1 (consecutive CTAs share a plane).
+// (three CTAs per SM: the 90^3 tile allows three in shared memory, and the register cap that
+// gives them costs a few spilled values of the line transform)
 template <int N1, int N3, int T1>
-__global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ H, int nb, PlaneGeom g,
+__global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict__ H, int nb, PlaneGeom g,
                                                      const int *__restrict__ plane_first,
                                                      const int *__restrict__ cell, const int *__restrict__ xo,
                                                      const float2 *__restrict__ phase, float2 *__restrict__ X,
@@ -417,7 +415,7 @@ __global__ void __launch_bounds__(FT) k_xpick_direct(const float2 *__restrict__ 
   __syncthreads();
   if (!band_ok) return;
   const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
-  pick_plane<N3, LD>(tile, cell + pf, xo + pf, phase + pf, npj, gt, TPB, X, b, xstride, lo_words);
+  pick_plane(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, gt, TPB, X, b, xstride, lo_words);
 }
 
 // Pass B writing whole grids (resident real-space wavefunctions): grid

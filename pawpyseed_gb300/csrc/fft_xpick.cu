@@ -53,7 +53,7 @@ bool fft_fast_supported(const PlaneGeom &g) {
 }
 
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
-                            long long xstride, int nb, long long lo_words) {
+                            long long xstride, int nb, long long lo_words, bool gamma) {
   using namespace fftfast;
   if (nb <= 0) return;
   PickFn fn = find_pick(g.N1, g.N3);
@@ -63,7 +63,8 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   const size_t smem = xpick_smem(g, cap);
   allow_smem((const void *)fn, smem);
   const int waves = resident_ctas((const void *)fn, smem);
-  const float2 *ph = pl.phase + (long long)kq * pl.npts;
+  // at Gamma every Bloch phase is 1: no phase list
+  const float2 *ph = gamma ? nullptr : pl.phase + (long long)kq * pl.npts;
   int bpc = 1;
   DirectFn dfn = find_direct(g.N1, g.N3, &bpc);
   const size_t dsmem = xpick_direct_smem(g, bpc);
@@ -81,7 +82,7 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
     PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, cap, X,
                                                                 xstride, lo_words));
   };
-  int mult = tune(std::make_tuple(lo_words ? 3 : 1, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
+  int mult = tune(std::make_tuple((lo_words ? 3 : 1) + (gamma ? 4 : 0), g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
   run(mult);
   note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
@@ -96,21 +97,26 @@ void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int b0
   note_work("fft_x_grid", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }
 
-// One CTA per segment: its points go to positions base[si] + p of the flat list.
+// One CTA per segment: its points go to positions base[si] + p of the flat list, with the
+// point's offset in the transformed plane's shared tile (row i, column k: i LD + k, LD the
+// padded row length) in place of its cell i N3 + k.
 __global__ void k_flatten_pick(const GatherSeg *__restrict__ segs, const int *__restrict__ base, int nkp,
-                               long long Q, int *__restrict__ cell, int *__restrict__ xo, float2 *__restrict__ phase) {
+                               long long Q, int N3, int LD, int *__restrict__ cell, int *__restrict__ xo,
+                               float2 *__restrict__ phase) {
   const GatherSeg sg = segs[blockIdx.x];
   const int q0 = base[blockIdx.x];
   for (int p = threadIdx.x; p < sg.npts; p += blockDim.x) {
-    cell[q0 + p] = sg.idx[p];
+    const int c = sg.idx[p], i = c / N3;
+    cell[q0 + p] = i * LD + (c - i * N3);
     xo[q0 + p] = (int)(sg.x_off + p);
     for (int k = 0; k < nkp; k++) phase[k * Q + q0 + p] = sg.phase[k * sg.phase_stride + p];
   }
 }
 
-void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl) {
+void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, int N3, PickList &pl) {
   if (nsegs <= 0) return;
-  PAWPY_LAUNCH("pick_list", k_flatten_pick<<<nsegs, 128, 0, stream()>>>(segs, base, nkp, pl.npts, pl.cell, pl.xo,
+  PAWPY_LAUNCH("pick_list", k_flatten_pick<<<nsegs, 128, 0, stream()>>>(segs, base, nkp, pl.npts, N3,
+                                                                         padded(N3), pl.cell, pl.xo,
                                                                          pl.phase));
 }
 

@@ -36,8 +36,9 @@ void launch_fft_planes_fast(const float2 *C, int Wpad, const int *plane_start, c
                             const PlaneGeom &g, float2 *H, int nb);
 struct GatherSeg;
 // The sphere points in plane order: points [plane_first[j], plane_first[j + 1])
-// lie in plane j of the second axis; cell is i*N3 + k within the plane, xo the
-// position in the picked-point vector, phase[kq*npts + q] the Bloch phase.
+// lie in plane j of the second axis; cell is the point's offset i*LD + k in the
+// transformed plane's shared tile (LD the padded row length), xo the position in
+// the picked-point vector, phase[kq*npts + q] the Bloch phase.
 struct PickList {
   const int *plane_first = nullptr;
   int *cell = nullptr, *xo = nullptr;
@@ -47,8 +48,9 @@ struct PickList {
 };
 // lo_words > 0: the rows are written in the split BF16 form (bf16split.cuh), lo plane lo_words
 // 32-bit words after the hi plane
+// gamma: the k-point is Gamma (every Bloch phase is 1, the phase list is not read)
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
-                            long long xstride, int nb, long long lo_words = 0);
+                            long long xstride, int nb, long long lo_words = 0, bool gamma = false);
 // Resident real-space wavefunctions of one k-point, bands in tiles of 16: the value of band b at
 // cell c (= (x N2 + y) N3 + z) is at grid_value_index(b, c, n3d).
 __host__ __device__ inline long long grid_value_index(int b, long long cell, long long n3d) {
@@ -57,7 +59,7 @@ __host__ __device__ inline long long grid_value_index(int b, long long cell, lon
 // pass B writing whole grids of bands [b0, b0 + nb) of one k-point (register sizes only)
 void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int b0, int nb);
 // fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
-void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, PickList &pl);
+void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, int N3, PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).
 void launch_fft_axis(float2 *grid, int nb, int N1, int N2, int N3, int axis, const Radices &r,
                      const float2 *tw);
@@ -125,7 +127,6 @@ struct ContractSource {
   long long xrows = 0;  // split form (tensor-core contraction): rows per plane of X
   const float2 *grid = nullptr;  // k-point kq at grid + kq gstride, grid_value_index layout
   long long n3d = 0, r0 = 0, npts = 0, gstride = 0;
-  long long grows = 0, gkp = 0;  // rows of 16 bands over all gkp k-points (gkp gstride / 16)
   int nband = 1;
   const int *gcell = nullptr;
   const float2 *gphase = nullptr;

@@ -165,7 +165,13 @@ struct Status {
   int *dev = nullptr, *host = nullptr;
   int next = 0;
 };
-thread_local std::vector<std::pair<int, std::string>> t_pending;  // slots read back on this thread's stream
+// slots read back by this thread, with the stream each read-back was ordered on
+struct PendingStatus {
+  int slot;
+  std::string what;
+  cudaStream_t stream;
+};
+thread_local std::vector<PendingStatus> t_pending;
 Status &status_state() {
   static Status s;
   return s;
@@ -193,18 +199,25 @@ void status_readback(int *dev_slot, const char *what) {
   Status &st = status_state();
   int slot = (int)(dev_slot - st.dev);
   PAWPY_CUDA(cudaMemcpyAsync(st.host + slot, dev_slot, sizeof(int), cudaMemcpyDeviceToHost, stream()));
-  t_pending.push_back({slot, what});
+  t_pending.push_back({slot, what, stream()});
 }
 
 void sync() {
-  PAWPY_CUDA(cudaStreamSynchronize(stream()));
+  const cudaStream_t s = stream();
+  PAWPY_CUDA(cudaStreamSynchronize(s));
   if (t_pending.empty()) return;
+  // only the read-backs ordered on the stream just waited for have landed
   Status &st = status_state();
   std::string msg;
-  for (auto &p : t_pending)
-    if (st.host[p.first] != 0 && msg.empty())
-      msg = p.second + " (status " + std::to_string(st.host[p.first]) + ")";
-  t_pending.clear();
+  std::vector<PendingStatus> rest;
+  for (auto &p : t_pending) {
+    if (p.stream != s) {
+      rest.push_back(p);
+      continue;
+    }
+    if (st.host[p.slot] != 0 && msg.empty()) msg = p.what + " (status " + std::to_string(st.host[p.slot]) + ")";
+  }
+  t_pending.swap(rest);
   if (!msg.empty()) throw Error(ERR_DEVICE_FLAG, msg);
 }
 

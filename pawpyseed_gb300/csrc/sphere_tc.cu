@@ -45,9 +45,9 @@ constexpr int DRAIN = 4;     // drain warps
 
 // GATHER = false: the picked rows are already split (bf16split.cuh), so a K block of A is
 // two TMA boxes and the pipeline is TMA -> MMA only (4-5 stages, two CTAs per SM).
-// GATHER = true: the producer gathers each K block's grid rows by TMA (tile::gather4) into a
-// ring of STG FP32 staging slots; CONV converter warps apply the Bloch phase, split and write
-// the A planes of an MMA stage.
+// GATHER = true: CONV converter warps gather the grid values with cp.async into a ring of
+// STG FP32 staging slots (STG - 1 K blocks in flight), apply the Bloch phase, split and
+// write the A planes of an MMA stage.
 template <int BN, bool GATHER>
 struct SphCfg {
   static constexpr int CONV = GATHER ? 8 : 0;
@@ -73,11 +73,17 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int bn) {
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// 1D bulk copy (16-byte aligned source, destination and size)
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
+// 8-byte cp.async; src_bytes 0 fills the destination with zeros
+__device__ __forceinline__ void cpa8z(uint32_t dst, const void *src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void conv_barrier(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
 }  // namespace
@@ -96,7 +102,6 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
   constexpr int STAGES = C::STAGES;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[STAGES], conv_full[STAGES], mma_empty[STAGES];
-  __shared__ __align__(8) unsigned long long stg_full[C::STG > 0 ? C::STG : 1], stg_empty[C::STG > 0 ? C::STG : 1];
   __shared__ __align__(8) unsigned long long bar_accf[2], bar_acce[2], bar_drain;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
@@ -135,10 +140,6 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
       mbar_init(smem_u32(&conv_full[s]), GATHER ? 32 * C::CONV : 1);
       mbar_init(smem_u32(&mma_empty[s]), 1);
     }
-    for (int s = 0; s < C::STG; s++) {
-      mbar_init(smem_u32(&stg_full[s]), 1);
-      mbar_init(smem_u32(&stg_empty[s]), 32 * C::CONV);
-    }
     for (int s = 0; s < 2; s++) {
       mbar_init(smem_u32(&bar_accf[s]), 1);
       mbar_init(smem_u32(&bar_acce[s]), DRAIN);
@@ -163,31 +164,10 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
 
   if (warp == 0) {
     if (lane == 0 && nkb > 0) {
-      // TMA producer: table planes (and, for picked rows, the A planes) of each K block; for
-      // grid values, the K block's 16 grid rows (one row = 16 bands of one cell) of each band
-      // tile by gather4, and its 16 Bloch phases, into the staging ring
-      int last[STAGES], last_g[C::STG > 0 ? C::STG : 1];
+      // TMA producer: table planes (and, for picked rows, the A planes) of each K block
+      int last[STAGES];
 #pragma unroll
       for (int s = 0; s < STAGES; s++) last[s] = -1;
-#pragma unroll
-      for (int s = 0; s < C::STG; s++) last_g[s] = -1;
-      const int ntile = (nrows + 15) / 16;
-      long long tile_row0 = 0;
-      int cell_next[KPTS];
-      auto load_cells = [&](int i) {
-#pragma unroll
-        for (int p = 0; p < KPTS; p++) {
-          const long long x = st.a_x + (long long)i * KPTS + p;
-          const int c = (GATHER && i < nkb && x < src.npts) ? __ldg(src.gcell + x) : -1;
-          cell_next[p] = c < 0 ? 0 : c;  // a gap's value is zeroed by its phase
-        }
-      };
-      if (GATHER) {
-        // (batches of the gathered form start on a k-point, so the tile's first band is a
-        // multiple of 128)
-        tile_row0 = (kq * ((src.nband + 15) / 16) + (src.r0 + row0 - kq * src.nband) / 16) * src.n3d;
-        load_cells(0);
-      }
       for (int i = 0; i < nkb; i++) {
         const int s = i % STAGES, r = i / STAGES;
         if (r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag)) {
@@ -206,38 +186,11 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
           tma_load_2d(a_plane(s, 1), &tmA, bf, 0, aplane + y);
         }
         last[s] = r;
-        if (GATHER) {
-          const int t = i % C::STG, u = i / C::STG;
-          if (u > 0 && !mbar_wait(smem_u32(&stg_empty[t]), (u - 1) & 1, &abort_flag)) {
-            if (!abort_flag) fail(12);
-            break;
-          }
-          if (abort_flag) break;
-          int cell[KPTS];
-#pragma unroll
-          for (int p = 0; p < KPTS; p++) cell[p] = cell_next[p];
-          load_cells(i + 1);
-          const uint32_t gf = smem_u32(&stg_full[t]);
-          const uint32_t slot = stg_base + t * C::STG_BYTES;
-          mbar_expect_tx(gf, ntile * KPTS * 128 + C::PH_BYTES);
-          for (int tt = 0; tt < ntile; tt++) {
-            const long long rb = tile_row0 + (long long)tt * src.n3d;
-#pragma unroll
-            for (int q = 0; q < KPTS / 4; q++)
-              tma_gather4(slot + (tt * KPTS + 4 * q) * 128, &tmA, gf, 0, (int)(rb + cell[4 * q]),
-                          (int)(rb + cell[4 * q + 1]), (int)(rb + cell[4 * q + 2]), (int)(rb + cell[4 * q + 3]));
-          }
-          bulk_load(ph_base + t * C::PH_BYTES, src.gphase + kq * src.npts + st.a_x + (long long)i * KPTS,
-                    C::PH_BYTES, gf);
-          last_g[t] = u;
-        }
       }
       if (abort_flag) {
         // let the copies already issued land before the CTA's memory is released
         for (int s = 0; s < STAGES; s++)
           if (last[s] >= 0) mbar_wait(smem_u32(&full[s]), last[s] & 1);
-        for (int s = 0; s < C::STG; s++)
-          if (last_g[s] >= 0) mbar_wait(smem_u32(&stg_full[s]), last_g[s] & 1);
       }
     }
   } else if (warp == 1) {
@@ -283,41 +236,89 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
     }
   } else if (GATHER && warp < 2 + C::CONV) {
     // converters, thread ct -> row ct % 128 (band b0 + row) and points [8 (ct / 128), +8) of
-    // each K block: the staged grid rows are [band tile][point][16 bands], so a warp's reads
-    // (32 consecutive bands of one point) are two 128-byte runs, and its 16-byte operand stores
-    // of 8 consecutive rows hit distinct banks of the swizzled tile
+    // each K block: a warp's copies read 32 consecutive bands of one grid cell (two 128-byte
+    // lines of the band-tiled grid) into the slot's [point][row] staging layout (consecutive
+    // 8-byte destinations), and its 16-byte operand stores of 8 consecutive rows hit distinct
+    // banks of the swizzled tile. Every converter thread runs every iteration (the named
+    // barriers need all of them); after an abort the waits return at once and the conversions
+    // are skipped.
     static_assert(!GATHER || C::CONV * 32 == 2 * STM, "two converter threads per row");
-    constexpr int PPT = KPTS / 2;
+    constexpr int NCT = 32 * C::CONV, STG = C::STG, D = STG - 1, PPT = KPTS / 2;
     const int ct = threadIdx.x - 64, row = ct & (STM - 1), pbase = (ct / STM) * PPT;
-    const bool live = row < nrows;
-    for (int i = 0; i < nkb; i++) {
-      const int s = i % STAGES, r = i / STAGES, t = i % C::STG, u = i / C::STG;
-      if (!mbar_wait(smem_u32(&stg_full[t]), u & 1, &abort_flag) ||
-          (r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag))) {
-        if (!abort_flag) fail(15);
-        break;
+    // rows are bands b0 + row of k-point kq (a tile never crosses a k-point)
+    const float2 *gk = src.grid + kq * src.gstride;
+    const int b0 = (int)(src.r0 + row0 - kq * src.nband);
+    int cell_next[PPT];
+    auto load_cells = [&](int i) {
+#pragma unroll
+      for (int pp = 0; pp < PPT; pp++) {
+        const long long x = st.a_x + (long long)i * KPTS + pbase + pp;
+        cell_next[pp] = (i < nkb && x < src.npts) ? __ldg(src.gcell + x) : -1;
       }
-      const float2 *sg = reinterpret_cast<const float2 *>(smem_raw + (stg_base + t * C::STG_BYTES - raw)) +
-                         (row >> 4) * KPTS * 16 + (row & 15);
-      const float2 *phs = reinterpret_cast<const float2 *>(smem_raw + (ph_base + t * C::PH_BYTES - raw));
-      unsigned char *ah = smem_raw + (a_plane(s, 0) - raw), *al = smem_raw + (a_plane(s, 1) - raw);
+    };
+    load_cells(0);
+    auto issue = [&](int i) {
+      if (i < nkb) {
+        const int t = i % STG;
+        int cell[PPT];
 #pragma unroll
-      for (int c = 0; c < PPT / 4; c++) {
-        uint32_t h[4], l[4];
+        for (int pp = 0; pp < PPT; pp++) cell[pp] = cell_next[pp];
+        load_cells(i + 1);
+        const uint32_t slot = stg_base + t * C::STG_BYTES;
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-          const int p = pbase + 4 * c + e;
-          const float2 g = live ? sg[p * 16] : make_float2(0.f, 0.f), ph = phs[p];
-          split_bf16x2(make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x), h[e], l[e]);
+        for (int pp = 0; pp < PPT; pp++) {
+          const int p = pbase + pp;
+          const bool ok = cell[pp] >= 0 && row < nrows;
+          const float2 *g = ok ? gk + grid_value_index(b0 + row, cell[pp], src.n3d) : src.grid;
+          cpa8z(slot + (p * STM + row) * 8, g, ok ? 8 : 0);
         }
-        const uint32_t off = sw64_offset(row, (pbase >> 2) + c);
-        *reinterpret_cast<uint4 *>(ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(al + off) = make_uint4(l[0], l[1], l[2], l[3]);
+        if (row == 0) {
+          // gaps between sites have cell -1: a zero phase
+#pragma unroll
+          for (int pp = 0; pp < PPT; pp++) {
+            const int p = pbase + pp;
+            const long long x = st.a_x + (long long)i * KPTS + p;
+            const bool ok = cell[pp] >= 0;
+            cpa8z(ph_base + (t * KPTS + p) * 8, ok ? src.gphase + kq * src.npts + x : src.gphase, ok ? 8 : 0);
+          }
+        }
       }
-      fence_async_smem();
-      mbar_arrive(smem_u32(&conv_full[s]));
-      mbar_arrive(smem_u32(&stg_empty[t]));
+      cpa_commit();
+    };
+    for (int i = 0; i < D; i++) issue(i);
+    for (int i = 0; i < nkb; i++) {
+      const int s = i % STAGES, r = i / STAGES, t = i % STG;
+      issue(i + D);
+      cpa_wait<D>();
+      conv_barrier(NCT);  // block i's values are in slot t for every converter thread
+      bool ok = !abort_flag;
+      if (ok && r > 0 && !mbar_wait(smem_u32(&mma_empty[s]), (r - 1) & 1, &abort_flag)) {
+        if (!abort_flag) fail(15);
+        ok = false;
+      }
+      if (ok) {
+        const float2 *sg = reinterpret_cast<const float2 *>(smem_raw + (stg_base + t * C::STG_BYTES - raw));
+        const float2 *phs = reinterpret_cast<const float2 *>(smem_raw + (ph_base - raw)) + t * KPTS;
+        unsigned char *ah = smem_raw + (a_plane(s, 0) - raw), *al = smem_raw + (a_plane(s, 1) - raw);
+#pragma unroll
+        for (int c = 0; c < PPT / 4; c++) {
+          uint32_t h[4], l[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int p = pbase + 4 * c + e;
+            const float2 g = sg[p * STM + row], ph = phs[p];
+            split_bf16x2(make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x), h[e], l[e]);
+          }
+          const uint32_t off = sw64_offset(row, (pbase >> 2) + c);
+          *reinterpret_cast<uint4 *>(ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<uint4 *>(al + off) = make_uint4(l[0], l[1], l[2], l[3]);
+        }
+        fence_async_smem();
+        mbar_arrive(smem_u32(&conv_full[s]));
+      }
+      conv_barrier(NCT);  // slot t is read by every converter thread before it is refilled
     }
+    cpa_wait<0>();
   } else if (warp >= 2 + C::CONV) {
     // drain warps: TMEM lane quarter (warp % 4), all BN columns
     const int quarter = warp & 3;
@@ -453,12 +454,7 @@ void launch_tc_sphere(const TcSite *sites_dev, int nsites, int bn, const void *p
   CUtensorMap ma = mb;
   long long aplane = 0;
   if (gather) {
-    // the band-tiled grid as rows of 16 bands (128 bytes) of one cell: k-point k, band tile t,
-    // cell c at row (k tiles + t) n3d + c; read one row at a time by gather4
-    PAWPY_REQUIRE(src.grows > 0 && src.grows < (1LL << 31) && src.gstride == src.grows / std::max(1LL, src.gkp) * 16,
-                  "resident grid rows out of range for 32-bit box coordinates");
-    ma = tensor_map_2d(const_cast<float2 *>(src.grid), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 32, src.grows, 128, 32, 1,
-                       CU_TENSOR_MAP_SWIZZLE_NONE);
+    PAWPY_REQUIRE(src.gstride > 0, "resident grid without a k-point stride");
   } else {
     PAWPY_REQUIRE(src.xrows >= nb && xtot % KPTS == 0, "picked-point blocks do not match the batch");
     aplane = xtot / KPTS * src.xrows;

@@ -66,17 +66,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       : "memory");
 }
 
-// Four rows y0..y3 (columns from x, one box row each) of a 2D tensor map whose box is one
-// row high, placed one after another at dst.
-__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y0, int y1,
-                                            int y2, int y3) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3)
-      : "memory");
-}
-
 // Shared-memory matrix descriptor of a K-major tile with 64-byte rows in the
 // 64-byte swizzle layout: 8-row groups 512 bytes apart, descriptor version 1.
 __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {

@@ -1,11 +1,12 @@
 """The sphere contraction on the tensor cores (split-BF16, csrc/sphere_tc.cu) against the FP32
 CUDA-core form and the oracle's FP64 projections.
 
-Both operand sources are covered: picked-point rows (the projections of setup_projections and of
-the smoothed partial waves on the defect) and the resident real-space grid of a prepared basis
-(pawpy_gpu_prepare_basis with real-space storage). Tolerances: projector coefficients within 1e-5
-of the largest coefficient against FP64 (as the collinear projector test), the two forms within
-2e-6 of it of each other, and the overlaps within 1e-5 of FP64 (the band-pair metric's target).
+Every operand source is covered: picked-point rows (the default), the band grids a projection
+pass writes for the gathered form (PAWPY_GPU_DEFECT_GRID=1), and the resident real-space grid of a
+prepared basis (pawpy_gpu_prepare_basis with real-space storage). Tolerances: projector
+coefficients within 1e-5 of the largest coefficient against FP64 (as the collinear projector
+test), the two forms within 2e-6 of it of each other, and the overlaps within 1e-5 of FP64 (the
+band-pair metric's target).
 """
 
 import os
@@ -42,8 +43,11 @@ def _with_mode(mode, fn):
         L.pawpy_gpu_set_sphere_contraction(1)
 
 
+@pytest.mark.parametrize("defect_grid", ["0", "1"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_tensor_core_projections_match_fp64_and_cuda_cores(name, workload_dirs, oracle_projectors):
+def test_tensor_core_projections_match_fp64_and_cuda_cores(name, defect_grid, workload_dirs, oracle_projectors,
+                                                           monkeypatch):
+    monkeypatch.setenv("PAWPY_GPU_DEFECT_GRID", defect_grid)
     from pawpyseed_gb300.wavefunction import Wavefunction
 
     dirs = workload_dirs(name)
@@ -64,10 +68,12 @@ def test_tensor_core_projections_match_fp64_and_cuda_cores(name, workload_dirs, 
 
 @pytest.mark.parametrize("name", ["cfg0", "cfg2s", "cfg3s"])
 @pytest.mark.parametrize("resident", [False, True])
-def test_tensor_core_overlaps_match_fp64(name, resident, workload_dirs, oracle_projectors):
+@pytest.mark.parametrize("defect_grid", ["0", "1"])
+def test_tensor_core_overlaps_match_fp64(name, resident, defect_grid, workload_dirs, oracle_projectors, monkeypatch):
     """project_all with every sphere contraction on the tensor cores (pseudo overlap in FP32): the
-    smoothed-wave projections of both structures, with the basis read from picked rows or from its
-    resident real-space grid."""
+    smoothed-wave projections of both structures, the defect's from picked rows or from the grids of
+    its projection pass, the basis's likewise or from its resident real-space grid."""
+    monkeypatch.setenv("PAWPY_GPU_DEFECT_GRID", defect_grid)
     from pawpyseed_gb300 import _lib
     from pawpyseed_gb300.projector import Projector
     from pawpyseed_gb300.wavefunction import Wavefunction
@@ -92,8 +98,10 @@ def test_tensor_core_overlaps_match_fp64(name, resident, workload_dirs, oracle_p
     assert np.abs(tc - cc).max() <= 2e-6
 
 
-def test_tensor_core_spinor_projections():
+@pytest.mark.parametrize("defect_grid", ["0", "1"])
+def test_tensor_core_spinor_projections(defect_grid, monkeypatch):
     """Spinor halves as rows of the contraction: both halves against the oracle."""
+    monkeypatch.setenv("PAWPY_GPU_DEFECT_GRID", defect_grid)
     import oracle as orc
     from test_gpu_ncl import half, ncl_case
 
