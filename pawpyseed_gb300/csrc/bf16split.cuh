@@ -8,11 +8,12 @@
 namespace pawpy {
 
 __device__ __forceinline__ void split_bf16x2(float2 v, uint32_t &hi, uint32_t &lo) {
-  const __nv_bfloat16 hr = __float2bfloat16_rn(v.x), hm = __float2bfloat16_rn(v.y);
-  const __nv_bfloat16 lr = __float2bfloat16_rn(v.x - __bfloat162float(hr));
-  const __nv_bfloat16 lm = __float2bfloat16_rn(v.y - __bfloat162float(hm));
-  hi = (uint32_t)__bfloat16_as_ushort(hr) | ((uint32_t)__bfloat16_as_ushort(hm) << 16);
-  lo = (uint32_t)__bfloat16_as_ushort(lr) | ((uint32_t)__bfloat16_as_ushort(lm) << 16);
+  // packed conversions: (re, im) to two BF16 in one instruction, each rounded to nearest
+  const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
 // Picked-point rows: complex64 X[row][xstride] (lo_words == 0), or the split form in K blocks

@@ -661,120 +661,187 @@ static double vnorm(const double *v) { return std::sqrt(v[0] * v[0] + v[1] * v[1
 // half box per axis (|a_j x a_k| rmax / V) N + 1, the centre round(coord N),
 // the cutoff (ndata_p - 1) rmax / ndata_{labels[s]} (the reference indexes the
 // denominator by the list position s). Tables carry dV V^-1/2.
-static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const int *labels,
-                          const double *coords, const std::vector<std::unique_ptr<SpeciesTables>> &sp,
-                          bool smooth, const double *lat, const int *N, double vol,
-                          const std::vector<DevKpt> &kpts, const double *rec) {
-  HostPhase hp("spheres");
-  S = SphereSet();
-  S.nsites = (int)site_nums.size();
-  if (S.nsites == 0) return;
+// One sphere set to build (the arguments of build_spheres).
+struct SphereJob {
+  SphereSet *S;
+  const std::vector<int> *site_nums;
+  const int *labels;
+  const double *coords;
+  const std::vector<std::unique_ptr<SpeciesTables>> *sp;
+  bool smooth;
+  const double *lat;
+  const int *N;
+  double vol;
+  const std::vector<DevKpt> *kpts;
+  const double *rec;
+  // between the two phases
   std::vector<SpeciesDev> sd;
-  for (auto &t : sp) sd.push_back(smooth ? t->smooth : t->proj);
-  double c23[3], c13[3], c12[3];
+  std::vector<int2> slabs;
+  std::vector<int> hc;
+  DevBuf<double> Ld;
+  DevBuf<int> Nd, counts;
+  DevBuf<int2> slabs_d;
+};
+
+// Sphere tables of several sets with one host round trip: every set's slab counts are
+// launched and read back together, then every set is compacted and tabulated.
+static void build_sphere_sets(std::vector<SphereJob> &jobs) {
+  HostPhase hp("spheres");
   auto cross = [](const double *a, const double *b, double *o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
     o[1] = a[2] * b[0] - a[0] * b[2];
     o[2] = a[0] * b[1] - a[1] * b[0];
   };
-  cross(lat + 3, lat + 6, c23);
-  cross(lat + 0, lat + 6, c13);
-  cross(lat + 0, lat + 3, c12);
-  S.host.resize(S.nsites);
-  std::vector<int2> slabs;
-  int lmoff = 0;
-  for (int s = 0; s < S.nsites; s++) {
-    int p = site_nums[s];
-    int e = labels[p];
-    PAWPY_REQUIRE(e >= 0 && e < (int)sp.size(), "site label out of range");
-    const SpeciesDev &spd = sd[e];
-    SiteDesc &h = S.host[s];
-    for (int a = 0; a < 3; a++) h.coord[a] = coords[3 * p + a];
-    h.species = e;
-    double rmax = spd.rmax;
-    h.g[0] = (int)(vnorm(c23) * rmax / vol * N[0]) + 1;
-    h.g[1] = (int)(vnorm(c13) * rmax / vol * N[1]) + 1;
-    h.g[2] = (int)(vnorm(c12) * rmax / vol * N[2]) + 1;
-    for (int a = 0; a < 3; a++) h.c[a] = (int)std::round(coords[3 * p + a] * N[a]);
-    int e_s = labels[s];
-    PAWPY_REQUIRE(e_s >= 0 && e_s < (int)sp.size(), "site label out of range");
-    h.R0 = (spd.size - 1) * rmax / sd[e_s].size;
-    h.total = spd.total;
-    h.lm_off = lmoff;
-    lmoff += h.total;
-    S.max_total = std::max(S.max_total, h.total);
-    for (int jb = 0; jb <= 2 * h.g[1]; jb++) slabs.push_back(make_int2(s, jb));
+  // phase 1: site descriptors and slab counts of every set
+  for (SphereJob &jb : jobs) {
+    SphereSet &S = *jb.S;
+    S = SphereSet();
+    S.nsites = (int)jb.site_nums->size();
+    if (S.nsites == 0) continue;
+    const double *lat = jb.lat;
+    const int *N = jb.N;
+    for (auto &t : *jb.sp) jb.sd.push_back(jb.smooth ? t->smooth : t->proj);
+    double c23[3], c13[3], c12[3];
+    cross(lat + 3, lat + 6, c23);
+    cross(lat + 0, lat + 6, c13);
+    cross(lat + 0, lat + 3, c12);
+    S.host.resize(S.nsites);
+    int lmoff = 0;
+    for (int s = 0; s < S.nsites; s++) {
+      int p = (*jb.site_nums)[s];
+      int e = jb.labels[p];
+      PAWPY_REQUIRE(e >= 0 && e < (int)jb.sp->size(), "site label out of range");
+      const SpeciesDev &spd = jb.sd[e];
+      SiteDesc &h = S.host[s];
+      for (int a = 0; a < 3; a++) h.coord[a] = jb.coords[3 * p + a];
+      h.species = e;
+      double rmax = spd.rmax;
+      h.g[0] = (int)(vnorm(c23) * rmax / jb.vol * N[0]) + 1;
+      h.g[1] = (int)(vnorm(c13) * rmax / jb.vol * N[1]) + 1;
+      h.g[2] = (int)(vnorm(c12) * rmax / jb.vol * N[2]) + 1;
+      for (int a = 0; a < 3; a++) h.c[a] = (int)std::round(jb.coords[3 * p + a] * N[a]);
+      int e_s = jb.labels[s];
+      PAWPY_REQUIRE(e_s >= 0 && e_s < (int)jb.sp->size(), "site label out of range");
+      h.R0 = (spd.size - 1) * rmax / jb.sd[e_s].size;
+      h.total = spd.total;
+      h.lm_off = lmoff;
+      lmoff += h.total;
+      S.max_total = std::max(S.max_total, h.total);
+      for (int q = 0; q <= 2 * h.g[1]; q++) jb.slabs.push_back(make_int2(s, q));
+    }
+    S.Ptot = lmoff;
+    jb.Ld.alloc(9);
+    jb.Ld.upload(lat, 9);
+    jb.Nd.alloc(3);
+    jb.Nd.upload(N, 3);
+    S.sites.alloc(S.nsites);
+    S.sites.upload(S.host.data(), S.nsites);
+    jb.slabs_d.alloc(jb.slabs.size());
+    jb.slabs_d.upload(jb.slabs.data(), jb.slabs.size());
+    jb.counts.alloc(jb.slabs.size());
+    launch_slab_count(S.sites.p, jb.slabs_d.p, (int)jb.slabs.size(), jb.Ld.p, jb.Nd.p, jb.counts.p);
   }
-  S.Ptot = lmoff;
-  DevBuf<double> Ld(9);
-  Ld.upload(lat, 9);
-  DevBuf<int> Nd(3);
-  Nd.upload(N, 3);
-  S.sites.alloc(S.nsites);
-  S.sites.upload(S.host.data(), S.nsites);
-  DevBuf<int2> slabs_d(slabs.size());
-  slabs_d.upload(slabs.data(), slabs.size());
-  DevBuf<int> counts(slabs.size());
-  launch_slab_count(S.sites.p, slabs_d.p, (int)slabs.size(), Ld.p, Nd.p, counts.p);
-  std::vector<int> hc(slabs.size());
-  counts.download(hc.data(), hc.size());
+  for (SphereJob &jb : jobs) {
+    if (jb.S->nsites == 0) continue;
+    jb.hc.resize(jb.slabs.size());
+    jb.counts.download(jb.hc.data(), jb.hc.size());
+  }
   sync();
-  long long pt = 0, val = 0;
-  S.site_pt.assign(S.nsites, 0);
-  S.site_val.assign(S.nsites, 0);
-  S.site_npts.assign(S.nsites, 0);
-  for (size_t q = 0; q < slabs.size(); q++) S.site_npts[slabs[q].x] += hc[q];
-  for (int s = 0; s < S.nsites; s++) {
-    S.site_pt[s] = pt;
-    S.site_val[s] = val;
-    pt += S.site_npts[s];
-    val += (long long)S.site_npts[s] * S.host[s].total;
+  // phase 2: compaction and tabulation of every set
+  for (SphereJob &jb : jobs) {
+    SphereSet &S = *jb.S;
+    if (S.nsites == 0) continue;
+    const double *lat = jb.lat;
+    const int *N = jb.N;
+    const double vol = jb.vol;
+    const std::vector<int2> &slabs = jb.slabs;
+    const std::vector<int> &hc = jb.hc;
+    long long pt = 0, val = 0;
+    S.site_pt.assign(S.nsites, 0);
+    S.site_val.assign(S.nsites, 0);
+    S.site_npts.assign(S.nsites, 0);
+    for (size_t q = 0; q < slabs.size(); q++) S.site_npts[slabs[q].x] += hc[q];
+    for (int s = 0; s < S.nsites; s++) {
+      S.site_pt[s] = pt;
+      S.site_val[s] = val;
+      pt += S.site_npts[s];
+      val += (long long)S.site_npts[s] * S.host[s].total;
+    }
+    pt = 0;
+    for (size_t q = 0; q < slabs.size(); q++) {
+      if (hc[q] == 0) continue;
+      int s = slabs[q].x;
+      SegFill f;
+      f.site = s;
+      f.jb = slabs[q].y;
+      f.pt_off = pt;
+      f.npts = hc[q];
+      f.site_pt = S.site_pt[s];
+      f.site_npts = S.site_npts[s];
+      f.site_val = S.site_val[s];
+      S.segs.push_back(f);
+      int j = f.jb - S.host[s].g[1] + S.host[s].c[1];
+      S.seg_plane.push_back(((j % N[1]) + N[1]) % N[1]);
+      pt += hc[q];
+    }
+    S.nseg = (int)S.segs.size();
+    S.npts = pt;
+    S.nvals = val;
+    S.species.alloc(jb.sd.size());
+    S.species.upload(jb.sd.data(), jb.sd.size());
+    S.nkp = (int)jb.kpts->size();
+    std::vector<double> kc(3 * (size_t)S.nkp);
+    for (int q = 0; q < S.nkp; q++)
+      for (int a = 0; a < 3; a++)
+        kc[3 * q + a] = (*jb.kpts)[q].kfrac[0] * jb.rec[a] + (*jb.kpts)[q].kfrac[1] * jb.rec[3 + a] +
+                        (*jb.kpts)[q].kfrac[2] * jb.rec[6 + a];
+    DevBuf<double> kcd(kc.size());
+    kcd.upload(kc.data(), kc.size());
+    S.idx.alloc(std::max(1LL, pt));
+    S.tab.alloc(std::max(1LL, val));
+    S.phase.alloc(std::max(1LL, pt * S.nkp));
+    DevBuf<SegFill> segs_d(std::max(1, S.nseg));
+    segs_d.upload(S.segs.data(), S.nseg);
+    double wscale = vol / N[0] / N[1] / N[2] * std::pow(vol, -0.5);
+    // half the smallest lattice-plane spacing: a point nearer its site than this has the
+    // unwrapped box displacement as its unique minimum image
+    double hmin = 1e300;
+    for (int a = 0; a < 3; a++) {
+      const double *u = lat + 3 * ((a + 1) % 3), *v = lat + 3 * ((a + 2) % 3);
+      double c[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+      hmin = std::min(hmin, 0.5 * std::fabs(vol) / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+    }
+    launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, jb.Ld.p, jb.Nd.p, wscale, hmin, kcd.p, S.nkp, pt,
+                    S.idx.p, S.tab.p, S.phase.p);
   }
-  pt = 0;
-  for (size_t q = 0; q < slabs.size(); q++) {
-    if (hc[q] == 0) continue;
-    int s = slabs[q].x;
-    SegFill f;
-    f.site = s;
-    f.jb = slabs[q].y;
-    f.pt_off = pt;
-    f.npts = hc[q];
-    f.site_pt = S.site_pt[s];
-    f.site_npts = S.site_npts[s];
-    f.site_val = S.site_val[s];
-    S.segs.push_back(f);
-    int j = f.jb - S.host[s].g[1] + S.host[s].c[1];
-    S.seg_plane.push_back(((j % N[1]) + N[1]) % N[1]);
-    pt += hc[q];
-  }
-  S.nseg = (int)S.segs.size();
-  S.npts = pt;
-  S.nvals = val;
-  S.species.alloc(sd.size());
-  S.species.upload(sd.data(), sd.size());
-  S.nkp = (int)kpts.size();
-  std::vector<double> kc(3 * (size_t)S.nkp);
-  for (int q = 0; q < S.nkp; q++)
-    for (int a = 0; a < 3; a++)
-      kc[3 * q + a] = kpts[q].kfrac[0] * rec[a] + kpts[q].kfrac[1] * rec[3 + a] + kpts[q].kfrac[2] * rec[6 + a];
-  DevBuf<double> kcd(kc.size());
-  kcd.upload(kc.data(), kc.size());
-  S.idx.alloc(std::max(1LL, pt));
-  S.tab.alloc(std::max(1LL, val));
-  S.phase.alloc(std::max(1LL, pt * S.nkp));
-  DevBuf<SegFill> segs_d(std::max(1, S.nseg));
-  segs_d.upload(S.segs.data(), S.nseg);
-  double wscale = vol / N[0] / N[1] / N[2] * std::pow(vol, -0.5);
-  // half the smallest lattice-plane spacing: a point nearer its site than this has the
-  // unwrapped box displacement as its unique minimum image
-  double hmin = 1e300;
-  for (int a = 0; a < 3; a++) {
-    const double *u = lat + 3 * ((a + 1) % 3), *v = lat + 3 * ((a + 2) % 3);
-    double c[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
-    hmin = std::min(hmin, 0.5 * std::fabs(vol) / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
-  }
-  launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, Ld.p, Nd.p, wscale, hmin, kcd.p, S.nkp, pt, S.idx.p,
-                  S.tab.p, S.phase.p);
+}
+
+static SphereJob sphere_job(SphereSet &S, const std::vector<int> &site_nums, const int *labels, const double *coords,
+                            const std::vector<std::unique_ptr<SpeciesTables>> &sp, bool smooth, const double *lat,
+                            const int *N, double vol, const std::vector<DevKpt> &kpts, const double *rec) {
+  SphereJob jb;
+  jb.S = &S;
+  jb.site_nums = &site_nums;
+  jb.labels = labels;
+  jb.coords = coords;
+  jb.sp = &sp;
+  jb.smooth = smooth;
+  jb.lat = lat;
+  jb.N = N;
+  jb.vol = vol;
+  jb.kpts = &kpts;
+  jb.rec = rec;
+  return jb;
+}
+
+// Sphere tables of one set (setup_site, utils.c:590-696, for every site).
+static void build_spheres(SphereSet &S, const std::vector<int> &site_nums, const int *labels,
+                          const double *coords, const std::vector<std::unique_ptr<SpeciesTables>> &sp,
+                          bool smooth, const double *lat, const int *N, double vol,
+                          const std::vector<DevKpt> &kpts, const double *rec) {
+  std::vector<SphereJob> jobs;
+  jobs.push_back(sphere_job(S, site_nums, labels, coords, sp, smooth, lat, N, vol, kpts, rec));
+  build_sphere_sets(jobs);
 }
 
 // One FFT pass over every band of wavefunction d, gathering onto several
@@ -1134,6 +1201,8 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     src.gstride = (long long)grid_kstride(d);
     src.npts = xtot;
     src.nband = d.nband;
+    src.gamma = true;
+    for (auto &q : d.kp) src.gamma = src.gamma && kpoint_is_gamma(q);
     src.gcell = gcell.p;
     src.gphase = gphase.p;
   } else {
@@ -1466,18 +1535,38 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   ps.pseudo_ready[0] = ps.pseudo_ready[1] = false;
   ps.recip = false;
   ps.cross_ready[0] = ps.cross_ready[1] = false;
+  // The N_RS pair matrices depend only on the species and positions: a host thread computes them
+  // (radial integrals on this thread's auxiliary stream, assembly on the host pool) while this
+  // thread builds the sphere tables and issues the projections.
+  const cudaStream_t aux = aux_stream();
+  const int dev = device();
+  std::exception_ptr pair_err;
+  std::thread pair_thread([&, aux, dev] {
+    try {
+      PAWPY_CUDA(cudaSetDevice(dev));
+      OnStream on(aux);
+      pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
+    } catch (...) {
+      pair_err = std::current_exception();
+    }
+  });
+  struct Joiner {
+    std::thread &t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } joiner{pair_thread};
   // smoothed partial waves of R's N_R sites on S's grid, and of S's N_S sites on R's grid
-  build_spheres(ps.sm_NR, ps.N_R, labels_R, coords_R, R.species, true, S.lattice, S.N, S.vol, S.kp, S.rec);
-  build_spheres(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, R.lattice, R.N, R.vol, R.kp, R.rec);
+  {
+    std::vector<SphereJob> jobs;
+    jobs.push_back(sphere_job(ps.sm_NR, ps.N_R, labels_R, coords_R, R.species, true, S.lattice, S.N, S.vol, S.kp,
+                              S.rec));
+    jobs.push_back(sphere_job(ps.sm_NS, ps.N_S, labels_S, coords_S, S.species, true, R.lattice, R.N, R.vol, R.kp,
+                              R.rec));
+    build_sphere_sets(jobs);
+  }
   ps.WP_S.alloc(std::max<size_t>(1, (size_t)S.nk * S.nband * ps.sm_NR.Ptot));
   ps.WP_R.alloc(std::max<size_t>(1, (size_t)R.nk * R.nband * ps.sm_NS.Ptot));
-  // The N_RS pair matrices depend only on the species and positions: their radial integrals run
-  // on the auxiliary stream (behind the first FFT pass at most) and the host assembles them
-  // while the projections below run on the device.
-  {
-    OnStream on(aux_stream());
-    pair_matrices(ps, wf_R, wf_S, labels_R, labels_S, coords_R, coords_S);
-  }
   // one FFT pass per wavefunction: pending <p|psi> and the smoothed-partial-wave projections together
   for (int side = 0; side < 2; side++) {
     DevWF &W = side == 0 ? S : R;
@@ -1496,6 +1585,8 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
     if (!sets.empty()) project_bands(W, sets, outs);
     if (!W.p_ready) W.p_ready = true;  // a prepared, shared basis is only read
   }
+  pair_thread.join();
+  if (pair_err) std::rethrow_exception(pair_err);
   publish_pair_matrices(ps, wf_R, wf_S);
   free_wave_projections(wf_R);
   free_wave_projections(wf_S);

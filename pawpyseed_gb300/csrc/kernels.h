@@ -128,6 +128,7 @@ struct ContractSource {
   const float2 *grid = nullptr;  // k-point kq at grid + kq gstride, grid_value_index layout
   long long n3d = 0, r0 = 0, npts = 0, gstride = 0;
   int nband = 1;
+  bool gamma = false;  // every k-point of the rows is Gamma (all Bloch phases 1)
   const int *gcell = nullptr;
   const float2 *gphase = nullptr;
 };

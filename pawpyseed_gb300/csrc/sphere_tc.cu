@@ -245,9 +245,10 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
     static_assert(!GATHER || C::CONV * 32 == 2 * STM, "two converter threads per row");
     constexpr int NCT = 32 * C::CONV, STG = C::STG, D = STG - 1, PPT = KPTS / 2;
     const int ct = threadIdx.x - 64, row = ct & (STM - 1), pbase = (ct / STM) * PPT;
-    // rows are bands b0 + row of k-point kq (a tile never crosses a k-point)
-    const float2 *gk = src.grid + kq * src.gstride;
+    // rows are bands b0 + row of k-point kq (a tile never crosses a k-point): the value at cell c
+    // is at growp + 16 c (grid_value_index with the band part hoisted)
     const int b0 = (int)(src.r0 + row0 - kq * src.nband);
+    const float2 *growp = src.grid + kq * src.gstride + grid_value_index(b0 + row, 0, src.n3d);
     int cell_next[PPT];
     auto load_cells = [&](int i) {
 #pragma unroll
@@ -269,10 +270,10 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
         for (int pp = 0; pp < PPT; pp++) {
           const int p = pbase + pp;
           const bool ok = cell[pp] >= 0 && row < nrows;
-          const float2 *g = ok ? gk + grid_value_index(b0 + row, cell[pp], src.n3d) : src.grid;
+          const float2 *g = ok ? growp + 16 * cell[pp] : src.grid;
           cpa8z(slot + (p * STM + row) * 8, g, ok ? 8 : 0);
         }
-        if (row == 0) {
+        if (row == 0 && !src.gamma) {
           // gaps between sites have cell -1: a zero phase
 #pragma unroll
           for (int pp = 0; pp < PPT; pp++) {
@@ -306,8 +307,14 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
 #pragma unroll
           for (int e = 0; e < 4; e++) {
             const int p = pbase + 4 * c + e;
-            const float2 g = sg[p * STM + row], ph = phs[p];
-            split_bf16x2(make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x), h[e], l[e]);
+            const float2 g = sg[p * STM + row];
+            if (src.gamma) {
+              // Gamma: every Bloch phase is 1 (a gap's value is zero: its copy was zero-filled)
+              split_bf16x2(g, h[e], l[e]);
+            } else {
+              const float2 ph = phs[p];
+              split_bf16x2(make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x), h[e], l[e]);
+            }
           }
           const uint32_t off = sw64_offset(row, (pbase >> 2) + c);
           *reinterpret_cast<uint4 *>(ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
