@@ -46,6 +46,34 @@ struct SpeciesTables {
   std::vector<double> D;  // total x total: (aeov - psov)[n_i][n_j] where (l,m) agree
 };
 
+// A CUDA event owned by the structure holding it (created on first record).
+struct OwnedEvent {
+  cudaEvent_t e = nullptr;
+  OwnedEvent() = default;
+  OwnedEvent(const OwnedEvent &) = delete;
+  OwnedEvent &operator=(const OwnedEvent &) = delete;
+  OwnedEvent(OwnedEvent &&o) noexcept : e(o.e) { o.e = nullptr; }
+  OwnedEvent &operator=(OwnedEvent &&o) noexcept {
+    if (this != &o) {
+      if (e) cudaEventDestroy(e);
+      e = o.e;
+      o.e = nullptr;
+    }
+    return *this;
+  }
+  ~OwnedEvent() {
+    if (e) cudaEventDestroy(e);
+  }
+  void record(cudaStream_t s) {
+    if (!e) PAWPY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PAWPY_CUDA(cudaEventRecord(e, s));
+  }
+  // the stream waits for the last record (nothing when never recorded)
+  void wait(cudaStream_t s) const {
+    if (e) PAWPY_CUDA(cudaStreamWaitEvent(s, e, 0));
+  }
+};
+
 struct SphereSet {
   int nsites = 0, Ptot = 0, max_total = 0, nkp = 0, nseg = 0;
   long long npts = 0, nvals = 0;
@@ -58,6 +86,9 @@ struct SphereSet {
   DevBuf<int> idx;
   DevBuf<float2> tab, phase;
   DevBuf<SpeciesDev> species;
+  // idx and phase are written on the library stream; tab on the auxiliary stream of the
+  // thread that built the set, which records tab_ready: readers of tab wait for it
+  OwnedEvent tab_ready;
 };
 
 // Sphere tables of the all-electron real-space wavefunctions of one wavefunction on
@@ -139,6 +170,8 @@ struct DevWF {
   DevWF &operator=(const DevWF &) = delete;
   // the buffers are freed on the library stream: it waits for the uploads first
   ~DevWF() {
+    // members are freed on the library stream: order it after the tables' auxiliary-stream fill
+    proj.tab_ready.wait(stream());
     for (cudaEvent_t e : c_ev) {
       cudaStreamWaitEvent(stream(), e, 0);
       cudaEventDestroy(e);
@@ -206,6 +239,11 @@ struct PairState {
   DevBuf<float2> cross[2];
   bool cross_ready[2] = {false, false};
   int cross_prec[2] = {-1, -1};
+  ~PairState() {
+    // members are freed on the library stream: order it after the tables' auxiliary-stream fill
+    sm_NR.tab_ready.wait(stream());
+    sm_NS.tab_ready.wait(stream());
+  }
 };
 
 // Overlaps are between wavefunction bands: a noncollinear band is two consecutive
@@ -695,6 +733,7 @@ static void build_sphere_sets(std::vector<SphereJob> &jobs) {
   // phase 1: site descriptors and slab counts of every set
   for (SphereJob &jb : jobs) {
     SphereSet &S = *jb.S;
+    S.tab_ready.wait(stream());  // the old tables are freed in the library stream's order
     S = SphereSet();
     S.nsites = (int)jb.site_nums->size();
     if (S.nsites == 0) continue;
@@ -811,8 +850,23 @@ static void build_sphere_sets(std::vector<SphereJob> &jobs) {
       double c[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
       hmin = std::min(hmin, 0.5 * std::fabs(vol) / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
     }
+    // the points' indices and phases (what the pick needs) on the library stream; the table
+    // values (needed only by the contraction, after the pick) on the auxiliary stream
     launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, jb.Ld.p, jb.Nd.p, wscale, hmin, kcd.p, S.nkp, pt,
-                    S.idx.p, S.tab.p, S.phase.p);
+                    S.idx.p, S.tab.p, S.phase.p, 1);
+    OwnedEvent inputs;
+    inputs.record(stream());
+    {
+      OnStream on(aux_stream());
+      inputs.wait(stream());
+      launch_seg_fill(S.sites.p, segs_d.p, S.nseg, S.species.p, jb.Ld.p, jb.Nd.p, wscale, hmin, kcd.p, S.nkp, pt,
+                      S.idx.p, S.tab.p, S.phase.p, 2);
+      S.tab_ready.record(stream());
+      // the fills' inputs, released in the auxiliary stream's order (after both fills)
+      DevBuf<double> kcd_done = std::move(kcd), L_done = std::move(jb.Ld);
+      DevBuf<SegFill> segs_done = std::move(segs_d);
+      DevBuf<int> N_done = std::move(jb.Nd);
+    }
   }
 }
 
@@ -1089,6 +1143,7 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   long long tc_lb = 0;
   DevBuf<TcSite> tsites_d;
   DevBuf<unsigned char> tc_planes;
+  OwnedEvent planes_ready;
   if (tc) {
     tc_bn = tc_sphere_width(max_total);
     for (size_t i = 0; i < sets.size(); i++) {
@@ -1117,12 +1172,16 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     }
     tc_brows = (int)tsites.size() * tc_bn;
     tc_lb = (long long)std::max(1, tc_maxkb) * 32;
-    tc_planes.alloc((size_t)2 * tc_brows * tc_lb * 2);
     tsites_d.alloc(std::max<size_t>(1, tsites.size()));
     tsites_d.upload(tsites.data(), tsites.size());
+    // the table planes follow the sets' table values on the auxiliary stream, beside the pick
+    OnStream on(aux_stream());
+    for (const SphereSet *S : sets) S->tab_ready.wait(stream());
+    tc_planes.alloc((size_t)2 * tc_brows * tc_lb * 2);
     DevBuf<TcTable> ttabs_d(std::max<size_t>(1, ttabs.size()));
     ttabs_d.upload(ttabs.data(), ttabs.size());
     launch_tc_tables(ttabs_d.p, (int)ttabs.size(), tc_maxkb, tc_bn, tc_brows, tc_lb, tc_planes.p);
+    planes_ready.record(stream());
   }
   int maxn1 = 0;
   for (auto &q : d.kp) maxn1 = std::max(maxn1, q.n1);
@@ -1263,9 +1322,11 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     const int cn = (int)(r1 - r0);
     src.r0 = r0;
     if (tc) {
+      planes_ready.wait(stream());
       launch_tc_sphere(tsites_d.p, (int)tsites.size(), tc_bn, tc_planes.p, tc_brows, tc_lb, src, cn, xtot, xtot);
       continue;
     }
+    for (const SphereSet *S : sets) S->tab_ready.wait(stream());
     launch_contract_staged(ch_d.p, (int)chunks.size(), max_total, src, partial.p, ptot, cn, xtot);
     for (size_t i = 0; i < sets.size(); i++) {
       const SphereSet &S = *sets[i];
@@ -1718,6 +1779,8 @@ static void build_recip_spread(const SphereSet &S, const DevWF &W, const std::ve
   c.tab = S.tab.p;
   c.phase = S.phase.p;
   c.npts = S.npts;
+  // the kernels that read these tables are ordered after their values
+  S.tab_ready.wait(stream());
 }
 
 // CA[k][band][Wpad] of every band of W (get_aug_freqs for the sites site_nums of W whose

@@ -172,7 +172,7 @@ void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, con
 // hmin: half the smallest lattice-plane spacing (points nearer their site skip the image search)
 void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
                      const double *lattice, const int *fftg, double wscale, double hmin, const double *kcart, int nkp,
-                     long long total_pts, int *idx, float2 *tab, float2 *phase);
+                     long long total_pts, int *idx, float2 *tab, float2 *phase, int what = 3);
 // x-axis transform of each plane j of nb bands, then X[b][x_off + p] = u(point p) exp(i k.path_p) for
 // the segments of plane j (segs sorted by plane; plane_start[N2+1])
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,

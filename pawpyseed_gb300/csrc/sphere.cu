@@ -125,7 +125,7 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
                            const int *__restrict__ Ng, double wscale, double hmin,
                            const double *__restrict__ kcart, int nkp,
                            long long total_pts, int *__restrict__ idx, float2 *__restrict__ tab,
-                           float2 *__restrict__ phase) {
+                           float2 *__restrict__ phase, int what) {
   __shared__ int warp_cnt[32];
   __shared__ int base_s;
   __shared__ double invN[3];
@@ -168,11 +168,17 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
       chunk += warp_cnt[w];
     }
     int pos = base_s + before + __popc(m & ((1u << lane) - 1u));
-    if (in && pos < sg.npts) {
+    // what & 1: the point's plane index and Bloch phases (the pick needs only these); what & 2:
+    // its table values
+    if (in && pos < sg.npts && (what & 1)) {
+      const int ii = ((ijk[0] % N[0]) + N[0]) % N[0];
+      const int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
+      idx[sg.pt_off + pos] = ii * N[2] + kk;
+    }
+    if (in && pos < sg.npts && (what & 2)) {
       int ii = ((ijk[0] % N[0]) + N[0]) % N[0];
       int jj = ((ijk[1] % N[1]) + N[1]) % N[1];
       int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
-      idx[sg.pt_off + pos] = ii * N[2] + kk;
       // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73):
       // nearer than hmin, the unwrapped box displacement is the unique minimum image;
       // otherwise search the 27 images
@@ -256,6 +262,8 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
         // conj(radial * Y_lm) * dV * V^-1/2
         tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] = make_float2(y * cs, -y * sn);
       }
+    }
+    if (in && pos < sg.npts && (what & 1)) {
       // exp(i k.path): the argument in units of pi reduced to [-1, 1] in double precision,
       // then the single-precision sincospi (the phase is stored in single precision)
       for (int kq = 0; kq < nkp; kq++) {
@@ -275,10 +283,11 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
 
 void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const SpeciesDev *species,
                      const double *lattice, const int *fftg, double wscale, double hmin, const double *kcart, int nkp,
-                     long long total_pts, int *idx, float2 *tab, float2 *phase) {
+                     long long total_pts, int *idx, float2 *tab, float2 *phase, int what) {
   if (nseg <= 0) return;
   PAWPY_LAUNCH("sphere_fill", k_seg_fill<<<nseg, 128, 0, stream()>>>(sites, segs, species, lattice, fftg, wscale,
-                                                                    hmin, kcart, nkp, total_pts, idx, tab, phase));
+                                                                    hmin, kcart, nkp, total_pts, idx, tab, phase,
+                                                                    what));
 }
 
 // ---------------------------------------------------------------------------

@@ -58,21 +58,20 @@ class Projector:
         reference does (projector.py:157).
         """
         ref, cur = self.basis.structure, self.wf.structure
-        M_R, M_S = [], []
-        for i in range(len(ref)):
-            for j in range(len(cur)):
-                if ref.distance(i, cur, j) <= 0.02 and ref.species[i] == cur.species[j]:
-                    M_R.append(i)
-                    M_S.append(j)
-        N_R = [i for i in range(len(ref)) if i not in M_R]
-        N_S = [j for j in range(len(cur)) if j not in M_S]
+        # all pair distances at once; the pairs in the reference's loop order (i outer, j inner)
+        D = ref.distance_matrix(cur)
+        same = (D <= 0.02) & (np.array(ref.species)[:, None] == np.array(cur.species)[None, :])
+        Mi, Mj = np.nonzero(same)
+        M_R, M_S = [int(x) for x in Mi], [int(x) for x in Mj]
+        in_M_R, in_M_S = set(M_R), set(M_S)
+        N_R = [i for i in range(len(ref)) if i not in in_M_R]
+        N_S = [j for j in range(len(cur)) if j not in in_M_S]
         N_RS = []
-        for i in N_R:
-            for j in N_S:
-                rmax1 = self.basis.cr.pps[ref.species[i]].rmax
-                rmax2 = self.wf.cr.pps[cur.species[i]].rmax
-                if ref.distance(i, cur, j) < rmax1 + rmax2:
-                    N_RS.append((i, j))
+        if N_R and N_S:
+            rmax1 = np.array([self.basis.cr.pps[ref.species[i]].rmax for i in N_R])
+            rmax2 = np.array([self.wf.cr.pps[cur.species[i]].rmax for i in N_R])
+            close = D[np.ix_(N_R, N_S)] < (rmax1 + rmax2)[:, None]
+            N_RS = [(N_R[a], N_S[b]) for a, b in zip(*np.nonzero(close))]
         return M_R, M_S, N_R, N_S, N_RS
 
     def setup_overlap(self):

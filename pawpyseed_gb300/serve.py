@@ -32,16 +32,19 @@ def site_lists(basis, defect):
     reference reads it from sites[i] with the basis index i, which fails for defect
     cells with vacancies (fewer sites than the basis)."""
     ref, cur = basis.structure, defect.structure
-    M_R, M_S = [], []
-    for i in range(len(ref)):
-        for j in range(len(cur)):
-            if ref.distance(i, cur, j) <= 0.02 and ref.species[i] == cur.species[j]:
-                M_R.append(i)
-                M_S.append(j)
-    N_R = [i for i in range(len(ref)) if i not in M_R]
-    N_S = [j for j in range(len(cur)) if j not in M_S]
-    N_RS = [(i, j) for i in N_R for j in N_S
-            if ref.distance(i, cur, j) < basis.cr.pps[ref.species[i]].rmax + defect.cr.pps[cur.species[j]].rmax]
+    D = ref.distance_matrix(cur)
+    same = (D <= 0.02) & (np.array(ref.species)[:, None] == np.array(cur.species)[None, :])
+    Mi, Mj = np.nonzero(same)
+    M_R, M_S = [int(x) for x in Mi], [int(x) for x in Mj]
+    in_M_R, in_M_S = set(M_R), set(M_S)
+    N_R = [i for i in range(len(ref)) if i not in in_M_R]
+    N_S = [j for j in range(len(cur)) if j not in in_M_S]
+    N_RS = []
+    if N_R and N_S:
+        r1 = np.array([basis.cr.pps[ref.species[i]].rmax for i in N_R])
+        r2 = np.array([defect.cr.pps[cur.species[j]].rmax for j in N_S])
+        close = D[np.ix_(N_R, N_S)] < r1[:, None] + r2[None, :]
+        N_RS = [(N_R[a], N_S[b]) for a, b in zip(*np.nonzero(close))]
     a = lambda x: np.ascontiguousarray(np.array(x, dtype=np.int32))  # noqa: E731
     return [a(M_R), a(M_S), a(N_R), a(N_S), a([x for x, _ in N_RS]), a([y for _, y in N_RS])]
 

@@ -75,14 +75,24 @@ class Structure:
         pymatgen's ``PeriodicSite.distance`` (used by the reference
         ``make_site_lists``, projector.py:135-159) is the minimum over lattice images.
         """
-        d = other.frac_coords[j] - self.frac_coords[i]
+        return float(self.distance_matrix(other, [i], [j])[0, 0])
+
+    def distance_matrix(self, other, rows=None, cols=None):
+        """Periodic minimum-image distances between the sites rows of self (default all) and the
+        sites cols of other: [len(rows), len(cols)], the 27 nearest images of the wrapped
+        fractional difference, as ``distance``."""
+        fa = self.frac_coords if rows is None else self.frac_coords[np.asarray(rows, dtype=int)]
+        fb = other.frac_coords if cols is None else other.frac_coords[np.asarray(cols, dtype=int)]
+        d = fb[None, :, :] - fa[:, None, :]
         d = d - np.round(d)
-        best = np.inf
+        L = self.lattice
+        best = np.full(d.shape[:2], np.inf)
         for a in (-1, 0, 1):
             for b in (-1, 0, 1):
                 for c in (-1, 0, 1):
-                    v = (d + np.array([a, b, c])) @ self.lattice
-                    best = min(best, float(np.sqrt(v @ v)))
+                    e = d + np.array([a, b, c], dtype=np.float64)
+                    v = e[..., 0:1] * L[0] + e[..., 1:2] * L[1] + e[..., 2:3] * L[2]
+                    best = np.minimum(best, np.sqrt(v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2]))
         return best
 
 
