@@ -71,9 +71,12 @@ void clear_error();
 // The single stream every kernel and copy of the library is ordered on.
 cudaStream_t stream();
 int device();
-// The calling thread's upload stream, and a scope in which stream() (and so
-// every launch and copy of the library) is another stream. Nothing may be
-// allocated inside such a scope.
+// The calling thread's upload stream (highest priority), and a scope in which
+// stream() (and so every launch, copy and allocation of the library) is another
+// stream. Memory allocated inside such a scope is ordered on that stream: another
+// stream that uses or frees it first waits for an event recorded there after the
+// allocation (and memory freed there was last used on that stream or before such
+// an event).
 cudaStream_t side_stream();
 // The calling thread's stream for work issued ahead of the library stream's queue.
 cudaStream_t aux_stream();

@@ -1597,9 +1597,10 @@ static void do_overlap_setup_real(pswf_t *wf_R, pswf_t *wf_S, const int *labels_
   ps.recip = false;
   ps.cross_ready[0] = ps.cross_ready[1] = false;
   // The N_RS pair matrices depend only on the species and positions: a host thread computes them
-  // (radial integrals on this thread's auxiliary stream, assembly on the host pool) while this
-  // thread builds the sphere tables and issues the projections.
-  const cudaStream_t aux = aux_stream();
+  // (radial integrals on this thread's high-priority upload stream, which is idle by then,
+  // assembly on the host pool)
+  // while this thread builds the sphere tables and issues the projections.
+  const cudaStream_t aux = side_stream();
   const int dev = device();
   std::exception_ptr pair_err;
   std::thread pair_thread([&, aux, dev] {

@@ -117,7 +117,7 @@ static thread_local cudaMemPool_t t_pool = nullptr;
 // so that its blocks are scheduled as soon as SM slots free up).
 static thread_local cudaStream_t t_side = nullptr;
 // ...and a third for work issued ahead of the main stream's queue (the first FFT
-// pass of a wavefunction whose projections come later), at normal priority.
+// pass of a wavefunction whose projections come later, sphere-table values).
 static thread_local cudaStream_t t_aux = nullptr;
 
 cudaStream_t side_stream() {
@@ -135,7 +135,11 @@ bool thread_has_stream() { return t_stream != nullptr; }
 cudaStream_t aux_stream() {
   if (!t_aux) {
     stream();
-    PAWPY_CUDA(cudaStreamCreateWithFlags(&t_aux, cudaStreamNonBlocking));
+    // high priority: its launches (the first FFT pass, the sphere tables' values and planes)
+    // are dispatched ahead of the waiting blocks of a long launch on the library stream
+    int lo = 0, hi = 0;
+    PAWPY_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PAWPY_CUDA(cudaStreamCreateWithPriority(&t_aux, cudaStreamNonBlocking, hi));
   }
   return t_aux;
 }

@@ -86,14 +86,15 @@ class Structure:
         d = fb[None, :, :] - fa[:, None, :]
         d = d - np.round(d)
         L = self.lattice
+        dc = d @ L
         best = np.full(d.shape[:2], np.inf)
         for a in (-1, 0, 1):
             for b in (-1, 0, 1):
                 for c in (-1, 0, 1):
-                    e = d + np.array([a, b, c], dtype=np.float64)
-                    v = e[..., 0:1] * L[0] + e[..., 1:2] * L[1] + e[..., 2:3] * L[2]
-                    best = np.minimum(best, np.sqrt(v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2]))
-        return best
+                    v = dc + np.array([a, b, c], dtype=np.float64) @ L
+                    np.minimum(best, np.einsum("ijk,ijk->ij", v, v), out=best)
+        # the square root is monotone and correctly rounded: the root of the least square
+        return np.sqrt(best)
 
 
 def write_poscar(path, struct, comment="synthetic"):
