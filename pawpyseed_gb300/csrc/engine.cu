@@ -962,7 +962,10 @@ static void transform_planes_early(DevWF &d) {
   if ((long long)(total * sizeof(float2)) > kEarlyPlanesBytes) return;
   if (!force && (long long)(kmax * sizeof(float2)) <= l2_bytes()) return;
   HostPhase hp("early_planes");
-  d.Hall.alloc(std::max<size_t>(total, 1));
+  {
+    HostPhase ha("early_planes_alloc");
+    d.Hall.alloc(std::max<size_t>(total, 1));
+  }
   d.hoff = off;
   if ((int)d.h_ev.size() != d.nk) {
     for (cudaEvent_t e : d.h_ev) PAWPY_CUDA(cudaEventDestroy(e));
@@ -977,6 +980,7 @@ static void transform_planes_early(DevWF &d) {
   PAWPY_CUDA(cudaStreamWaitEvent(xs, ready, 0));
   PAWPY_CUDA(cudaEventDestroy(ready));
   {
+    HostPhase hl("early_planes_launch");
     OnStream on(xs);
     for (int k = 0; k < d.nk; k++) {
       DevKpt &q = d.kp[k];

@@ -49,7 +49,14 @@ struct Runtime {
     double work = 0;  // algorithmic bytes or flops the launches declared (note_work)
   };
   std::map<std::string, Fam> fams;
-  std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  // profiled launches: family, start and end events, the stream, whether the end was recorded
+  struct Pending {
+    std::string family;
+    cudaEvent_t a, b;
+    cudaStream_t s;
+    bool ended;
+  };
+  std::vector<Pending> pending;
   std::vector<cudaEvent_t> event_pool;
   std::recursive_mutex mu;
 };
@@ -84,21 +91,27 @@ cudaEvent_t take_event(Runtime &r) {
 
 void drain_locked(Runtime &r) {
   for (auto &p : r.pending) {
+    if (!p.ended) {
+      // a launch that failed between its two records: nothing to time
+      r.event_pool.push_back(p.a);
+      r.event_pool.push_back(p.b);
+      continue;
+    }
     float ms = 0;
-    PAWPY_CUDA(cudaEventSynchronize(p.second.second));
-    PAWPY_CUDA(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
-    auto &f = r.fams[p.first];
+    PAWPY_CUDA(cudaEventSynchronize(p.b));
+    PAWPY_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+    auto &f = r.fams[p.family];
     f.ms += ms;
     f.n += 1;
     if (r.has_origin) {
       float t0 = 0, t1 = 0;
-      PAWPY_CUDA(cudaEventElapsedTime(&t0, r.origin, p.second.first));
-      PAWPY_CUDA(cudaEventElapsedTime(&t1, r.origin, p.second.second));
+      PAWPY_CUDA(cudaEventElapsedTime(&t0, r.origin, p.a));
+      PAWPY_CUDA(cudaEventElapsedTime(&t1, r.origin, p.b));
       if (f.first < 0 || t0 < f.first) f.first = t0;
       if (t1 > f.last) f.last = t1;
     }
-    r.event_pool.push_back(p.second.first);
-    r.event_pool.push_back(p.second.second);
+    r.event_pool.push_back(p.a);
+    r.event_pool.push_back(p.b);
   }
   r.pending.clear();
 }
@@ -325,8 +338,9 @@ void launch_begin(const char *family) {
   r.launches++;
   if (r.profile) {
     cudaEvent_t a = take_event(r), b = take_event(r);
-    PAWPY_CUDA(cudaEventRecord(a, t_stream ? t_stream : r.s));
-    r.pending.push_back({family, {a, b}});
+    const cudaStream_t s = t_stream ? t_stream : r.s;
+    PAWPY_CUDA(cudaEventRecord(a, s));
+    r.pending.push_back({family, a, b, s, false});
   }
 }
 
@@ -339,8 +353,16 @@ void note_work(const char *family, double units) {
 void launch_end(const char *family) {
   Runtime &r = rt();
   std::lock_guard<std::recursive_mutex> g(r.mu);
-  if (r.profile && !r.pending.empty() && r.pending.back().first == family)
-    PAWPY_CUDA(cudaEventRecord(r.pending.back().second.second, t_stream ? t_stream : r.s));
+  if (!r.profile) return;
+  // the latest open launch of this family on this thread's stream (launches of other host
+  // threads may have been recorded in between)
+  const cudaStream_t s = t_stream ? t_stream : r.s;
+  for (auto it = r.pending.rbegin(); it != r.pending.rend(); ++it)
+    if (!it->ended && it->s == s && it->family == family) {
+      PAWPY_CUDA(cudaEventRecord(it->b, s));
+      it->ended = true;
+      return;
+    }
 }
 
 namespace {
