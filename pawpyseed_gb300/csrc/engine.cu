@@ -962,10 +962,7 @@ static void transform_planes_early(DevWF &d) {
   if ((long long)(total * sizeof(float2)) > kEarlyPlanesBytes) return;
   if (!force && (long long)(kmax * sizeof(float2)) <= l2_bytes()) return;
   HostPhase hp("early_planes");
-  {
-    HostPhase ha("early_planes_alloc");
-    d.Hall.alloc(std::max<size_t>(total, 1));
-  }
+  if (d.Hall.n < total || d.Hall.n == 0) d.Hall.alloc(std::max<size_t>(total, 1));
   d.hoff = off;
   if ((int)d.h_ev.size() != d.nk) {
     for (cudaEvent_t e : d.h_ev) PAWPY_CUDA(cudaEventDestroy(e));
@@ -980,7 +977,6 @@ static void transform_planes_early(DevWF &d) {
   PAWPY_CUDA(cudaStreamWaitEvent(xs, ready, 0));
   PAWPY_CUDA(cudaEventDestroy(ready));
   {
-    HostPhase hl("early_planes_launch");
     OnStream on(xs);
     for (int k = 0; k < d.nk; k++) {
       DevKpt &q = d.kp[k];
@@ -1339,8 +1335,9 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
     }
   }
   if (early) {
-    // consumed: the planes go back to the pool (freed in stream order after the second pass)
-    d.Hall.reset();
+    // consumed; the buffer stays with the wavefunction for its next first pass (a fresh
+    // allocation of several GB from the stream-ordered pool was measured to block the host
+    // for 2.6 ms); released with the wavefunction
     d.h_ready = false;
   }
 }
