@@ -67,6 +67,10 @@ def parse():
     ap.add_argument("--cpu-report", action="store_true",
                     help="the reference algorithm's CPU port per workload (0, 1, 2): defect setup, overlaps, "
                          "pairs/s and its error against FP64, one JSON line each (no GPU work)")
+    ap.add_argument("--ingest-report", action="store_true",
+                    help="WAVECAR reading: the library reader (device plane-wave spheres, parallel record "
+                         "reads), the same without a device, and the serial numpy restatement")
+    ap.add_argument("--ingest-child", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--precision-report", action="store_true",
                     help="overlap matrix of the workload in every precision against FP64 (error and time)")
     return ap.parse_args()
@@ -673,8 +677,78 @@ def run_cpu_report(args):
                               sample=smp.describe())), flush=True)
 
 
+def _time_reader(path, nwk, reps):
+    from pawpyseed_gb300 import _lib
+
+    L = _lib.lib()
+    kws = np.full(nwk, 1.0 / nwk)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        p = L.pawpy_gpu_read_wavefunctions(path.encode(), kws)
+        _lib.check()
+        ts.append(time.perf_counter() - t0)
+        L.pawpy_gpu_free_pswf(p)
+    return float(np.median(ts)) * 1e3
+
+
+def run_ingest_report(args):
+    """Per workload (64-atom, 216-atom): the defect WAVECAR written to a temporary directory (in the
+    page cache), then read by pawpy_gpu_read_wavefunctions with the plane-wave spheres on the
+    device, by the same reader in a process that sees no CUDA device (spheres on the host threads),
+    and by the serial numpy restatement of reader.c; and the spheres alone (device, numpy)."""
+    import tempfile
+
+    from pawpyseed_gb300 import _lib, synth, vaspio
+
+    if args.ingest_child:
+        path, nwk = args.ingest_child.rsplit(":", 1)
+        print(json.dumps(dict(ms=_time_reader(path, int(nwk), 5))), flush=True)
+        return
+    L = _lib.lib()
+    for cfg in (1, 2):
+        w = synth.small_workload(cfg)
+        _, defect_s = synth.structures(cfg)
+        data = synth.wavefunction_data(defect_s, w, 22 + 7 * cfg)
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "WAVECAR")
+            vaspio.write_wavecar(path, data["lattice"], data["encut"], data["kpts"], data["coeffs"],
+                                 data["energies"], data["occs"], nspin=data["nspin"])
+            size = os.path.getsize(path)
+            nwk = data["nwk"]
+            dev_ms = _time_reader(path, nwk, 5)
+            env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--ingest-child", "%s:%d" % (path, nwk)],
+                               env=env, capture_output=True, text=True, check=True)
+            host_ms = json.loads(r.stdout.strip().splitlines()[-1])["ms"]
+            t0 = time.perf_counter()
+            vaspio.read_wavecar_numpy(path)
+            numpy_ms = (time.perf_counter() - t0) * 1e3
+        lat = np.ascontiguousarray(np.asarray(data["lattice"], dtype=np.float64).reshape(-1))
+        ks = [np.ascontiguousarray(k, dtype=np.float64) for k in np.asarray(data["kpts"]).reshape(-1, 3)]
+        L.pawpy_gpu_gvectors(lat, ks[0], float(data["encut"]), None, 0)
+        _lib.check()
+        t0 = time.perf_counter()
+        for k in ks:
+            L.pawpy_gpu_gvectors(lat, k, float(data["encut"]), None, 0)
+        sph_dev_ms = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        for k in ks:
+            vaspio.gvectors(data["lattice"], k, data["encut"])
+        sph_np_ms = (time.perf_counter() - t0) * 1e3
+        print(json.dumps(dict(workload=cfg, wavecar_bytes=size, kpoints=len(ks), bands=data["nband"],
+                              plane_waves=[int(g.shape[0]) for g in data["gs"]][:1],
+                              reader_ms=dev_ms, reader_gb_s=size / dev_ms / 1e6,
+                              reader_no_device_ms=host_ms, numpy_reader_ms=numpy_ms,
+                              spheres_device_ms=sph_dev_ms, spheres_numpy_ms=sph_np_ms,
+                              host_threads=threads_used())), flush=True)
+
+
 def main():
     args = parse()
+    if args.ingest_report or args.ingest_child:
+        run_ingest_report(args)
+        return
     if args.cpu_report:
         run_cpu_report(args)
         return

@@ -19,6 +19,8 @@
 #ifndef PAWPY_GPU_H
 #define PAWPY_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 #include <complex>
 typedef std::complex<double> pawpy_c128;
@@ -370,8 +372,25 @@ int pawpy_gpu_project_realspace_all(pawpy_c128 *out, pswf_t *wf, pswf_t *wf_R, i
                                     double *coords, int *labels_R, double *coords_R);
 
 /* WAVECAR reader producing a pswf_t with the reference's layout and VASP plane-
- * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf. */
+ * wave order (reader.c:129-315 semantics); free with pawpy_gpu_free_pswf.
+ * Replaces read_wavefunctions (reader.c:317-322). The plane-wave spheres of all
+ * k-points are enumerated in one device launch where a CUDA device is present
+ * (on the host threads otherwise), while the coefficient records are read in
+ * parallel straight into the bands' arrays. */
 pswf_t *pawpy_gpu_read_wavefunctions(const char *filename, const double *kpt_weights);
+/* The same from the bytes of a WAVECAR in memory (an inflated .gz or .bz2 file,
+ * pawpyc.pyx:217-222). Replaces read_wavefunctions_from_str (reader.c:324-329),
+ * which has no length argument: the header's record length and counts bound the
+ * reads. */
+pswf_t *pawpy_gpu_read_wavefunctions_from_str(const char *start, const double *kpt_weights);
+/* As pawpy_gpu_read_wavefunctions_from_str with the buffer's length: a record
+ * past len is an error (status 4) instead of a read past the buffer. */
+pswf_t *pawpy_gpu_read_wavefunctions_from_bytes(const char *data, size_t len, const double *kpt_weights);
+/* The plane-wave sphere of one k-point (kpt in reciprocal-lattice units) of a
+ * cell (lattice rows, A) at ENCUT (eV), enumerated on the device in VASP order
+ * (reader.c:230-271): writes the int triples to out (3*cap ints; out may be NULL
+ * to count) and returns their number, or -1 (status 5 without a CUDA device). */
+int pawpy_gpu_gvectors(const double *lattice, const double *kpt, double encut, int *out, int cap);
 /* Builds a pswf_t from in-memory arrays: Gs[iwk] int32[3*nplane[iwk]] and
  * Cs[iwk] complex64[nband*nplane[iwk]] for iwk = spin*nwk + k. Copies them.
  * is_ncl: noncollinear (spinor) coefficients; nplane counts both halves (up

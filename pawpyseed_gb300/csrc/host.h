@@ -1,6 +1,8 @@
 // Host-side declarations shared by the translation units of libpawpy_gpu.
 #pragma once
 
+#include <cmath>
+#include <cstddef>
 #include <vector>
 
 #include "common.h"
@@ -10,8 +12,29 @@ namespace pawpy {
 // --- wavefunction files and ownership (host_wavecar.cpp) ---
 double det3(const double *m);
 void reciprocal(const double *lat, double *rec);
+// hbar^2/2m in eV A^2, the reader's c (reader.c:11)
+constexpr double kGsphereC = 0.262465831;
+// nb{1,2,3}max of reader.c:55-127 (kept in double precision)
+void gsphere_bounds(const double *rec, double encut, double nb[3]);
+// The reader's cutoff test of one plane wave k + g (reader.c:243-251), in its
+// order of operations: |s| = pow(s.s, 0.5), pow(|s|, 2.0) / c <= ENCUT.
+inline bool gsphere_keep(const double *rec, const double *k, int g1, int g2, int g3, double encut) {
+  double s[3];
+  for (int j = 0; j < 3; j++) s[j] = (k[0] + g1) * rec[j] + (k[1] + g2) * rec[3 + j] + (k[2] + g3) * rec[6 + j];
+  const double g = std::pow(s[0] * s[0] + s[1] * s[1] + s[2] * s[2], 0.5);
+  return std::pow(g, 2.0) / kGsphereC <= encut;
+}
+// The plane-wave list of one k-point in VASP order (int triples), on the host.
 std::vector<int> enumerate_gvectors(const double *rec, const double *k, double encut);
+// The lists of nk k-points (kpts [nk][3]); on the device where a CUDA device is
+// present (gsphere.cu), on the host threads otherwise.
+std::vector<std::vector<int>> gsphere_lists(const double *rec, double encut, const double *kpts, int nk);
+// Whether the process sees a CUDA device.
+bool device_present();
 pswf_t *read_wavecar(const char *path, const double *kws);
+// The same from the bytes of a WAVECAR in memory; len = SIZE_MAX when the
+// caller does not know it (read_wavefunctions_from_str, reader.c:324-329).
+pswf_t *read_wavecar_bytes(const char *data, size_t len, const double *kws);
 pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const double *lattice,
                          const double *kpts, const double *weights, const int *nplane,
                          const int *const *Gs, const pawpy_c64 *const *Cs, const double *energies,

@@ -9,11 +9,19 @@
 // truncated (reader.c:230-271), the noncollinear doubling (reader.c:274-284).
 // Every member is allocated with malloc/calloc so that the reference's
 // free_pswf (utils.c:275-301) and pawpy_gpu_free_pswf release the same objects.
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cerrno>
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
 #include <cstdio>
-#include <string>
 #include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "common.h"
@@ -21,7 +29,7 @@
 
 namespace pawpy {
 
-static const double kC = 0.262465831;  // hbar^2/2m in eV A^2
+static const double kC = kGsphereC;
 
 static void cross(const double *a, const double *b, double *o) {
   o[0] = a[1] * b[2] - a[2] * b[1];
@@ -44,8 +52,7 @@ void reciprocal(const double *lat, double *rec) {
   for (int i = 0; i < 9; i++) rec[i] *= 2.0 * M_PI / v;
 }
 
-// nb{1,2,3}max of reader.c:55-127 (kept in double precision).
-static void nb_bounds(const double *rec, double encut, double nb[3]) {
+void gsphere_bounds(const double *rec, double encut, double nb[3]) {
   const double *b1 = rec, *b2 = rec + 3, *b3 = rec + 6;
   double m1 = norm3(b1), m2 = norm3(b2), m3 = norm3(b3);
   double kc = std::pow(encut * kC, 0.5), v[3];
@@ -70,7 +77,7 @@ static void nb_bounds(const double *rec, double encut, double nb[3]) {
 // The plane-wave list of one k-point in VASP order; returns int triples.
 std::vector<int> enumerate_gvectors(const double *rec, const double *k, double encut) {
   double nb[3];
-  nb_bounds(rec, encut, nb);
+  gsphere_bounds(rec, encut, nb);
   std::vector<int> out;
   for (int i3 = 0; i3 <= 2 * nb[2]; i3++) {
     int g3 = i3 > nb[2] ? (int)(i3 - 2 * nb[2] - 1) : i3;
@@ -78,11 +85,7 @@ std::vector<int> enumerate_gvectors(const double *rec, const double *k, double e
       int g2 = i2 > nb[1] ? (int)(i2 - 2 * nb[1] - 1) : i2;
       for (int i1 = 0; i1 <= 2 * nb[0]; i1++) {
         int g1 = i1 > nb[0] ? (int)(i1 - 2 * nb[0] - 1) : i1;
-        double s[3];
-        for (int j = 0; j < 3; j++)
-          s[j] = (k[0] + g1) * rec[j] + (k[1] + g2) * rec[3 + j] + (k[2] + g3) * rec[6 + j];
-        double g = norm3(s);
-        if (std::pow(g, 2.0) / kC <= encut) {
+        if (gsphere_keep(rec, k, g1, g2, g3, encut)) {
           out.push_back(g1);
           out.push_back(g2);
           out.push_back(g3);
@@ -147,15 +150,39 @@ static void update_bounds(pswf_t *wf, const int *g, int n) {
     }
 }
 
-pswf_t *read_wavecar(const char *path, const double *kws) {
-  FILE *fp = std::fopen(path, "rb");
-  if (!fp) throw Error(ERR_IO, std::string("cannot open ") + path);
-  struct Closer {
-    FILE *f;
-    ~Closer() { std::fclose(f); }
-  } closer{fp};
+// Where the bytes of a WAVECAR come from: a file read with pread (one file
+// descriptor shared by the reading threads) or memory.
+struct WcSource {
+  int fd = -1;
+  const char *mem = nullptr;
+  size_t len = 0;  // bytes available (SIZE_MAX: unknown, memory only)
+  void read(long long off, size_t n, void *dst) const {
+    if (off < 0 || (len != SIZE_MAX && ((size_t)off > len || n > len - (size_t)off)))
+      throw Error(ERR_IO, "short WAVECAR record");
+    if (mem) {
+      std::memcpy(dst, mem + off, n);
+      return;
+    }
+    char *d = static_cast<char *>(dst);
+    while (n) {
+      const ssize_t r = ::pread(fd, d, n, (off_t)off);
+      if (r < 0 && errno == EINTR) continue;
+      if (r <= 0) throw Error(ERR_IO, "short WAVECAR record");
+      d += r;
+      off += r;
+      n -= (size_t)r;
+    }
+  }
+};
+
+// read_wavecar (reader.c:129-315) in three stages: the header records of every
+// k-point; the plane-wave spheres of all k-points in one device launch
+// (gsphere_lists), while the host threads read the coefficient records straight
+// into the bands' arrays (records in parallel, no staging copy); the spheres
+// checked against the records' plane-wave counts.
+static pswf_t *read_wavecar_from(const WcSource &src, const double *kws) {
   double head[3];
-  if (std::fread(head, 8, 3, fp) != 3) throw Error(ERR_IO, "short WAVECAR header");
+  src.read(0, sizeof head, head);
   long nrecl = std::lround(head[0]);
   int nspin = (int)std::lround(head[1]);
   long rtag = std::lround(head[2]);
@@ -163,32 +190,61 @@ pswf_t *read_wavecar(const char *path, const double *kws) {
     throw Error(ERR_UNSUPPORTED, "only complex64 WAVECARs (rtag 45200) are supported");
   if (nrecl < 96 || nrecl % 8) throw Error(ERR_IO, "bad WAVECAR record length");
   std::vector<double> rec(nrecl / 8);
-  auto read_rec = [&](long irec, void *dst) {
-    if (std::fseek(fp, irec * nrecl, SEEK_SET) || std::fread(dst, 1, nrecl, fp) != (size_t)nrecl)
-      throw Error(ERR_IO, "short WAVECAR record");
-  };
-  read_rec(1, rec.data());
+  src.read(nrecl, nrecl, rec.data());
   int nwk = (int)std::lround(rec[0]), nband = (int)std::lround(rec[1]);
   double encut = rec[2];
   double lat[9];
   for (int i = 0; i < 9; i++) lat[i] = rec[3 + i];
   if (nspin < 1 || nspin > 2 || nwk < 1 || nband < 1) throw Error(ERR_IO, "bad WAVECAR dimensions");
+  if ((long)(4 + 3 * nband) * 8 > nrecl) throw Error(ERR_IO, "WAVECAR record too short for its band header");
   pswf_t *wf = new_pswf(nspin, nwk, nband, encut, lat);
-  std::vector<float> cbuf(nrecl / 4);
+  const int nk = nwk * nspin;
   try {
-    for (int iwk = 0; iwk < nwk * nspin; iwk++) {
-      long irec = (long)iwk * (1 + nband);
-      read_rec(irec + 2, rec.data());
+    std::vector<double> kvec(3 * (size_t)nk);
+    for (int iwk = 0; iwk < nk; iwk++) {
+      const long long irec = (long long)iwk * (1 + nband);
+      src.read((irec + 2) * nrecl, nrecl, rec.data());
       int nplane = (int)std::lround(rec[0]);
+      if (nplane < 1 || (long)nplane * 8 > nrecl) throw Error(ERR_IO, "WAVECAR record too short for its bands");
       kpoint_t *kp = new_kpoint(nband, nplane, &rec[1], kws ? kws[iwk % nwk] : 0.0);
       wf->kpts[iwk] = kp;
       kp->up = (short)(iwk / nwk);
       for (int b = 0; b < nband; b++) {
         kp->bands[b]->energy = rec[4 + 3 * b];
         kp->bands[b]->occ = rec[6 + 3 * b];
+        kp->bands[b]->Cs = xmalloc<pawpy_c64>(nplane);
       }
-      std::vector<int> g = enumerate_gvectors(wf->reclattice, kp->k, encut);
-      int ncnt = (int)g.size() / 3;
+      for (int a = 0; a < 3; a++) kvec[3 * iwk + a] = kp->k[a];
+    }
+    // coefficient records: band b of k-point iwk is record 3 + iwk (1 + nband) + b
+    // (reader.c:288-299); only the plane-wave count's bytes are read
+    std::exception_ptr read_err;
+    std::thread reader([&] {
+      try {
+        host_parallel_for(nk * nband, [&](int i) {
+          const int iwk = i / nband, b = i - iwk * nband;
+          kpoint_t *kp = wf->kpts[iwk];
+          const long long irec = (long long)iwk * (1 + nband) + 3 + b;
+          src.read(irec * nrecl, sizeof(pawpy_c64) * kp->num_waves, kp->bands[b]->Cs);
+        });
+      } catch (...) {
+        read_err = std::current_exception();
+      }
+    });
+    std::vector<std::vector<int>> gl;
+    std::exception_ptr g_err;
+    try {
+      gl = gsphere_lists(wf->reclattice, encut, kvec.data(), nk);
+    } catch (...) {
+      g_err = std::current_exception();
+    }
+    reader.join();
+    if (g_err) std::rethrow_exception(g_err);
+    if (read_err) std::rethrow_exception(read_err);
+    for (int iwk = 0; iwk < nk; iwk++) {
+      kpoint_t *kp = wf->kpts[iwk];
+      std::vector<int> &g = gl[iwk];
+      const int nplane = kp->num_waves, ncnt = (int)g.size() / 3;
       if (2 * ncnt == nplane) {
         wf->is_ncl = 1;
         g.insert(g.end(), g.begin(), g.end());
@@ -198,19 +254,34 @@ pswf_t *read_wavecar(const char *path, const double *kws) {
       kp->Gs = xmalloc<int>((size_t)3 * nplane);
       std::copy(g.begin(), g.end(), kp->Gs);
       update_bounds(wf, kp->Gs, ncnt);
-      if ((long)nplane * 8 > nrecl) throw Error(ERR_IO, "WAVECAR record too short for its bands");
-      for (int b = 0; b < nband; b++) {
-        read_rec(irec + 3 + b, cbuf.data());
-        pawpy_c64 *c = xmalloc<pawpy_c64>(nplane);
-        std::memcpy(static_cast<void *>(c), cbuf.data(), sizeof(pawpy_c64) * nplane);
-        kp->bands[b]->Cs = c;
-      }
     }
   } catch (...) {
     free_pswf_all(wf);
     throw;
   }
   return wf;
+}
+
+pswf_t *read_wavecar(const char *path, const double *kws) {
+  WcSource src;
+  src.fd = ::open(path, O_RDONLY | O_CLOEXEC);
+  if (src.fd < 0) throw Error(ERR_IO, std::string("cannot open ") + path);
+  struct Closer {
+    int fd;
+    ~Closer() { ::close(fd); }
+  } closer{src.fd};
+  struct stat st;
+  if (::fstat(src.fd, &st) != 0) throw Error(ERR_IO, std::string("cannot stat ") + path);
+  src.len = (size_t)st.st_size;
+  return read_wavecar_from(src, kws);
+}
+
+pswf_t *read_wavecar_bytes(const char *data, size_t len, const double *kws) {
+  PAWPY_REQUIRE(data != nullptr, "WAVECAR bytes are NULL");
+  WcSource src;
+  src.mem = data;
+  src.len = len;
+  return read_wavecar_from(src, kws);
 }
 
 pswf_t *pswf_from_arrays(int nspin, int nwk, int nband, double encut, const double *lattice,
@@ -361,6 +432,18 @@ pswf_t *pawpy_gpu_read_wavefunctions(const char *filename, const double *kpt_wei
   PAWPY_API_BEGIN
   PAWPY_REQUIRE(filename != nullptr, "filename is NULL");
   return read_wavecar(filename, kpt_weights);
+  PAWPY_API_END(nullptr)
+}
+
+pswf_t *pawpy_gpu_read_wavefunctions_from_str(const char *start, const double *kpt_weights) {
+  PAWPY_API_BEGIN
+  return read_wavecar_bytes(start, SIZE_MAX, kpt_weights);
+  PAWPY_API_END(nullptr)
+}
+
+pswf_t *pawpy_gpu_read_wavefunctions_from_bytes(const char *data, size_t len, const double *kpt_weights) {
+  PAWPY_API_BEGIN
+  return read_wavecar_bytes(data, len, kpt_weights);
   PAWPY_API_END(nullptr)
 }
 

@@ -168,6 +168,18 @@ cudaStream_t stream() {
   return r.s;
 }
 
+bool device_present() {
+  static const bool present = [] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return n > 0;
+  }();
+  return present;
+}
+
 int device() {
   stream();
   return rt().dev;

@@ -12,8 +12,6 @@ import ctypes as C
 import bz2
 import gzip
 import os
-import shutil
-import tempfile
 import time
 
 import numpy as np
@@ -117,22 +115,16 @@ class Wavefunction:
         dim = np.array([vr.parameters["NGX"], vr.parameters["NGY"], vr.parameters["NGZ"]])
         kws = np.ascontiguousarray(vr.actual_kpoints_weights, dtype=np.float64)
         path = str(wavecar)
-        tmp = None
-        # compressed WAVECARs are inflated on the host first (pawpyc.pyx:217-222 reads them
-        # through zopen for names containing .gz or .bz2)
+        # compressed WAVECARs are inflated in memory and read from the bytes (pawpyc.pyx:217-222
+        # reads them through zopen for names containing .gz or .bz2)
         opener = gzip.open if ".gz" in path else bz2.open if ".bz2" in path else None
         if opener is not None:
-            tmp = tempfile.NamedTemporaryFile(delete=False)
             with opener(path, "rb") as src:
-                shutil.copyfileobj(src, tmp)
-            tmp.close()
-            path = tmp.name
-        try:
+                data = src.read()
+            ptr = _lib.lib().pawpy_gpu_read_wavefunctions_from_bytes(data, len(data), kws)
+        else:
             ptr = _lib.lib().pawpy_gpu_read_wavefunctions(path.encode(), kws)
-            _lib.check()
-        finally:
-            if tmp is not None:
-                os.unlink(tmp.name)
+        _lib.check()
         return cls(read_poscar(struct), ptr, CoreRegion(cr), dim, vr.actual_kpoints, kws,
                             vr.parameters["SYMPREC"], setup_projectors)
 

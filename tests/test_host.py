@@ -102,6 +102,51 @@ def test_reference_wavecar_fixture_gsphere(golden):
     assert np.array_equal(gs, g["gs"])
 
 
+def test_wavecar_from_bytes_reads_as_the_file(workload_dirs):
+    """pawpy_gpu_read_wavefunctions_from_bytes / _from_str (read_wavefunctions_from_str,
+    reader.c:324-329) give the file reader's wavefunction; a short buffer is an error."""
+    from pawpyseed_gb300 import _lib
+
+    d = workload_dirs("cfg3s")["basis"]
+    path = os.path.join(d, "WAVECAR")
+    data = open(path, "rb").read()
+    L = _lib.lib()
+    kws = np.ones(64)
+    pf = L.pawpy_gpu_read_wavefunctions(path.encode(), kws)
+    _lib.check()
+    pb = L.pawpy_gpu_read_wavefunctions_from_bytes(data, len(data), kws)
+    _lib.check()
+    ps = L.pawpy_gpu_read_wavefunctions_from_str(data, kws)
+    _lib.check()
+    try:
+        a = pf.contents
+        for p in (pb, ps):
+            b = p.contents
+            assert (a.nspin, a.nwk, a.nband, a.is_ncl) == (b.nspin, b.nwk, b.nband, b.is_ncl)
+            assert [a.G_bounds[i] for i in range(6)] == [b.G_bounds[i] for i in range(6)]
+            for k in range(a.nspin * a.nwk):
+                ka, kb = a.kpts[k].contents, b.kpts[k].contents
+                n = ka.num_waves
+                assert kb.num_waves == n
+                assert np.array_equal(np.ctypeslib.as_array(ka.Gs, shape=(3 * n,)),
+                                      np.ctypeslib.as_array(kb.Gs, shape=(3 * n,)))
+                for band in range(a.nband):
+                    ca = np.ctypeslib.as_array(C.cast(ka.bands[band].contents.Cs, C.POINTER(C.c_float)),
+                                               shape=(2 * n,))
+                    cb = np.ctypeslib.as_array(C.cast(kb.bands[band].contents.Cs, C.POINTER(C.c_float)),
+                                               shape=(2 * n,))
+                    assert np.array_equal(ca, cb)
+                    assert ka.bands[band].contents.energy == kb.bands[band].contents.energy
+    finally:
+        for p in (pf, pb, ps):
+            L.pawpy_gpu_free_pswf(p)
+    short = data[: len(data) - 8]
+    p = L.pawpy_gpu_read_wavefunctions_from_bytes(short, len(short), kws)
+    assert not p
+    assert L.pawpy_gpu_last_error() == 4
+    L.pawpy_gpu_clear_error()
+
+
 def test_reader_errors_are_reported_not_fatal(tmp_path):
     from pawpyseed_gb300 import _lib
 
