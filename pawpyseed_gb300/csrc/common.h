@@ -80,6 +80,9 @@ int device();
 cudaStream_t side_stream();
 // The calling thread's stream for work issued ahead of the library stream's queue.
 cudaStream_t aux_stream();
+// The calling thread's stream above aux_stream, for short launches that the host
+// waits on while long ones run on the auxiliary stream.
+cudaStream_t prio_stream();
 // Whether the calling thread orders its work on a stream of its own (pawpy_gpu_thread_stream).
 bool thread_has_stream();
 struct OnStream {

@@ -722,8 +722,26 @@ struct SphereJob {
 };
 
 // Sphere tables of several sets with one host round trip: every set's slab counts are
-// launched and read back together, then every set is compacted and tabulated.
+// launched and read back together, then every set is compacted and tabulated. The counts,
+// their read-back and the index lists run on the priority stream (after the library
+// stream's work so far; the library stream then waits for them), so that the host's wait
+// for the counts does not last as long as a first FFT pass on the auxiliary stream.
+static void build_sphere_sets_on(std::vector<SphereJob> &jobs);
 static void build_sphere_sets(std::vector<SphereJob> &jobs) {
+  const cudaStream_t lib = stream();
+  OwnedEvent start, done;
+  start.record(lib);
+  {
+    OnStream on(prio_stream());
+    start.wait(stream());
+    build_sphere_sets_on(jobs);
+    // the jobs' buffers, allocated on the priority stream, are freed on the library stream
+    done.record(stream());
+  }
+  done.wait(lib);
+}
+
+static void build_sphere_sets_on(std::vector<SphereJob> &jobs) {
   HostPhase hp("spheres");
   auto cross = [](const double *a, const double *b, double *o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
@@ -922,6 +940,8 @@ static bool plane_geom(DevWF &d, int k, PlaneGeom &g) {
 
 // Largest H of all k-points that the early first FFT pass may hold.
 constexpr long long kEarlyPlanesBytes = 8LL << 30;
+// Bands per launch of the early first pass.
+constexpr int kEarlyChunkBands = 128;
 
 static long long l2_bytes() {
   static long long v = -1;
@@ -980,8 +1000,12 @@ static void transform_planes_early(DevWF &d) {
     OnStream on(xs);
     for (int k = 0; k < d.nk; k++) {
       DevKpt &q = d.kp[k];
-      launch_fft_planes_fast(coeffs(d, k), q.Wpad, q.plane_start.p, q.plane_off.p, geo[k], d.Hall.p + off[k],
-                             d.nband);
+      // in launches of kEarlyChunkBands bands: the launches on the priority stream (sphere
+      // counts and index lists) are dispatched when a launch's blocks retire
+      const size_t hb = (size_t)q.n1 * d.N[1] * d.N[2];
+      for (int b0 = 0; b0 < d.nband; b0 += kEarlyChunkBands)
+        launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
+                               d.Hall.p + off[k] + b0 * hb, std::min(kEarlyChunkBands, d.nband - b0));
       PAWPY_CUDA(cudaEventRecord(d.h_ev[k], xs));
     }
   }
@@ -1427,9 +1451,6 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   for (int e = 0; e < num_elems; e++) pps[e].num_cart_gridpts = cart_gridpts_bound(pps[e], wf->lattice, fftg);
   set_grid(d, fftg);
   ensure_all_planes(d);
-  // with the projections deferred to overlap_setup_real, the first FFT pass runs now, beside the
-  // table and sphere work below
-  if (!g_host_proj) transform_planes_early(d);
   d.species.clear();
   for (int e = 0; e < num_elems; e++) d.species.push_back(species_tables(pps[e]));
   d.labels.assign(labels, labels + num_sites);
@@ -1438,6 +1459,10 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   std::iota(all.begin(), all.end(), 0);
   build_spheres(d.proj, all, d.labels.data(), d.coords.data(), d.species, false, d.lattice, d.N, d.vol, d.kp,
                 d.rec);
+  // with the projections deferred to overlap_setup_real, the first FFT pass runs from here on,
+  // beside the sphere and pair work of overlap_setup_real (issued after the projector spheres,
+  // whose point counts the host reads back: those then run on an idle device)
+  if (!g_host_proj) transform_planes_early(d);
   d.site_lmoff.resize(num_sites);
   for (int s = 0; s < num_sites; s++) d.site_lmoff[s] = d.proj.host[s].lm_off;
   d.P.alloc((size_t)d.nk * d.nband * d.proj.Ptot);

@@ -260,12 +260,13 @@ __global__ void __launch_bounds__(FT) k_planes_direct(const float2 *__restrict__
 // The pick of one plane: value at tile offset pto (row * LD + column of the transformed plane)
 // times the point's Bloch phase (phase == nullptr: the k-point is Gamma, the phase is 1), to its
 // position in the picked-point row of band b. The lists are read from global memory (L2) U
-// points per thread at a time, all loads in flight before the stores.
+// points per thread at a time, all loads in flight before the stores: the phase is bound by
+// the latency of those loads, so U is as large as the registers of the line transform allow.
+template <int U = 8>
 __device__ __forceinline__ void pick_plane(const float2 *tile, const int *__restrict__ pto,
                                            const int *__restrict__ xo, const float2 *__restrict__ phase, int npj,
                                            int t0, int nt, float2 *X, long long b, long long xstride,
                                            long long lo_words) {
-  constexpr int U = 8;
   for (int q0 = t0; q0 < npj; q0 += nt * U) {
     int c[U], o[U];
     float2 f[U];
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
 // through L1 (consecutive CTAs share a plane).
 // (three CTAs per SM: the 90^3 tile allows three in shared memory, and the register cap that
 // gives them costs a few spilled values of the line transform)
-template <int N1, int N3, int T1>
+template <int N1, int N3, int T1, int U>
 __global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict__ H, int nb, PlaneGeom g,
                                                      const int *__restrict__ plane_first,
                                                      const int *__restrict__ cell, const int *__restrict__ xo,
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict
   __syncthreads();
   if (!band_ok) return;
   const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
-  pick_plane(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, gt, TPB, X, b, xstride, lo_words);
+  pick_plane<U>(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, gt, TPB, X, b, xstride, lo_words);
 }
 
 // Pass B writing whole grids (resident real-space wavefunctions): grid

@@ -19,11 +19,14 @@ PickFn find_pick(int n1, int n3) {
   return nullptr;
 }
 
-DirectFn find_direct(int n1, int n3, int *bpc) {
-#define X(a, b)                     \
-  if (n1 == a && n3 == b) {         \
-    *bpc = direct_bands(a, b);      \
-    return k_xpick_direct<a, b, direct_lanes(a)>; \
+// the direct kernel picking u = 8, 16 or 32 points per thread at a time
+DirectFn find_direct(int n1, int n3, int u, int *bpc) {
+#define X(a, b)                                                         \
+  if (n1 == a && n3 == b) {                                             \
+    *bpc = direct_bands(a, b);                                          \
+    if (u == 32) return k_xpick_direct<a, b, direct_lanes(a), 32>;      \
+    if (u == 16) return k_xpick_direct<a, b, direct_lanes(a), 16>;      \
+    return k_xpick_direct<a, b, direct_lanes(a), 8>;                    \
   }
   PAWPY_FFT_PAIRS(X)
 #undef X
@@ -66,15 +69,17 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   // at Gamma every Bloch phase is 1: no phase list
   const float2 *ph = gamma ? nullptr : pl.phase + (long long)kq * pl.npts;
   int bpc = 1;
-  DirectFn dfn = find_direct(g.N1, g.N3, &bpc);
+  DirectFn dfn[3];
+  for (int v = 0; v < 3; v++) dfn[v] = find_direct(g.N1, g.N3, 8 << v, &bpc);
   const size_t dsmem = xpick_direct_smem(g, bpc);
-  allow_smem((const void *)dfn, dsmem);
-  // candidates: 1, 2, 4 band groups per plane of the pipelined kernel; 0 the direct kernel
+  for (DirectFn f : dfn) allow_smem((const void *)f, dsmem);
+  // candidates: 1, 2, 4 band groups per plane of the pipelined kernel; 0, -1, -2 the direct
+  // kernel picking 8, 16, 32 points per thread at a time
   auto run = [&](int mult) {
-    if (mult == 0) {
+    if (mult <= 0) {
       dim3 grid(ceil_div(nb, bpc), g.N2);
-      PAWPY_LAUNCH("fft_x_pick", dfn<<<grid, FT, dsmem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, X,
-                                                                    xstride, lo_words));
+      PAWPY_LAUNCH("fft_x_pick", dfn[-mult]<<<grid, FT, dsmem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo,
+                                                                           ph, X, xstride, lo_words));
       return;
     }
     const int G = std::max(1, std::min(nb, ceil_div((long long)waves * mult, g.N2)));
@@ -82,7 +87,7 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
     PAWPY_LAUNCH("fft_x_pick", fn<<<grid, FT, smem, stream()>>>(H, nb, g, pl.plane_first, pl.cell, pl.xo, ph, cap, X,
                                                                 xstride, lo_words));
   };
-  int mult = tune(std::make_tuple((lo_words ? 3 : 1) + (gamma ? 4 : 0), g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
+  int mult = tune(std::make_tuple((lo_words ? 3 : 1) + (gamma ? 4 : 0), g.N1, g.N2, g.N3), {0, -1, -2, 1, 2, 4}, run);
   run(mult);
   note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
 }

@@ -132,6 +132,9 @@ static thread_local cudaStream_t t_side = nullptr;
 // ...and a third for work issued ahead of the main stream's queue (the first FFT
 // pass of a wavefunction whose projections come later, sphere-table values).
 static thread_local cudaStream_t t_aux = nullptr;
+// ...and a fourth, above the third, for short work that the host waits on while
+// the third is busy (the sphere point counts and index lists).
+static thread_local cudaStream_t t_prio = nullptr;
 
 cudaStream_t side_stream() {
   if (!t_side) {
@@ -149,12 +152,23 @@ cudaStream_t aux_stream() {
   if (!t_aux) {
     stream();
     // high priority: its launches (the first FFT pass, the sphere tables' values and planes)
-    // are dispatched ahead of the waiting blocks of a long launch on the library stream
+    // are dispatched ahead of the waiting blocks of a long launch on the library stream; one
+    // level below the highest, which the sphere lists use (prio_stream)
     int lo = 0, hi = 0;
     PAWPY_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    PAWPY_CUDA(cudaStreamCreateWithPriority(&t_aux, cudaStreamNonBlocking, hi));
+    PAWPY_CUDA(cudaStreamCreateWithPriority(&t_aux, cudaStreamNonBlocking, hi < lo ? hi + 1 : hi));
   }
   return t_aux;
+}
+
+cudaStream_t prio_stream() {
+  if (!t_prio) {
+    stream();
+    int lo = 0, hi = 0;
+    PAWPY_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PAWPY_CUDA(cudaStreamCreateWithPriority(&t_prio, cudaStreamNonBlocking, hi));
+  }
+  return t_prio;
 }
 
 OnStream::OnStream(cudaStream_t s) : prev(t_stream) { t_stream = s; }
@@ -545,7 +559,7 @@ int pawpy_gpu_thread_stream(int on) {
       }
       ring_free(r);
     }
-    for (cudaStream_t *ps : {&t_side, &t_aux})
+    for (cudaStream_t *ps : {&t_side, &t_aux, &t_prio})
       if (*ps) {
         cudaStream_t u = *ps;
         *ps = nullptr;
@@ -610,6 +624,7 @@ void pawpy_gpu_synchronize(void) {
   // uploads and early transforms on the thread's other streams count as the library's work
   if (t_side) PAWPY_CUDA(cudaStreamSynchronize(t_side));
   if (t_aux) PAWPY_CUDA(cudaStreamSynchronize(t_aux));
+  if (t_prio) PAWPY_CUDA(cudaStreamSynchronize(t_prio));
   pawpy::sync();
   PAWPY_API_END()
 }
