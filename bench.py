@@ -325,12 +325,13 @@ FFT_TRAFFIC = {
 def roofline(stats, w, basis, wf, lists, cr):
     """Dominant kernel family of one profiled step: achieved algorithmic rate against the measured peak.
 
-    The library's launches declare their algorithmic work while profiling: 8 N1 N2 N3 bytes per
-    band and FFT pass (so 16 N^3 per band-FFT over the two passes: one complex64 read and write
-    of the grid), 8 bytes per picked value the sphere contraction reads, and 8 M N K useful flops
-    of the overlap contraction per k-point (K: plane waves plus augmentation columns). achieved =
-    the family's declared work in the step / its device time in the step (CUDA events around
-    every launch, on the stream it runs on); per-launch work is uniform within a family.
+    The library's launches declare their algorithmic work while profiling: per band, the first
+    FFT pass reads the coefficients and writes the occupied planes of H (8 (W + n1 N2 N3) bytes),
+    the second reads those planes and writes the picked values (8 (n1 N2 N3 + picked points)
+    bytes: complex64, or BF16 hi and lo words); 8 bytes per picked value the sphere contraction
+    reads; 8 M N K useful flops of the overlap contraction per k-point (K: plane waves plus
+    augmentation columns). achieved = the family's declared work in the step / its device time in
+    the step (CUDA events around every launch, on the stream it runs on).
     """
     hbm, tc, src = peaks()
     if not stats:
@@ -367,8 +368,7 @@ def roofline(stats, w, basis, wf, lists, cr):
     else:
         out.update(bound="hbm", achieved=None, peak=hbm, unit="GB/s", frac=None)
     if fam == "fft":
-        N3 = int(np.prod(w["dim"]))
-        out.update(algorithmic_bytes_per_band_fft=16.0 * N3)
+        out.update(algorithmic_bytes_per_band_fft=work / (wf.nband * wf.nwk * wf.nspin))
         t = FFT_TRAFFIC.get(tuple(int(x) for x in w["dim"]))
         if t is not None:
             out.update(traffic=t, traffic_unit="bytes per band-FFT (ncu dram__bytes_read+write, both passes)")

@@ -1131,18 +1131,16 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   seg_base_d.upload(seg_base.data(), seg_base.size());
   plane_first_d.upload(plane_first.data(), plane_first.size());
   const long long npick = plane_first[d.N[1]];
-  DevBuf<int> pick_cell(std::max(1LL, npick)), pick_xo(std::max(1LL, npick));
+  DevBuf<uint2> pick_ent(std::max(1LL, npick));
   DevBuf<float2> pick_phase(std::max(1LL, npick * d.nk));
   PickList plist;
   plist.plane_first = plane_first_d.p;
-  plist.cell = pick_cell.p;
-  plist.xo = pick_xo.p;
+  plist.ent = pick_ent.p;
   plist.phase = pick_phase.p;
   plist.npts = npick;
   plist.max_plane_pts = max_plane_pts;
   for (size_t i = 0; i < sets.size(); i++)
     PAWPY_REQUIRE(sets[i]->nkp == d.nk, "sphere tables and wavefunction differ in k-points");
-  launch_flatten_pick(segs_d.p, seg_base_d.p, (int)sorted.size(), d.nk, d.N[2], plist);
   DevBuf<int> pstart_d(pstart.size());
   pstart_d.upload(pstart.data(), pstart.size());
   DevBuf<ChunkContract> ch_d(std::max<size_t>(1, chunks.size()));
@@ -1309,6 +1307,10 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
   }
   DevBuf<float2> partial(tc ? 1 : (size_t)cbatch * std::max(1, ptot));
   if (xtot == 0) return;
+  // the pick entries carry the offsets of the values in a band's row (32-bit)
+  PAWPY_REQUIRE(!split_x || ((xtot + 15) / 16) * pick_stride < (1LL << 32), "picked rows too large for 32-bit offsets");
+  if (!gather) launch_flatten_pick(segs_d.p, seg_base_d.p, (int)sorted.size(), d.nk, d.N[2], split_x ? pick_stride : 0,
+                                   plist);
   for (long long r0 = 0; r0 < rows; r0 += cbatch) {
     const long long r1 = std::min(rows, r0 + cbatch);
     if (split_x) launch_zero_picked_blocks(X.p, tail_blocks.p, ntail, cbatch * 16, (int)(r1 - r0), lo_words);
@@ -1339,7 +1341,8 @@ static void project_bands(DevWF &d, const std::vector<const SphereSet *> &sets,
         } else {
           launch_fft_planes(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, g,
                             d.r[1], d.r[2], d.tw[1].p, d.tw[2].p, H.p, nb);
-          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, pick_stride, nb, lo_words);
+          launch_fft_x_pick(H.p, g, d.r[0], d.tw[0].p, segs_d.p, pstart_d.p, k, xb, pick_stride, nb, lo_words,
+                            plist.npts);
         }
       }
     }

@@ -257,40 +257,80 @@ __global__ void __launch_bounds__(FT) k_planes_direct(const float2 *__restrict__
 // the plane's H rows of the current and the next band (cp.async), tile
 // [N1][LD] the transformed plane and, when the plane has at most pts_cap
 // points, a copy of its pick list (the same for every band).
-// The pick of one plane: value at tile offset pto (row * LD + column of the transformed plane)
-// times the point's Bloch phase (phase == nullptr: the k-point is Gamma, the phase is 1), to its
-// position in the picked-point row of band b. The lists are read from global memory (L2) U
-// points per thread at a time, all loads in flight before the stores: the phase is bound by
-// the latency of those loads, so U is as large as the registers of the line transform allow.
-template <int U = 8>
-__device__ __forceinline__ void pick_plane(const float2 *tile, const int *__restrict__ pto,
-                                           const int *__restrict__ xo, const float2 *__restrict__ phase, int npj,
-                                           int t0, int nt, float2 *X, long long b, long long xstride,
+// The pick of one plane from a tile of transformed values: the value at tile offset e.x
+// (row * LD + column of the plane) times the point's Bloch phase (phase == nullptr: the k-point
+// is Gamma, the phase is 1), to offset e.y of the band's picked row Xrow: complex64 values
+// (lo_words == 0), or BF16 (re, im) words of the split form, the lo word lo_words after the hi
+// word (the entries carry the K-block offsets, bf16split.cuh). The entries are read from global
+// memory (L2) U at a time per thread, all loads in flight before the stores.
+template <int U>
+__device__ __forceinline__ void pick_plane(const float2 *tile, const uint2 *__restrict__ ent,
+                                           const float2 *__restrict__ phase, int npj, int t0, int nt, void *Xrow,
                                            long long lo_words) {
   for (int q0 = t0; q0 < npj; q0 += nt * U) {
-    int c[U], o[U];
+    uint2 e[U];
     float2 f[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int q = q0 + u * nt;
       if (q < npj) {
-        c[u] = __ldg(pto + q);
-        o[u] = __ldg(xo + q);
+        e[u] = __ldg(ent + q);
         if (phase) f[u] = __ldg(phase + q);
       }
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int q = q0 + u * nt;
-      if (q < npj) put_picked(X, b, xstride, lo_words, o[u], phase ? cmul(tile[c[u]], f[u]) : tile[c[u]]);
+      if (q < npj) {
+        const float2 v = phase ? cmul(tile[e[u].x], f[u]) : tile[e[u].x];
+        if (lo_words) {
+          uint32_t h, l;
+          split_bf16x2(v, h, l);
+          uint32_t *w = static_cast<uint32_t *>(Xrow) + e[u].y;
+          w[0] = h;
+          w[lo_words] = l;
+        } else {
+          static_cast<float2 *>(Xrow)[e[u].y] = v;
+        }
+      }
     }
   }
+}
+
+// The same from a tile held already split (thi, tlo: the hi and lo words of the transformed
+// values; Gamma point, split rows): two words copied per point.
+template <int U>
+__device__ __forceinline__ void pick_plane_split(const uint32_t *thi, const uint32_t *tlo, const uint2 *__restrict__ ent,
+                                                 int npj, int t0, int nt, uint32_t *Xrow, long long lo_words) {
+  for (int q0 = t0; q0 < npj; q0 += nt * U) {
+    uint2 e[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * nt;
+      if (q < npj) e[u] = __ldg(ent + q);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * nt;
+      if (q < npj) {
+        uint32_t *w = Xrow + e[u].y;
+        w[0] = thi[e[u].x];
+        w[lo_words] = tlo[e[u].x];
+      }
+    }
+  }
+}
+
+// the band's picked row: 16 words per row within a K block (split form), xstride values otherwise
+__device__ __forceinline__ void *picked_row(float2 *X, long long b, long long xstride, long long lo_words) {
+  return lo_words ? static_cast<void *>(reinterpret_cast<uint32_t *>(X) + b * 16)
+                  : static_cast<void *>(X + b * xstride);
 }
 
 template <int N1, int N3>
 __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H, int nb, PlaneGeom g,
                                                    const int *__restrict__ plane_first,
-                                                   const int *__restrict__ cell, const int *__restrict__ xo,
+                                                   const uint2 *__restrict__ ent,
                                                    const float2 *__restrict__ phase, int pts_cap,
                                                    float2 *__restrict__ X, long long xstride, long long lo_words) {
   constexpr int LD = padded(N3);
@@ -300,8 +340,7 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
   float2 *stage = reinterpret_cast<float2 *>(smraw);
   float2 *tile = stage + 2 * per;
   float2 *pph = tile + N1 * LD;
-  int *pto = reinterpret_cast<int *>(pph + pts_cap);
-  int *pxo = pto + pts_cap;
+  uint2 *pent = reinterpret_cast<uint2 *>(pph + pts_cap);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int j = blockIdx.x, G = gridDim.y;
   const int s1 = wrapi(g.g1min, N1);
@@ -321,8 +360,7 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
   if (b < nb) prefetch(b, 0);
   if (staged)
     for (int q = threadIdx.x; q < npj; q += blockDim.x) {
-      pto[q] = cell[pf + q];
-      pxo[q] = xo[pf + q];
+      pent[q] = ent[pf + q];
       pph[q] = phase ? phase[pf + q] : make_float2(1.f, 0.f);
     }
   for (int it = 0; b < nb; it++, b += G) {
@@ -356,12 +394,22 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
       }
     }
     __syncthreads();
+    void *xr = picked_row(X, b, xstride, lo_words);
     if (staged) {
-      for (int q = threadIdx.x; q < npj; q += blockDim.x)
-        put_picked(X, b, xstride, lo_words, pxo[q], cmul(tile[pto[q]], pph[q]));
+      for (int q = threadIdx.x; q < npj; q += blockDim.x) {
+        const float2 v = cmul(tile[pent[q].x], pph[q]);
+        if (lo_words) {
+          uint32_t h, l;
+          split_bf16x2(v, h, l);
+          uint32_t *w = static_cast<uint32_t *>(xr) + pent[q].y;
+          w[0] = h;
+          w[lo_words] = l;
+        } else {
+          static_cast<float2 *>(xr)[pent[q].y] = v;
+        }
+      }
     } else {
-      pick_plane(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, threadIdx.x, blockDim.x, X, b, xstride,
-                         lo_words);
+      pick_plane<8>(tile, ent + pf, phase ? phase + pf : nullptr, npj, threadIdx.x, blockDim.x, xr, lo_words);
     }
   }
 }
@@ -371,13 +419,16 @@ __global__ void __launch_bounds__(FT) k_xpick_pipe(const float2 *__restrict__ H,
 // threads, one band each; a group loads plane j of its band from H straight
 // into registers (all loads of a lane in flight at once), transforms the
 // first axis into its shared tile [N1][LD] and picks from the flat list
-// through L1 (consecutive CTAs share a plane).
+// through L1 (consecutive CTAs share a plane). STILE (Gamma point, split rows):
+// the transform's outputs are split into BF16 hi and lo words as they enter the
+// tile (two planes of [N1][LD] words, the same bytes), once per grid point
+// instead of once per picked point, and the pick copies words.
 // (three CTAs per SM: the 90^3 tile allows three in shared memory, and the register cap that
 // gives them costs a few spilled values of the line transform)
-template <int N1, int N3, int T1, int U>
+template <int N1, int N3, int T1, bool STILE>
 __global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict__ H, int nb, PlaneGeom g,
                                                      const int *__restrict__ plane_first,
-                                                     const int *__restrict__ cell, const int *__restrict__ xo,
+                                                     const uint2 *__restrict__ ent,
                                                      const float2 *__restrict__ phase, float2 *__restrict__ X,
                                                      long long xstride, long long lo_words) {
   constexpr int LD = padded(N3), L1 = N1 / T1;
@@ -387,6 +438,7 @@ __global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict
   extern __shared__ __align__(16) unsigned char smraw[];
   const int grp = threadIdx.x / TPB, gt = threadIdx.x - grp * TPB;
   float2 *tile = reinterpret_cast<float2 *>(smraw) + grp * (N1 * LD);
+  uint32_t *thi = reinterpret_cast<uint32_t *>(tile), *tlo = thi + N1 * LD;
   const int warp = gt >> 5, lane = threadIdx.x & 31;
   const int b = blockIdx.x * BPC + grp, j = blockIdx.y;
   const int n1 = g.n1, s1 = wrapi(g.g1min, N1);
@@ -407,16 +459,26 @@ __global__ void __launch_bounds__(FT, 3) k_xpick_direct(const float2 *__restrict
       }
       reg::line_fft<N1, T1, 1>(x, h);
       if (ok) {
-        float2 *tp = tile + (L1 * reg::bitrev(h, T1)) * LD + z;
+        const int t0 = (L1 * reg::bitrev(h, T1)) * LD + z;
+        if constexpr (STILE) {
 #pragma unroll
-        for (int k = 0; k < L1; k++) tp[k * LD] = x[k];
+          for (int k = 0; k < L1; k++) split_bf16x2(x[k], thi[t0 + k * LD], tlo[t0 + k * LD]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < L1; k++) tile[t0 + k * LD] = x[k];
+        }
       }
     }
   }
   __syncthreads();
   if (!band_ok) return;
   const int pf = plane_first[j], npj = plane_first[j + 1] - pf;
-  pick_plane<U>(tile, cell + pf, xo + pf, phase ? phase + pf : nullptr, npj, gt, TPB, X, b, xstride, lo_words);
+  if constexpr (STILE)
+    pick_plane_split<16>(thi, tlo, ent + pf, npj, gt, TPB, reinterpret_cast<uint32_t *>(X) + (long long)b * 16,
+                         lo_words);
+  else
+    pick_plane<16>(tile, ent + pf, phase ? phase + pf : nullptr, npj, gt, TPB, picked_row(X, b, xstride, lo_words),
+                   lo_words);
 }
 
 // Pass B writing whole grids (resident real-space wavefunctions): grid

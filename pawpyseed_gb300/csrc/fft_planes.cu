@@ -59,7 +59,8 @@ void launch_fft_planes_fast(const float2 *C, int Wpad, const int *plane_start, c
   };
   int mult = tune(std::make_tuple(0, g.N1, g.N2, g.N3), {0, 1, 2, 4}, run);
   run(mult);
-  note_work("fft_planes", 8.0 * g.N1 * g.N2 * g.N3 * nb);
+  // algorithmic bytes: the coefficients read, the occupied planes of H written
+  note_work("fft_planes", 8.0 * ((double)Wpad + (double)g.n1 * g.N2 * g.N3) * nb);
 }
 
 }  // namespace pawpy

@@ -116,7 +116,7 @@ void launch_fft_planes(const float2 *C, int Wpad, const int *plane_start, const 
   dim3 grid(g.n1, nb);
   PAWPY_LAUNCH("fft_planes", k_fft_planes<<<grid, 256, smem, stream()>>>(C, Wpad, plane_start, plane_off,
                                                                           g, r2, r3, tw2, tw3, H));
-  note_work("fft_planes", 8.0 * g.N1 * g.N2 * g.N3 * nb);
+  note_work("fft_planes", 8.0 * ((double)Wpad + (double)g.n1 * g.N2 * g.N3) * nb);
 }
 
 // Generic: one CTA per (line group along `axis`, band); lines are loaded whole.

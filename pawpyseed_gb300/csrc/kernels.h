@@ -39,9 +39,12 @@ struct GatherSeg;
 // lie in plane j of the second axis; cell is the point's offset i*LD + k in the
 // transformed plane's shared tile (LD the padded row length), xo the position in
 // the picked-point vector, phase[kq*npts + q] the Bloch phase.
+// ent[q] = (offset of the point in the transformed plane's shared tile, offset of its value in
+// a band's picked row: K-block word offset (pos / 16) * kb_words + pos % 16 of the split form,
+// or the position pos in a complex64 row)
 struct PickList {
   const int *plane_first = nullptr;
-  int *cell = nullptr, *xo = nullptr;
+  uint2 *ent = nullptr;
   float2 *phase = nullptr;
   long long npts = 0;
   int max_plane_pts = 0;
@@ -58,8 +61,10 @@ __host__ __device__ inline long long grid_value_index(int b, long long cell, lon
 }
 // pass B writing whole grids of bands [b0, b0 + nb) of one k-point (register sizes only)
 void launch_fft_x_grid(const float2 *H, const PlaneGeom &g, float2 *grid, int b0, int nb);
-// fills pl.cell/xo/phase from segments sorted by plane; base[si] = first flat position of segment si
-void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, int N3, PickList &pl);
+// fills pl.ent/phase from segments sorted by plane; base[si] = first flat position of segment si;
+// kb_words > 0: row offsets of the split form (K blocks kb_words words apart), 0: complex64 rows
+void launch_flatten_pick(const GatherSeg *segs, const int *base, int nsegs, int nkp, int N3, long long kb_words,
+                         PickList &pl);
 // Generic in-place transform of full grids along one axis (single-band paths).
 void launch_fft_axis(float2 *grid, int nb, int N1, int N2, int N3, int axis, const Radices &r,
                      const float2 *tw);
@@ -175,9 +180,10 @@ void launch_seg_fill(const SiteDesc *sites, const SegFill *segs, int nseg, const
                      long long total_pts, int *idx, float2 *tab, float2 *phase, int what = 3);
 // x-axis transform of each plane j of nb bands, then X[b][x_off + p] = u(point p) exp(i k.path_p) for
 // the segments of plane j (segs sorted by plane; plane_start[N2+1])
+// (npicked: the points the segments pick, for the launch's algorithmic bytes)
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
                        const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb,
-                       long long lo_words = 0);
+                       long long lo_words, long long npicked);
 // P[(band_base + b)*Ptot + o] = sum over c < col[o].y of partial[b][col[o].x + c*col[o].z]: the
 // chunks of column o's site, in chunk order
 void launch_chunk_reduce(const float2 *partial, int ptot, const int4 *col, float2 *P, int Ptot, int nb,

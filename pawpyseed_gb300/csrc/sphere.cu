@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256) k_fft_x_pick(const float2 *__restrict__ H
 
 void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, const float2 *tw1,
                        const GatherSeg *segs, const int *plane_start, int kq, float2 *X, long long xstride, int nb,
-                       long long lo_words) {
+                       long long lo_words, long long npicked) {
   if (nb <= 0) return;
   size_t smem = sizeof(float2) * (2 * (size_t)g.N1 * g.N3 + g.N1);
   PAWPY_REQUIRE(smem <= 227 * 1024, "FFT tile does not fit in shared memory");
@@ -332,7 +332,7 @@ void launch_fft_x_pick(const float2 *H, const PlaneGeom &g, const Radices &r1, c
   dim3 grid(g.N2, nb);
   PAWPY_LAUNCH("fft_x_pick", k_fft_x_pick<<<grid, 256, smem, stream()>>>(H, g, r1, tw1, segs, plane_start, kq, X,
                                                                         xstride, lo_words));
-  note_work("fft_x_pick", 8.0 * g.N1 * g.N2 * g.N3 * nb);
+  note_work("fft_x_pick", 8.0 * ((double)g.n1 * g.N2 * g.N3 + (double)npicked) * nb);
 }
 
 // ---------------------------------------------------------------------------
