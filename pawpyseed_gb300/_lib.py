@@ -46,7 +46,7 @@ def _declare(L):
     L.pawpy_gpu_read_wavefunctions_from_bytes.restype = _wfp
     L.pawpy_gpu_read_wavefunctions_from_bytes.argtypes = [C.c_char_p, C.c_size_t, _dp]
     L.pawpy_gpu_gvectors.restype = C.c_int
-    L.pawpy_gpu_gvectors.argtypes = [_dp, _dp, C.c_double, _ip, C.c_int]
+    L.pawpy_gpu_gvectors.argtypes = [_dp, _dp, C.c_double, C.c_void_p, C.c_int]
     L.pawpy_gpu_wavefunction_from_arrays.restype = _wfp
     L.pawpy_gpu_wavefunction_from_arrays.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
                                                     _ip, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),

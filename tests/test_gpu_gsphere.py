@@ -72,7 +72,7 @@ def device_gvectors(lattice, kpt, encut):
     n = L.pawpy_gpu_gvectors(lat, k, float(encut), None, 0)
     _lib.check()
     out = np.zeros((max(n, 1), 3), dtype=np.int32)
-    m = L.pawpy_gpu_gvectors(lat, k, float(encut), out.reshape(-1), n)
+    m = L.pawpy_gpu_gvectors(lat, k, float(encut), out.ctypes.data, n)
     _lib.check()
     assert m == n
     return out[:n]
