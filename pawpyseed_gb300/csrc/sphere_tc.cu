@@ -73,9 +73,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int bn) {
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// 8-byte cp.async; src_bytes 0 fills the destination with zeros
+// 8- and 16-byte cp.async; src_bytes 0 fills the destination with zeros
 __device__ __forceinline__ void cpa8z(uint32_t dst, const void *src, int src_bytes) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cpa16z(uint32_t dst, const void *src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -235,51 +238,56 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
       umma_commit(smem_u32(&bar_drain));
     }
   } else if (GATHER && warp < 2 + C::CONV) {
-    // converters, thread ct -> row ct % 128 (band b0 + row) and points [8 (ct / 128), +8) of
-    // each K block: a warp's copies read 32 consecutive bands of one grid cell (two 128-byte
-    // lines of the band-tiled grid) into the slot's [point][row] staging layout (consecutive
-    // 8-byte destinations), and its 16-byte operand stores of 8 consecutive rows hit distinct
-    // banks of the swizzled tile. Every converter thread runs every iteration (the named
-    // barriers need all of them); after an abort the waits return at once and the conversions
-    // are skipped.
+    // converters. Copies: thread ct -> rows 2 (ct % 64) and 2 (ct % 64) + 1 (bands b0 + row,
+    // 16 contiguous bytes of the band-tiled grid) and points [4 (ct / 64), +4) of each K block:
+    // a warp's copies read 32 bands of one grid cell (two 128-byte lines) into the slot's
+    // [point][row] staging layout. Conversion: thread ct -> row ct % 128 and points
+    // [8 (ct / 128), +8): its 16-byte operand stores of 8 consecutive rows hit distinct banks of
+    // the swizzled tile. Every converter thread runs every iteration (the named barriers need
+    // all of them); after an abort the waits return at once and the conversions are skipped.
     static_assert(!GATHER || C::CONV * 32 == 2 * STM, "two converter threads per row");
-    constexpr int NCT = 32 * C::CONV, STG = C::STG, D = STG - 1, PPT = KPTS / 2;
+    constexpr int NCT = 32 * C::CONV, STG = C::STG, D = STG - 1, PPT = KPTS / 2, CPT = KPTS / 4;
     const int ct = threadIdx.x - 64, row = ct & (STM - 1), pbase = (ct / STM) * PPT;
-    // rows are bands b0 + row of k-point kq (a tile never crosses a k-point): the value at cell c
-    // is at growp + 16 c (grid_value_index with the band part hoisted)
+    const int crow = 2 * (ct & 63), cbase = (ct >> 6) * CPT;
+    // rows are bands b0 + row of k-point kq (a tile never crosses a k-point and starts on a
+    // multiple of 16 bands): the pair of rows at cell c starts at growp + 16 c (grid_value_index
+    // with the band part hoisted)
     const int b0 = (int)(src.r0 + row0 - kq * src.nband);
-    const float2 *growp = src.grid + kq * src.gstride + grid_value_index(b0 + row, 0, src.n3d);
-    int cell_next[PPT];
+    const float2 *growp = src.grid + kq * src.gstride + grid_value_index(b0 + crow, 0, src.n3d);
+    int cell_next[CPT];
     auto load_cells = [&](int i) {
+      const long long x = st.a_x + (long long)i * KPTS + cbase;
+      if (i < nkb && x + CPT <= src.npts) {
+        const int4 v = __ldg(reinterpret_cast<const int4 *>(src.gcell + x));
+        cell_next[0] = v.x, cell_next[1] = v.y, cell_next[2] = v.z, cell_next[3] = v.w;
+      } else {
 #pragma unroll
-      for (int pp = 0; pp < PPT; pp++) {
-        const long long x = st.a_x + (long long)i * KPTS + pbase + pp;
-        cell_next[pp] = (i < nkb && x < src.npts) ? __ldg(src.gcell + x) : -1;
+        for (int pp = 0; pp < CPT; pp++) cell_next[pp] = (i < nkb && x + pp < src.npts) ? __ldg(src.gcell + x + pp) : -1;
       }
     };
     load_cells(0);
     auto issue = [&](int i) {
       if (i < nkb) {
         const int t = i % STG;
-        int cell[PPT];
+        int cell[CPT];
 #pragma unroll
-        for (int pp = 0; pp < PPT; pp++) cell[pp] = cell_next[pp];
+        for (int pp = 0; pp < CPT; pp++) cell[pp] = cell_next[pp];
         load_cells(i + 1);
         const uint32_t slot = stg_base + t * C::STG_BYTES;
 #pragma unroll
-        for (int pp = 0; pp < PPT; pp++) {
-          const int p = pbase + pp;
-          const bool ok = cell[pp] >= 0 && row < nrows;
+        for (int pp = 0; pp < CPT; pp++) {
+          const int p = cbase + pp;
+          const bool ok = cell[pp] >= 0 && crow < nrows;
           const float2 *g = ok ? growp + 16 * cell[pp] : src.grid;
-          cpa8z(slot + (p * STM + row) * 8, g, ok ? 8 : 0);
+          cpa16z(slot + (p * STM + crow) * 8, g, ok ? 16 : 0);
         }
         if (row == 0 && !src.gamma) {
-          // gaps between sites have cell -1: a zero phase
+          // the points' Bloch phases (a gap's value is zero: any finite phase will do)
 #pragma unroll
           for (int pp = 0; pp < PPT; pp++) {
             const int p = pbase + pp;
             const long long x = st.a_x + (long long)i * KPTS + p;
-            const bool ok = cell[pp] >= 0;
+            const bool ok = x < src.npts;
             cpa8z(ph_base + (t * KPTS + p) * 8, ok ? src.gphase + kq * src.npts + x : src.gphase, ok ? 8 : 0);
           }
         }
