@@ -386,21 +386,29 @@ __global__ void __launch_bounds__(SphCfg<BN, GATHER>::NTHREADS, SphCfg<BN, GATHE
 // Table planes of the sites: rows [b_row, b_row + bn) of site s, row 2c = (Tr, -Ti) and
 // row 2c + 1 = (Ti, Tr) of channel c at each local point j (point j - lead of the site's
 // table; zero outside the site and for c >= total), split into BF16 hi (plane 0) and lo
-// (plane 1) planes of brows rows of lb elements. Grid (point blocks, bn, sites).
-__global__ void k_tc_tables(const TcTable *__restrict__ tabs, int brows, long long lb,
+// (plane 1) planes of brows rows of lb elements. Grid (point blocks, sites): a thread
+// writes every row of its point (consecutive threads, consecutive words of a row).
+__global__ void k_tc_tables(const TcTable *__restrict__ tabs, int bn, int brows, long long lb,
                             __nv_bfloat16 *__restrict__ planes) {
-  const TcTable t = tabs[blockIdx.z];
+  const TcTable t = tabs[blockIdx.y];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= t.nkb * KPTS) return;
-  const int n = blockIdx.y, c = n >> 1, p = j - t.lead;
-  float2 v = make_float2(0.f, 0.f);
-  if (c < t.total && p >= 0 && p < t.npts) v = __ldg(t.tab + (long long)c * t.npts + p);
-  const float2 e = (n & 1) ? make_float2(v.y, v.x) : make_float2(v.x, -v.y);
-  uint32_t h, l;
-  split_bf16x2(e, h, l);
-  const long long off = (long long)(t.b_row + n) * lb + 2LL * j;
-  *reinterpret_cast<uint32_t *>(planes + off) = h;
-  *reinterpret_cast<uint32_t *>(planes + (long long)brows * lb + off) = l;
+  const int p = j - t.lead;
+  const bool in = p >= 0 && p < t.npts;
+  uint32_t *hi = reinterpret_cast<uint32_t *>(planes + (long long)t.b_row * lb + 2LL * j);
+  uint32_t *lo = reinterpret_cast<uint32_t *>(planes + ((long long)brows + t.b_row) * lb + 2LL * j);
+  const long long rw = lb / 2;  // 32-bit words from one row to the next
+  for (int c = 0; c < bn / 2; c++) {
+    float2 v = make_float2(0.f, 0.f);
+    if (c < t.total && in) v = __ldg(t.tab + (long long)c * t.npts + p);
+    uint32_t h0, l0, h1, l1;
+    split_bf16x2(make_float2(v.x, -v.y), h0, l0);
+    split_bf16x2(make_float2(v.y, v.x), h1, l1);
+    hi[(2 * c) * rw] = h0;
+    lo[(2 * c) * rw] = l0;
+    hi[(2 * c + 1) * rw] = h1;
+    lo[(2 * c + 1) * rw] = l1;
+  }
 }
 
 __global__ void k_zero_picked_blocks(uint32_t *__restrict__ X, const long long *__restrict__ blocks,
@@ -428,8 +436,8 @@ void launch_tc_tables(const TcTable *tabs_dev, int nsites, int max_nkb, int bn, 
                       void *planes) {
   if (nsites <= 0 || max_nkb <= 0) return;
   PAWPY_REQUIRE(lb % KELEM == 0 && lb >= (long long)max_nkb * KELEM, "table planes too short");
-  dim3 grid(ceil_div(max_nkb * KPTS, 128), bn, nsites);
-  PAWPY_LAUNCH("tc_tables", k_tc_tables<<<grid, 128, 0, stream()>>>(tabs_dev, brows, lb,
+  dim3 grid(ceil_div(max_nkb * KPTS, 128), nsites);
+  PAWPY_LAUNCH("tc_tables", k_tc_tables<<<grid, 128, 0, stream()>>>(tabs_dev, bn, brows, lb,
                                                                    static_cast<__nv_bfloat16 *>(planes)));
 }
 
