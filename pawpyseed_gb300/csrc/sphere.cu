@@ -118,6 +118,101 @@ void launch_slab_count(const SiteDesc *sites, const int2 *slabs, int nslabs, con
   PAWPY_LAUNCH("sphere_count", k_slab_count<<<nslabs, 256, 0, stream()>>>(sites, slabs, lattice, fftg, counts));
 }
 
+// The table values of one inside point of a site (ijk: its unwrapped box position, path: the
+// displacement from the site): conj(radial * Y_lm) * dV * V^-1/2 of every channel lm at
+// tab[sg.site_val + lm site_npts + point], point = pos within the segment.
+__device__ __forceinline__ void fill_point_tables(const SiteDesc &s, const SpeciesDev &sp, const SegFill &sg,
+                                                  const double *L, const int *N, const int *ijk,
+                                                  const double *path, double hmin, double wscale, int pos,
+                                                  float2 *__restrict__ tab) {
+  int ii = ((ijk[0] % N[0]) + N[0]) % N[0];
+  int jj = ((ijk[1] % N[1]) + N[1]) % N[1];
+  int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
+  // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73):
+  // nearer than hmin, the unwrapped box displacement is the unique minimum image;
+  // otherwise search the 27 images
+  double t[3] = {path[0], path[1], path[2]}, r = s_norm(path);
+  if (!(r < hmin)) {
+    // the image of least squared distance is the image of least distance (the square root
+    // is monotone and correctly rounded), so one square root at the end gives the same r
+    double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
+    double r2 = INFINITY;
+    for (int a = -1; a <= 1; a++)
+      for (int b = -1; b <= 1; b++)
+        for (int c = -1; c <= 1; c++) {
+          double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
+          double v[3];
+          s_to_cart(f, L, v);
+          double dd = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+          if (dd < r2) {
+            r2 = dd;
+            t[0] = v[0];
+            t[1] = v[1];
+            t[2] = v[2];
+          }
+        }
+    r = sqrt(r2);
+  }
+  // Y_lm(theta, phi) of the displacement t without transcendental calls:
+  // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
+  // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
+  // (FP64 division is slow on this part: one reciprocal each for r and rho)
+  double ct = 1.0, cp = 1.0, sp_ = 0.0;
+  if (r != 0) {
+    ct = t[2] * (1.0 / r);
+    double rho = sqrt(t[0] * t[0] + t[1] * t[1]);
+    if (rho != 0 && r - fabs(t[2]) != 0) {
+      const double irho = 1.0 / rho;
+      cp = t[0] * irho;
+      sp_ = t[1] * irho;
+    }
+  }
+  // The channel values in single precision (the table is stored in single precision; the
+  // geometry above and the spline index below stay in double precision)
+  const float ctf = (float)ct, cpf = (float)cp, spf = (float)sp_;
+  const float stf = sqrtf(fmaxf(0.f, (float)(1.0 - ct * ct)));
+  // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence:
+  // P_l^m = ((2l-1) ct P_{l-1}^m - (l+m-1) P_{l-2}^m) / (l-m)
+  float P[4][4];
+  P[0][0] = 1.f;
+  for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * stf * P[m - 1][m - 1];
+  for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ctf * P[m][m];
+  P[2][0] = (3.f * ctf * P[1][0] - 1.f * P[0][0]) * 0.5f;
+  P[3][0] = (5.f * ctf * P[2][0] - 2.f * P[1][0]) * (1.f / 3.f);
+  P[3][1] = (5.f * ctf * P[2][1] - 3.f * P[1][1]) * 0.5f;
+  float er[4] = {1.f, cpf, 0.f, 0.f}, ei[4] = {0.f, spf, 0.f, 0.f};
+  for (int m = 2; m <= 3; m++) {
+    er[m] = er[m - 1] * cpf - ei[m - 1] * spf;
+    ei[m] = er[m - 1] * spf + ei[m - 1] * cpf;
+  }
+  // linear-grid spline interpolation (proj_interpolate, utils.c:461-475); x_j = rmax/size*j
+  double xlast = sp.h * (sp.size - 1);
+  int ind = (int)(r * sp.inv_h);
+  if (ind > sp.size - 2) ind = sp.size - 2;
+  const float dd = (float)(r - sp.h * ind);
+  const float ws = (float)wscale;
+  float rad = 0.f;
+  int last_f = -1;
+  for (int lm = 0; lm < sp.total; lm++) {
+    int l = sp.lm_l[lm], mm = sp.lm_m[lm], fi = sp.lm_f[lm];
+    if (fi != last_f) {
+      const double *f = sp.f + (long long)fi * sp.size;
+      const double *sb = sp.spl + (long long)fi * 3 * sp.size;
+      rad = r > xlast ? 0.f
+                      : (float)f[ind] + dd * ((float)sb[ind] + dd * ((float)sb[sp.size + ind] +
+                                                                      dd * (float)sb[2 * sp.size + ind]));
+      last_f = fi;
+    }
+    int am = mm < 0 ? -mm : mm;
+    float plm = l <= 3 ? P[l][am] : 0.f;
+    // lm_coef carries the m < 0 factor of P_l^{-|m|} (utils.c:379-380)
+    float y = (float)sp.lm_coef[lm] * plm * rad * ws;
+    float cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
+    // conj(radial * Y_lm) * dV * V^-1/2
+    tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] = make_float2(y * cs, -y * sn);
+  }
+}
+
 // One CTA per segment: compact the slab's inside points in (i, k) order and
 // tabulate them (double precision, rounded to complex64 at the end).
 __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__restrict__ segs,
@@ -143,6 +238,23 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
     for (int a = 0; a < 3; a++) invN[a] = 1.0 / N[a];
   }
   __syncthreads();
+  if (what == 2 && 2 * s.g[0] + 1 <= N[0] && 2 * s.g[2] + 1 <= N[2]) {
+    // tables alone, after the index fill: the segment's inside points are idx[pt_off + pos]
+    // (wrapped cells i N3 + k, each the image of exactly one box point, the box being no wider
+    // than the cell): one thread per point, the same displacement and values as below
+    const int lo0 = box_i(s, 0, 0), lo2 = box_i(s, 2, 0);
+    for (int pos = threadIdx.x; pos < sg.npts; pos += blockDim.x) {
+      const int c = idx[sg.pt_off + pos], ii = c / N[2], kk = c - ii * N[2];
+      const int ijk[3] = {lo0 + ((ii - lo0) % N[0] + N[0]) % N[0], box_i(s, 1, sg.jb),
+                          lo2 + ((kk - lo2) % N[2] + N[2]) % N[2]};
+      const double fr[3] = {ijk[0] * invN[0] - s.coord[0], ijk[1] * invN[1] - s.coord[1],
+                            ijk[2] * invN[2] - s.coord[2]};
+      double path[3];
+      s_to_cart(fr, L, path);
+      fill_point_tables(s, sp, sg, L, N, ijk, path, hmin, wscale, pos, tab);
+    }
+    return;
+  }
   const int n = (2 * s.g[0] + 1) * (2 * s.g[2] + 1);
   const int w2 = 2 * s.g[2] + 1;
   for (int start = 0; start < n; start += blockDim.x) {
@@ -175,94 +287,7 @@ __global__ void k_seg_fill(const SiteDesc *__restrict__ sites, const SegFill *__
       const int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
       idx[sg.pt_off + pos] = ii * N[2] + kk;
     }
-    if (in && pos < sg.npts && (what & 2)) {
-      int ii = ((ijk[0] % N[0]) + N[0]) % N[0];
-      int jj = ((ijk[1] % N[1]) + N[1]) % N[1];
-      int kk = ((ijk[2] % N[2]) + N[2]) % N[2];
-      // minimum-image displacement from the site to the wrapped grid point (utils.c:51-73):
-      // nearer than hmin, the unwrapped box displacement is the unique minimum image;
-      // otherwise search the 27 images
-      double t[3] = {path[0], path[1], path[2]}, r = s_norm(path);
-      if (!(r < hmin)) {
-        // the image of least squared distance is the image of least distance (the square root
-        // is monotone and correctly rounded), so one square root at the end gives the same r
-        double gp[3] = {(double)ii / N[0], (double)jj / N[1], (double)kk / N[2]};
-        double r2 = INFINITY;
-        for (int a = -1; a <= 1; a++)
-          for (int b = -1; b <= 1; b++)
-            for (int c = -1; c <= 1; c++) {
-              double f[3] = {gp[0] + a - s.coord[0], gp[1] + b - s.coord[1], gp[2] + c - s.coord[2]};
-              double v[3];
-              s_to_cart(f, L, v);
-              double dd = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-              if (dd < r2) {
-                r2 = dd;
-                t[0] = v[0];
-                t[1] = v[1];
-                t[2] = v[2];
-              }
-            }
-        r = sqrt(r2);
-      }
-      // Y_lm(theta, phi) of the displacement t without transcendental calls:
-      // cos(theta) = t_z / r and exp(i phi) = (t_x + i t_y) / rho give the same angles the
-      // reference takes from acos (utils.c:553-561; phi = 0 on the polar axis and at r = 0).
-      // (FP64 division is slow on this part: one reciprocal each for r and rho)
-      double ct = 1.0, cp = 1.0, sp_ = 0.0;
-      if (r != 0) {
-        ct = t[2] * (1.0 / r);
-        double rho = sqrt(t[0] * t[0] + t[1] * t[1]);
-        if (rho != 0 && r - fabs(t[2]) != 0) {
-          const double irho = 1.0 / rho;
-          cp = t[0] * irho;
-          sp_ = t[1] * irho;
-        }
-      }
-      // The channel values in single precision (the table is stored in single precision; the
-      // geometry above and the spline index below stay in double precision)
-      const float ctf = (float)ct, cpf = (float)cp, spf = (float)sp_;
-      const float stf = sqrtf(fmaxf(0.f, (float)(1.0 - ct * ct)));
-      // associated Legendre P_l^m (Condon-Shortley phase), 0 <= m <= l <= 3, by recurrence:
-      // P_l^m = ((2l-1) ct P_{l-1}^m - (l+m-1) P_{l-2}^m) / (l-m)
-      float P[4][4];
-      P[0][0] = 1.f;
-      for (int m = 1; m <= 3; m++) P[m][m] = -(2 * m - 1) * stf * P[m - 1][m - 1];
-      for (int m = 0; m < 3; m++) P[m + 1][m] = (2 * m + 1) * ctf * P[m][m];
-      P[2][0] = (3.f * ctf * P[1][0] - 1.f * P[0][0]) * 0.5f;
-      P[3][0] = (5.f * ctf * P[2][0] - 2.f * P[1][0]) * (1.f / 3.f);
-      P[3][1] = (5.f * ctf * P[2][1] - 3.f * P[1][1]) * 0.5f;
-      float er[4] = {1.f, cpf, 0.f, 0.f}, ei[4] = {0.f, spf, 0.f, 0.f};
-      for (int m = 2; m <= 3; m++) {
-        er[m] = er[m - 1] * cpf - ei[m - 1] * spf;
-        ei[m] = er[m - 1] * spf + ei[m - 1] * cpf;
-      }
-      // linear-grid spline interpolation (proj_interpolate, utils.c:461-475); x_j = rmax/size*j
-      double xlast = sp.h * (sp.size - 1);
-      int ind = (int)(r * sp.inv_h);
-      if (ind > sp.size - 2) ind = sp.size - 2;
-      const float dd = (float)(r - sp.h * ind);
-      const float ws = (float)wscale;
-      float rad = 0.f;
-      int last_f = -1;
-      for (int lm = 0; lm < sp.total; lm++) {
-        int l = sp.lm_l[lm], mm = sp.lm_m[lm], fi = sp.lm_f[lm];
-        if (fi != last_f) {
-          const double *f = sp.f + (long long)fi * sp.size;
-          const double *sb = sp.spl + (long long)fi * 3 * sp.size;
-          rad = r > xlast ? 0.f
-                          : (float)f[ind] + dd * ((float)sb[ind] + dd * ((float)sb[sp.size + ind] +
-                                                                          dd * (float)sb[2 * sp.size + ind]));
-          last_f = fi;
-        }
-        int am = mm < 0 ? -mm : mm;
-        float plm = l <= 3 ? P[l][am] : 0.f;
-        // lm_coef carries the m < 0 factor of P_l^{-|m|} (utils.c:379-380)
-        float y = (float)sp.lm_coef[lm] * plm * rad * ws;
-        float cs = er[am], sn = mm < 0 ? -ei[am] : ei[am];
-        // conj(radial * Y_lm) * dV * V^-1/2
-        tab[sg.site_val + (long long)lm * sg.site_npts + (sg.pt_off - sg.site_pt) + pos] = make_float2(y * cs, -y * sn);
-      }
-    }
+    if (in && pos < sg.npts && (what & 2)) fill_point_tables(s, sp, sg, L, N, ijk, path, hmin, wscale, pos, tab);
     if (in && pos < sg.npts && (what & 1)) {
       // exp(i k.path): the argument in units of pi reduced to [-1, 1] in double precision,
       // then the single-precision sincospi (the phase is stored in single precision)
