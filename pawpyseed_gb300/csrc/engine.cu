@@ -141,6 +141,8 @@ struct DevWF {
   // per k-point: the upload of its coefficients on the side stream (empty when
   // the upload was ordered on the library stream); band pointers of the upload
   std::vector<cudaEvent_t> c_ev;
+  // ... and of each batch of kUploadChunkBands bands of it (c_chunk_ev[k][batch])
+  std::vector<std::vector<cudaEvent_t>> c_chunk_ev;
   DevBuf<const float2 *> host_ptrs;
   // resident real-space wavefunctions [k][band][N1][N2][N3] (a prepared basis)
   DevBuf<float2> grid;
@@ -176,6 +178,8 @@ struct DevWF {
       cudaStreamWaitEvent(stream(), e, 0);
       cudaEventDestroy(e);
     }
+    for (auto &v : c_chunk_ev)
+      for (cudaEvent_t e : v) cudaEventDestroy(e);
     for (cudaEvent_t e : h_ev) {
       cudaStreamWaitEvent(stream(), e, 0);
       cudaEventDestroy(e);
@@ -183,11 +187,25 @@ struct DevWF {
   }
 };
 
+// Bands per launch of the in-place read of host coefficients (each batch has its event).
+constexpr int kUploadChunkBands = 128;
+
 // Makes the library stream wait for the upload of k-point k's coefficients;
 // their device address.
 static const float2 *coeffs(DevWF &d, int k) {
   if (!d.c_ev.empty()) PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.c_ev[k], 0));
   return d.C.p + d.kp[k].c_off;
+}
+
+// The same for bands [b0, b0 + nb) of k-point k only; the address of band b0.
+static const float2 *coeffs(DevWF &d, int k, int b0, int nb) {
+  if (!d.c_chunk_ev.empty()) {
+    for (int c = b0 / kUploadChunkBands; c * kUploadChunkBands < b0 + nb; c++)
+      PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.c_chunk_ev[k][c], 0));
+  } else if (!d.c_ev.empty()) {
+    PAWPY_CUDA(cudaStreamWaitEvent(stream(), d.c_ev[k], 0));
+  }
+  return d.C.p + d.kp[k].c_off + (size_t)b0 * d.kp[k].Wpad;
 }
 
 // The library stream waits for the uploads and the early transforms of d.
@@ -446,12 +464,21 @@ static void ensure_coeffs(DevWF &d) {
     PAWPY_CUDA(cudaEventDestroy(ready));
     d.c_ev.assign(d.nk, nullptr);
     for (auto &e : d.c_ev) PAWPY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    const int nchunk = ceil_div(d.nband, kUploadChunkBands);
+    d.c_chunk_ev.assign(d.nk, std::vector<cudaEvent_t>(nchunk, nullptr));
     {
       OnStream on(up);
       for (int k = 0; k < d.nk; k++) {
         DevKpt &q = d.kp[k];
-        launch_load_host_bands(d.host_ptrs.p + (size_t)k * d.nband, q.W, q.inv_d.p, d.C.p + q.c_off, q.Wpad,
-                               d.nband);
+        // in batches of bands, each with its event: the first FFT pass of a batch starts when its
+        // bands have arrived
+        for (int c = 0; c < nchunk; c++) {
+          const int b0 = c * kUploadChunkBands, nb = std::min(kUploadChunkBands, d.nband - b0);
+          launch_load_host_bands(d.host_ptrs.p + (size_t)k * d.nband + b0, q.W, q.inv_d.p,
+                                 d.C.p + q.c_off + (size_t)b0 * q.Wpad, q.Wpad, nb);
+          PAWPY_CUDA(cudaEventCreateWithFlags(&d.c_chunk_ev[k][c], cudaEventDisableTiming));
+          PAWPY_CUDA(cudaEventRecord(d.c_chunk_ev[k][c], up));
+        }
         PAWPY_CUDA(cudaEventRecord(d.c_ev[k], up));
       }
     }
@@ -1003,9 +1030,11 @@ static void transform_planes_early(DevWF &d) {
       // in launches of kEarlyChunkBands bands: the launches on the priority stream (sphere
       // counts and index lists) are dispatched when a launch's blocks retire
       const size_t hb = (size_t)q.n1 * d.N[1] * d.N[2];
-      for (int b0 = 0; b0 < d.nband; b0 += kEarlyChunkBands)
-        launch_fft_planes_fast(coeffs(d, k) + (size_t)b0 * q.Wpad, q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
-                               d.Hall.p + off[k] + b0 * hb, std::min(kEarlyChunkBands, d.nband - b0));
+      for (int b0 = 0; b0 < d.nband; b0 += kEarlyChunkBands) {
+        const int nb = std::min(kEarlyChunkBands, d.nband - b0);
+        launch_fft_planes_fast(coeffs(d, k, b0, nb), q.Wpad, q.plane_start.p, q.plane_off.p, geo[k],
+                               d.Hall.p + off[k] + b0 * hb, nb);
+      }
       PAWPY_CUDA(cudaEventRecord(d.h_ev[k], xs));
     }
   }
