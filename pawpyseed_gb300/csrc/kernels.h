@@ -54,6 +54,10 @@ struct PickList {
 // gamma: the k-point is Gamma (every Bloch phase is 1, the phase list is not read)
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
                             long long xstride, int nb, long long lo_words = 0, bool gamma = false);
+// pass B on the tensor cores (xpick_tc.cu): Gamma point, split rows (lo_words > 0), n1 <= 64,
+// 2 N1 <= 256, N3 <= 128
+bool xpick_tc_supported(const PlaneGeom &g);
+void launch_xpick_tc(const float2 *H, const PlaneGeom &g, const PickList &pl, float2 *X, int nb, long long lo_words);
 // Resident real-space wavefunctions of one k-point, bands in tiles of 16: the value of band b at
 // cell c (= (x N2 + y) N3 + z) is at grid_value_index(b, c, n3d).
 __host__ __device__ inline long long grid_value_index(int b, long long cell, long long n3d) {

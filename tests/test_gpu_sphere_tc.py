@@ -123,3 +123,40 @@ def test_tensor_core_spinor_projections(defect_grid, monkeypatch):
             scale = np.abs(ref).max()
             for b in range(ow.nband):
                 assert np.abs(got[k][b][h] - ref[b]).max() <= TOL * scale
+
+
+@pytest.mark.parametrize("name", ["cfg0", "cfg2s"])
+def test_tensor_core_second_pass_matches_fp64(name, workload_dirs, oracle_projectors, monkeypatch):
+    """The second FFT pass on the tensor cores (PAWPY_GPU_XPICK_TC=1: the transform along the first
+    axis as a split-BF16 DFT product, fused with the pick; Gamma k-points, split rows): projections
+    within 1e-5 of the largest coefficient against FP64, within 5e-6 of it of the register-FFT
+    form, and the overlaps of the whole projection within 1e-5 of FP64."""
+    from pawpyseed_gb300.projector import Projector
+    from pawpyseed_gb300.wavefunction import Wavefunction
+
+    dirs = workload_dirs(name)
+    op = oracle_projectors(name)
+
+    def proj():
+        w = Wavefunction.from_directory(dirs["defect"])
+        w.check_c_projectors()
+        return _projections(w)
+
+    def overlaps():
+        basis = Wavefunction.from_directory(dirs["basis"])
+        wf = Wavefunction.from_directory(dirs["defect"])
+        basis.check_c_projectors()
+        return Projector(wf, basis).project_all()
+
+    monkeypatch.setenv("PAWPY_GPU_XPICK_TC", "1")
+    tcx = _with_mode(2, proj)
+    full = _with_mode(2, overlaps)
+    monkeypatch.setenv("PAWPY_GPU_XPICK_TC", "0")
+    reg = _with_mode(2, proj)
+    ref = np.array(op.wf.P)
+    scale = np.abs(ref).max()
+    assert np.abs(tcx - ref).max() <= TOL * scale
+    assert np.abs(tcx - reg).max() <= 5e-6 * scale
+    t = op.full()
+    tv = np.array([op.band_vector(t, b) for b in range(op.wf.nband)])
+    assert np.abs(full - tv).max() <= TOL
