@@ -167,6 +167,7 @@ struct DevWF {
   Radices r[3];
   DevBuf<float2> tw[3];
   std::unique_ptr<AeTables> ae;  // real-space all-electron tables (last grid asked for)
+  TcSplitCache gemm_cache;       // split planes of C as operand A of the overlap contraction
   DevWF() = default;
   DevWF(const DevWF &) = delete;
   DevWF &operator=(const DevWF &) = delete;
@@ -2147,7 +2148,7 @@ static int flip_k(const DevWF &R, int k, int flip) {
 static int choose_splits(int M, int N, int nz, int maxK) {
   int tiles = ceil_div(M, 64) * ceil_div(N, 64) * nz;
   int chunks = maxK / 16;
-  int s = std::max(1, ceil_div(2 * 152, tiles));
+  int s = std::max(1, ceil_div(2 * sm_count(), tiles));
   s = std::min(s, std::max(1, chunks / 32));
   return std::min(s, 64);
 }
@@ -2225,7 +2226,10 @@ static void overlap_gemm(PairState &ps, int flip, const float2 *B32, float2 *out
   for (const GemmBatch &g : hb) flops += 8.0 * NR * NS * (double)(g.K1 + g.K2 + g.K3);
   note_work(prec == PAWPY_GPU_BF16X3 ? "gemm_bf16x3" : prec == PAWPY_GPU_TF32 ? "gemm_tf32" : "gemm_f32", flops);
   if (prec == PAWPY_GPU_BF16X3 || prec == PAWPY_GPU_TF32) {
-    launch_zgemm_tc(db.p, hb, NR, NS, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr);
+    // the basis's coefficient planes are split once and kept with it (operand A's first segment
+    // is C_R except in the cross terms)
+    launch_zgemm_tc(db.p, hb, NR, NS, prec == PAWPY_GPU_TF32, g_tc_splits, nullptr,
+                    what == Contraction::kCross ? nullptr : &R.gemm_cache);
     return;
   }
   int splits = choose_splits(NR, NS, nk, maxK);

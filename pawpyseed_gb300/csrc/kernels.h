@@ -3,6 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <vector>
+
 #include "common.h"
 #include "fft_block.cuh"
 
@@ -54,6 +57,8 @@ struct PickList {
 // gamma: the k-point is Gamma (every Bloch phase is 1, the phase list is not read)
 void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList &pl, int kq, float2 *X,
                             long long xstride, int nb, long long lo_words = 0, bool gamma = false);
+// the device's SM count (tc_gemm.cu)
+int sm_count();
 // pass B on the tensor cores (xpick_tc.cu): Gamma point, split rows (lo_words > 0), n1 <= 64,
 // 2 N1 <= 256, N3 <= 128
 bool xpick_tc_supported(const PlaneGeom &g);
@@ -218,8 +223,23 @@ void set_tc_tile(int bn);
 struct TcGemmInfo {
   int splits = 0, Kc = 0, ctas = 0, bn = 0;  // bn: defect bands per tile
 };
+// The split planes of the first segment of operand A (a resident basis's coefficients, the
+// same device arrays call after call), built on the first call that gives it and read by the
+// later ones (after ready): only the augmentation columns are split per call. Owned by the
+// basis; one precision and shape (a call of another shape splits everything itself).
+struct TcSplitCache {
+  std::mutex mu;
+  bool built = false, tf32 = false;
+  int nz = 0, Mpad = 0, K1 = 0;
+  std::vector<const float2 *> src;
+  DevBuf<unsigned char> planes;
+  cudaEvent_t ready = nullptr;
+  ~TcSplitCache() {
+    if (ready) cudaEventDestroy(ready);
+  }
+};
 void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
-                     int splits_hint, TcGemmInfo *info);
+                     int splits_hint, TcGemmInfo *info, TcSplitCache *cacheA = nullptr);
 // The two kernels behind launch_zgemm_f32 (64x64 tiles, 256 threads; grid (M/64, N/64, nz*splits)
 // and (M*N/1024, nz)), for callers that launch them on their own stream.
 __global__ void __launch_bounds__(256) k_zgemm_f32(const GemmBatch *batches, int M, int N, int splits,

@@ -101,9 +101,10 @@ __host__ __device__ constexpr uint32_t idesc(bool tf32, bool negA, int bn) {
 // few K blocks, so the bias stays near 6 FLUSH 2^-24 |S| whatever K is.
 template <bool TF32, int BN>
 __global__ void __launch_bounds__(NTHREADS, (BN == 128 ? 1 : 2))  // CTAs per SM
-    k_tc_zgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-               const GemmBatch *__restrict__ batches, const int *__restrict__ kblocks, int M, int N, int Mpad,
-               int Npad, int nz, int splits, float2 *__restrict__ ws, int *__restrict__ status) {
+    k_tc_zgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2, int kbs,
+               const __grid_constant__ CUtensorMap tmB, const GemmBatch *__restrict__ batches,
+               const int *__restrict__ kblocks, int M, int N, int Mpad, int Npad, int nz, int splits,
+               float2 *__restrict__ ws, int *__restrict__ status) {
   using P = Prec<TF32, BN>;
   constexpr int TN = BN;
   constexpr int TMEM_COLS = P::TMEM_COLS;
@@ -169,10 +170,14 @@ __global__ void __launch_bounds__(NTHREADS, (BN == 128 ? 1 : 2))  // CTAs per SM
         const uint32_t full = smem_u32(&bar_full[s]);
         const uint32_t st = sbase + s * P::STAGE;
         mbar_expect_tx(full, P::STAGE);
-        const int x = (kb0 + i) * P::KB;
+        const int kb = kb0 + i, x = kb * P::KB;
+        // operand A: K blocks below kbs from tmA, the rest from tmA2 (planes of the columns
+        // from kbs KB on)
+        const CUtensorMap *ma = kb < kbs ? &tmA : &tmA2;
+        const int xa = kb < kbs ? x : (kb - kbs) * P::KB;
 #pragma unroll
         for (int p = 0; p < P::NPL; p++) {
-          tma_load_2d(st + p * P::A_PLANE, &tmA, full, x, p * rowsA + z * Mpad + m0);
+          tma_load_2d(st + p * P::A_PLANE, ma, full, xa, p * rowsA + z * Mpad + m0);
           tma_load_2d(st + P::NPL * P::A_PLANE + p * P::B_PLANE, &tmB, full, x, p * rowsB + z * Npad + n0);
         }
         last_round[s] = r;
@@ -286,12 +291,13 @@ __global__ void __launch_bounds__(NTHREADS, (BN == 128 ? 1 : 2))  // CTAs per SM
   }
 }
 
-// Splits one operand into planes [plane][z][rows_pad][Kc]: element (z, row, k)
-// is A1[row][k] (k < K1), A2[row][k - K1] (k < K1 + K2), A3[row][k - K1 - K2]
-// (k < K1 + K2 + K3) or zero; rows >= rows are zero. side 0 takes the A pointers of the batch, side 1 the B pointers.
+// Splits columns [k_off, k_off + Kc) of one operand into planes [plane][z][rows_pad][Kc]:
+// element (z, row, k) is column c = k_off + k, A1[row][c] (c < K1), A2[row][c - K1]
+// (c < K1 + K2), A3[row][c - K1 - K2] (c < K1 + K2 + K3) or zero; rows >= rows are zero.
+// side 0 takes the A pointers of the batch, side 1 the B pointers.
 template <bool TF32>
 __global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, int rows, int rows_pad, int Kc,
-                               int nz, void *__restrict__ planes) {
+                               int k_off, int nz, void *__restrict__ planes) {
   const int z = blockIdx.z, row = blockIdx.y;
   const int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
   if (k0 >= Kc) return;
@@ -304,7 +310,7 @@ __global__ void k_split_planes(const GemmBatch *__restrict__ batches, int side, 
   float2 v[4];
 #pragma unroll
   for (int e = 0; e < 4; e++) {
-    const int k = k0 + e;
+    const int k = k_off + k0 + e;
     v[e] = make_float2(0.f, 0.f);
     if (row < rows) {
       if (k < bt.K1)
@@ -392,15 +398,16 @@ CUtensorMap plane_map(void *base, bool tf32, long long Kc, long long rows, int b
 // One launch of the contraction with tiles of bn defect bands and the given K split (plus
 // the fixed-order reduction of the split partial sums).
 template <bool TF32, int BN>
-void launch_tile(const CUtensorMap &ma, const void *pb, int Kc, const GemmBatch *batches_dev, const int *kb_dev,
-                 int M, int N, int Mpad, int Npad, int nz, int splits, float2 *ws, int *st) {
+void launch_tile(const CUtensorMap &ma, const CUtensorMap &ma2, int kbs, const void *pb, int Kc,
+                 const GemmBatch *batches_dev, const int *kb_dev, int M, int N, int Mpad, int Npad, int nz, int splits,
+                 float2 *ws, int *st) {
   using P = Prec<TF32, BN>;
   const CUtensorMap mb = plane_map(const_cast<void *>(pb), TF32, Kc, (long long)P::NPL * nz * Npad, BN);
   allow_dynamic_smem((const void *)k_tc_zgemm<TF32, BN>, P::SMEM);
   dim3 grid(Mpad / TM, ceil_div(N, BN), nz * splits);
   PAWPY_LAUNCH(TF32 ? "gemm_tf32" : "gemm_bf16x3",
-               (k_tc_zgemm<TF32, BN><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, mb, batches_dev, kb_dev, M, N, Mpad,
-                                                                           Npad, nz, splits, ws, st)));
+               (k_tc_zgemm<TF32, BN><<<grid, NTHREADS, P::SMEM, stream()>>>(ma, ma2, kbs, mb, batches_dev, kb_dev, M,
+                                                                           N, Mpad, Npad, nz, splits, ws, st)));
   if (splits > 1) {
     dim3 g2(ceil_div((long long)M * N, 256 * 4), nz);
     PAWPY_LAUNCH("gemm_reduce", k_split_reduce<<<g2, 256, 0, stream()>>>(batches_dev, ws, M, N, splits, nz));
@@ -426,7 +433,7 @@ std::map<std::tuple<int, int, int, int, int>, TcChoice> &tc_tuned() {
 
 template <bool TF32>
 void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, int splits_hint,
-            TcGemmInfo *info) {
+            TcGemmInfo *info, TcSplitCache *cacheA) {
   using P = Prec<TF32, BN_MAX>;
   HostPhase hp("tc_gemm");
   const int nz = (int)hb.size();
@@ -468,25 +475,56 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
   int max_splits = 1;
   for (auto &c : cands) max_splits = std::max(max_splits, c.splits);
 
-  DevBuf<unsigned char> pa((size_t)P::NPL * nz * Mpad * Kc * P::ESZ);
+  // operand A's first segment from the cache when every batch's first segment is the cached one
+  // (same arrays, a whole number of K blocks): only columns [K1, Kc) are split per call
+  int K1 = hb[0].K1;
+  bool cached = cacheA && K1 > 0 && K1 % P::KB == 0 && K1 < Kc;
+  for (int z = 0; z < nz && cached; z++) cached = hb[z].K1 == K1;
+  if (cached) {
+    std::lock_guard<std::mutex> lk(cacheA->mu);
+    if (!cacheA->built) {
+      cacheA->planes.alloc((size_t)P::NPL * nz * Mpad * K1 * P::ESZ);
+      dim3 g(ceil_div(K1 / 4, 256), Mpad, nz);
+      PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g, 256, 0, stream()>>>(batches_dev, 0, M, Mpad, K1, 0, nz,
+                                                                               cacheA->planes.p));
+      if (!cacheA->ready) PAWPY_CUDA(cudaEventCreateWithFlags(&cacheA->ready, cudaEventDisableTiming));
+      PAWPY_CUDA(cudaEventRecord(cacheA->ready, stream()));
+      cacheA->built = true;
+      cacheA->tf32 = TF32;
+      cacheA->nz = nz;
+      cacheA->Mpad = Mpad;
+      cacheA->K1 = K1;
+      cacheA->src.resize(nz);
+      for (int z = 0; z < nz; z++) cacheA->src[z] = hb[z].A1;
+    }
+    cached = cacheA->tf32 == TF32 && cacheA->nz == nz && cacheA->Mpad == Mpad && cacheA->K1 == K1;
+    for (int z = 0; z < nz && cached; z++) cached = cacheA->src[z] == hb[z].A1;
+    if (cached) PAWPY_CUDA(cudaStreamWaitEvent(stream(), cacheA->ready, 0));
+  }
+  const int Ka = cached ? Kc - K1 : Kc;  // columns of the per-call planes of A
+  DevBuf<unsigned char> pa((size_t)P::NPL * nz * Mpad * Ka * P::ESZ);
   DevBuf<unsigned char> pb((size_t)P::NPL * nz * Npad * Kc * P::ESZ);
   DevBuf<int> kb_dev(nz);
   kb_dev.upload(kbl.data(), nz);
   {
-    dim3 g(ceil_div(Kc / 4, 256), Mpad, nz);
-    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g, 256, 0, stream()>>>(batches_dev, 0, M, Mpad, Kc, nz, pa.p));
+    dim3 g(ceil_div(Ka / 4, 256), Mpad, nz);
+    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g, 256, 0, stream()>>>(batches_dev, 0, M, Mpad, Ka,
+                                                                             cached ? K1 : 0, nz, pa.p));
     dim3 g2(ceil_div(Kc / 4, 256), Npad, nz);
-    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g2, 256, 0, stream()>>>(batches_dev, 1, N, Npad, Kc, nz, pb.p));
+    PAWPY_LAUNCH("tc_split", k_split_planes<TF32><<<g2, 256, 0, stream()>>>(batches_dev, 1, N, Npad, Kc, 0, nz, pb.p));
   }
-  const CUtensorMap ma = plane_map(pa.p, TF32, Kc, (long long)P::NPL * nz * Mpad, TM);
+  const CUtensorMap ma = cached ? plane_map(cacheA->planes.p, TF32, K1, (long long)P::NPL * nz * Mpad, TM)
+                                : plane_map(pa.p, TF32, Kc, (long long)P::NPL * nz * Mpad, TM);
+  const CUtensorMap ma2 = cached ? plane_map(pa.p, TF32, Ka, (long long)P::NPL * nz * Mpad, TM) : ma;
+  const int kbs = cached ? K1 / P::KB : Kc / P::KB;
   DevBuf<float2> ws;
   if (max_splits > 1) ws.alloc((size_t)max_splits * nz * N * M);
   int *st = device_status();
   auto run = [&](const TcChoice &c) {
     if (c.bn == 128)
-      launch_tile<TF32, 128>(ma, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
+      launch_tile<TF32, 128>(ma, ma2, kbs, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
     else
-      launch_tile<TF32, 64>(ma, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
+      launch_tile<TF32, 64>(ma, ma2, kbs, pb.p, Kc, batches_dev, kb_dev.p, M, N, Mpad, Npad, nz, c.splits, ws.p, st);
   };
   TcChoice choice = cands[0];
   if (cands.size() > 1) {
@@ -548,12 +586,12 @@ void run_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int 
 void set_tc_tile(int bn) { g_tc_tile = (bn == 64 || bn == 128) ? bn : 0; }
 
 void launch_zgemm_tc(const GemmBatch *batches_dev, const std::vector<GemmBatch> &hb, int M, int N, bool tf32,
-                     int splits_hint, TcGemmInfo *info) {
+                     int splits_hint, TcGemmInfo *info, TcSplitCache *cacheA) {
   if (hb.empty() || M <= 0 || N <= 0) return;
   if (tf32)
-    run_tc<true>(batches_dev, hb, M, N, splits_hint, info);
+    run_tc<true>(batches_dev, hb, M, N, splits_hint, info, cacheA);
   else
-    run_tc<false>(batches_dev, hb, M, N, splits_hint, info);
+    run_tc<false>(batches_dev, hb, M, N, splits_hint, info, cacheA);
 }
 
 }  // namespace pawpy

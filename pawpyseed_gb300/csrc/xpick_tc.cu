@@ -13,10 +13,10 @@
 // One persistent CTA per SM over the items (j-major, band fastest); warp roles:
 //   0: TMA of the DFT operand B (both planes, every K block) once;
 //   1: TMEM allocation and the MMA issue (one elected lane), two accumulator sets;
-//   2..5: converters: the item's occupied planes of H (FP32) into the split A stage
+//   XT_CONV converter warps: the item's occupied planes of H (FP32) into the split A stage
 //         (K-major, 64-byte swizzle), loads of the next item issued before its stage frees;
-//   6..9: drain: TMEM rows (lane quarter = warp % 4) to the split plane tile;
-//   10..: pick: the plane's entries from the tile to the picked rows.
+//   XT_DRAIN = 4 drain warps: TMEM rows (lane quarter = warp % 4) to the split plane tile;
+//   XT_PICK pick warps: the plane's entries from the tile to the picked rows.
 // Stages: one A stage, two TMEM accumulators, one tile; every wait is bounded (4 s) and a
 // wait that runs out writes the status word and stops every role; the MMAs and the B copy
 // are waited for before the TMEM is freed and the CTA ends.
