@@ -1484,6 +1484,10 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   for (int e = 0; e < num_elems; e++) pps[e].num_cart_gridpts = cart_gridpts_bound(pps[e], wf->lattice, fftg);
   set_grid(d, fftg);
   ensure_all_planes(d);
+  // with the projections deferred to overlap_setup_real, the first FFT pass runs from here on,
+  // beside the table, sphere and pair work (its launches of 128 bands let the sphere counts on the
+  // priority stream through within one launch)
+  if (!g_host_proj) transform_planes_early(d);
   d.species.clear();
   for (int e = 0; e < num_elems; e++) d.species.push_back(species_tables(pps[e]));
   d.labels.assign(labels, labels + num_sites);
@@ -1492,10 +1496,6 @@ static void do_setup_projections(pswf_t *wf, ppot_t *pps, int num_elems, int num
   std::iota(all.begin(), all.end(), 0);
   build_spheres(d.proj, all, d.labels.data(), d.coords.data(), d.species, false, d.lattice, d.N, d.vol, d.kp,
                 d.rec);
-  // with the projections deferred to overlap_setup_real, the first FFT pass runs from here on,
-  // beside the sphere and pair work of overlap_setup_real (issued after the projector spheres,
-  // whose point counts the host reads back: those then run on an idle device)
-  if (!g_host_proj) transform_planes_early(d);
   d.site_lmoff.resize(num_sites);
   for (int s = 0; s < num_sites; s++) d.site_lmoff[s] = d.proj.host[s].lm_off;
   d.P.alloc((size_t)d.nk * d.nband * d.proj.Ptot);
