@@ -2524,6 +2524,7 @@ int pawpy_gpu_upload(pswf_t *wf) {
 ppot_t *get_projector_list(int num_els, int *labels, int *ls, double *wave_grids, double *projectors,
                            double *aewaves, double *pswaves, double *rmaxs, double grid_encut) {
   PAWPY_API_BEGIN
+  HostPhase hp_api("get_projector_list");
   return cached_projector_list(num_els, labels, ls, wave_grids, projectors, aewaves, pswaves, rmaxs, grid_encut);
   PAWPY_API_END(nullptr)
 }

@@ -691,51 +691,71 @@ ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, con
     kwave.download(h_kw.data(), kwave.n);
     smooth.download(h_sm.data(), smooth.n);
     sync();
-    // ---- host: splines of the transforms, the smooth difference on the linear grid, overlaps
-    long o_ng = 0;
-    int f = 0;
-    for (int e = 0; e < num_els; e++) {
-      ppot_t &pp = pps[e];
-      int ng = pp.wave_gridsize, nd = pp.proj_gridsize, np = pp.num_projs;
-      pp.kwave_grid = dupd(std::vector<double>(h_ks.begin() + 2 * o_ng, h_ks.begin() + 2 * o_ng + ng));
-      for (int k = 0; k < np; k++, f++) {
-        funcset_t &fs = pp.funcs[k];
-        fs.kwave = dupd(std::vector<double>(h_kw.begin() + f_off[f], h_kw.begin() + f_off[f] + ng));
-        fs.kwave_spline = new_spline3(pp.kwave_grid, fs.kwave, ng);
-        const double *sm = h_sm.data() + f_off[f];
-        double **ss = new_spline3(dense[e].data(), sm, ng);
-        std::vector<double> sdw(nd);
-        for (int p = 1; p < nd; p++) sdw[p] = interp_log(pp.smooth_grid[p], ng, dense[e].data(), sm, ss);
-        sdw[0] = fs.l > 0 ? 0.0 : sdw[1];
-        for (int q = 0; q < 3; q++) std::free(ss[q]);
-        std::free(ss);
-        fs.smooth_diffwave = dupd(sdw);
-        fs.smooth_diffwave_spline = new_spline3(pp.smooth_grid, fs.smooth_diffwave, nd);
-      }
-      pp.pspw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      pp.aepw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      pp.diff_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
-      if (!pp.pspw_overlap_matrix || !pp.aepw_overlap_matrix || !pp.diff_overlap_matrix) throw std::bad_alloc();
-      std::vector<double> prod(ng), b(ng), c(ng), d(ng);
-      for (int i = 0; i < np; i++)
-        for (int j = i; j < np; j++) {
-          if (pp.funcs[i].l != pp.funcs[j].l) continue;
-          const funcset_t &a1 = pp.funcs[i], &a2 = pp.funcs[j];
-          double *mats[3] = {pp.pspw_overlap_matrix, pp.aepw_overlap_matrix, pp.diff_overlap_matrix};
-          for (int w = 0; w < 3; w++) {
-            for (int q = 0; q < ng; q++) {
-              if (w == 0) prod[q] = a1.pswave[q] * a2.pswave[q];
-              else if (w == 1) prod[q] = a1.aewave[q] * a2.aewave[q];
-              else prod[q] = (a1.aewave[q] - a1.pswave[q]) * (a2.aewave[q] - a2.pswave[q]);
-            }
-            spline_coeffs(pp.wave_grid, prod.data(), ng, b.data(), c.data(), d.data());
-            double v = spline_integral(pp.wave_grid, prod.data(), b.data(), c.data(), d.data(), ng);
-            mats[w][i * np + j] = v;
-            mats[w][j * np + i] = v;
-          }
+    HostPhase hp_post("projector_list_splines");
+    // ---- host: splines of the transforms, the smooth difference on the linear grid, overlaps;
+    // the functions and the overlap integrals are independent: one host thread each
+    std::vector<int> f_el, f_k;
+    {
+      long o_ng = 0;
+      for (int e = 0; e < num_els; e++) {
+        ppot_t &pp = pps[e];
+        pp.kwave_grid = dupd(std::vector<double>(h_ks.begin() + 2 * o_ng, h_ks.begin() + 2 * o_ng + pp.wave_gridsize));
+        for (int k = 0; k < pp.num_projs; k++) {
+          f_el.push_back(e);
+          f_k.push_back(k);
         }
-      o_ng += ng;
+        o_ng += pp.wave_gridsize;
+        const int np = pp.num_projs;
+        pp.pspw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
+        pp.aepw_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
+        pp.diff_overlap_matrix = static_cast<double *>(std::calloc(np * np, sizeof(double)));
+        if (!pp.pspw_overlap_matrix || !pp.aepw_overlap_matrix || !pp.diff_overlap_matrix) throw std::bad_alloc();
+      }
     }
+    host_parallel_for((int)f_el.size(), [&](int f) {
+      const int e = f_el[f], k = f_k[f];
+      ppot_t &pp = pps[e];
+      const int ng = pp.wave_gridsize, nd = pp.proj_gridsize;
+      funcset_t &fs = pp.funcs[k];
+      fs.kwave = dupd(std::vector<double>(h_kw.begin() + f_off[f], h_kw.begin() + f_off[f] + ng));
+      fs.kwave_spline = new_spline3(pp.kwave_grid, fs.kwave, ng);
+      const double *sm = h_sm.data() + f_off[f];
+      double **ss = new_spline3(dense[e].data(), sm, ng);
+      std::vector<double> sdw(nd);
+      for (int p = 1; p < nd; p++) sdw[p] = interp_log(pp.smooth_grid[p], ng, dense[e].data(), sm, ss);
+      sdw[0] = fs.l > 0 ? 0.0 : sdw[1];
+      for (int q = 0; q < 3; q++) std::free(ss[q]);
+      std::free(ss);
+      fs.smooth_diffwave = dupd(sdw);
+      fs.smooth_diffwave_spline = new_spline3(pp.smooth_grid, fs.smooth_diffwave, nd);
+    });
+    // overlap integrals <ps|ps>, <ae|ae>, <ae-ps|ae-ps> of the function pairs of equal l
+    struct OvTask {
+      int e, i, j, w;
+    };
+    std::vector<OvTask> ov;
+    for (int e = 0; e < num_els; e++)
+      for (int i = 0; i < pps[e].num_projs; i++)
+        for (int j = i; j < pps[e].num_projs; j++)
+          if (pps[e].funcs[i].l == pps[e].funcs[j].l)
+            for (int w = 0; w < 3; w++) ov.push_back({e, i, j, w});
+    host_parallel_for((int)ov.size(), [&](int t) {
+      const OvTask &o = ov[t];
+      ppot_t &pp = pps[o.e];
+      const int ng = pp.wave_gridsize, np = pp.num_projs;
+      const funcset_t &a1 = pp.funcs[o.i], &a2 = pp.funcs[o.j];
+      std::vector<double> prod(ng), b(ng), c(ng), d(ng);
+      for (int q = 0; q < ng; q++) {
+        if (o.w == 0) prod[q] = a1.pswave[q] * a2.pswave[q];
+        else if (o.w == 1) prod[q] = a1.aewave[q] * a2.aewave[q];
+        else prod[q] = (a1.aewave[q] - a1.pswave[q]) * (a2.aewave[q] - a2.pswave[q]);
+      }
+      spline_coeffs(pp.wave_grid, prod.data(), ng, b.data(), c.data(), d.data());
+      const double v = spline_integral(pp.wave_grid, prod.data(), b.data(), c.data(), d.data(), ng);
+      double *mat = o.w == 0 ? pp.pspw_overlap_matrix : o.w == 1 ? pp.aepw_overlap_matrix : pp.diff_overlap_matrix;
+      mat[o.i * np + o.j] = v;
+      mat[o.j * np + o.i] = v;
+    });
   } catch (...) {
     free_ppot_array(pps, num_els);
     throw;
