@@ -624,10 +624,7 @@ ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, con
         f.diffwave = dupd(df);
         f.proj = dupd(std::vector<double>(projectors + pr, projectors + pr + nd));
         pr += nd;
-        f.proj_spline = new_spline3(pp.proj_grid, f.proj, nd);
-        f.aewave_spline = new_spline3(pp.wave_grid, f.aewave, ng);
-        f.pswave_spline = new_spline3(pp.wave_grid, f.pswave, ng);
-        f.diffwave_spline = new_spline3(pp.wave_grid, f.diffwave, ng);
+        // (their splines are fitted while the device transforms run, below)
       }
       nf += np;
     }
@@ -686,6 +683,21 @@ ppot_t *device_projector_list(int num_els, const int *labels, const int *ls, con
     PAWPY_LAUNCH("radial_sbt", k_sbt_forward<<<nf, 256, zsm, stream()>>>(d_els.p, d_fns.p));
     double kcut = std::pow(0.262465831 * grid_encut, 0.5);
     PAWPY_LAUNCH("radial_sbt", k_sbt_inverse<<<nf, 256, zsm, stream()>>>(d_els.p, d_fns.p, kcut));
+    // the host splines of the input functions, one function per host thread, beside the transforms
+    {
+      std::vector<std::pair<int, int>> fk;
+      for (int e = 0; e < num_els; e++)
+        for (int k = 0; k < pps[e].num_projs; k++) fk.push_back({e, k});
+      host_parallel_for((int)fk.size(), [&](int i) {
+        ppot_t &pp = pps[fk[i].first];
+        funcset_t &f = pp.funcs[fk[i].second];
+        const int nd = pp.proj_gridsize, ng = pp.wave_gridsize;
+        f.proj_spline = new_spline3(pp.proj_grid, f.proj, nd);
+        f.aewave_spline = new_spline3(pp.wave_grid, f.aewave, ng);
+        f.pswave_spline = new_spline3(pp.wave_grid, f.pswave, ng);
+        f.diffwave_spline = new_spline3(pp.wave_grid, f.diffwave, ng);
+      });
+    }
     std::vector<double> h_ks(ks.n), h_kw(kwave.n), h_sm(smooth.n);
     ks.download(h_ks.data(), ks.n);
     kwave.download(h_kw.data(), kwave.n);
