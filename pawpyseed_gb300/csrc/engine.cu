@@ -227,6 +227,50 @@ struct AugKey {
   }
 };
 
+// Pinned host staging for uploads issued behind long device work: a copy from pinned memory
+// returns at once, where one from pageable memory can wait for the stream's earlier launches.
+// begin() waits for the previous round's copies before the buffer is rewritten.
+struct PinnedStage {
+  void *h = nullptr;
+  size_t cap = 0, used = 0;
+  cudaEvent_t done = nullptr;
+  PinnedStage() = default;
+  PinnedStage(const PinnedStage &) = delete;
+  PinnedStage &operator=(const PinnedStage &) = delete;
+  ~PinnedStage() {
+    if (done) {
+      cudaEventSynchronize(done);
+      cudaEventDestroy(done);
+    }
+    if (h) cudaFreeHost(h);
+  }
+  void begin(size_t bytes) {
+    if (done) PAWPY_CUDA(cudaEventSynchronize(done));
+    if (bytes > cap) {
+      if (h) PAWPY_CUDA(cudaFreeHost(h));
+      h = nullptr;
+      PAWPY_CUDA(cudaMallocHost(&h, bytes));
+      cap = bytes;
+    }
+    used = 0;
+  }
+  template <typename T>
+  void upload(DevBuf<T> &d, const std::vector<T> &v) {
+    const size_t bytes = v.size() * sizeof(T);
+    if (!bytes) return;
+    used = (used + 15) & ~size_t(15);
+    PAWPY_REQUIRE(used + bytes <= cap, "pinned staging overflow");
+    char *p = static_cast<char *>(h) + used;
+    std::memcpy(p, v.data(), bytes);
+    used += bytes;
+    PAWPY_CUDA(cudaMemcpyAsync(d.p, p, bytes, cudaMemcpyHostToDevice, stream()));
+  }
+  void end() {
+    if (!done) PAWPY_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    PAWPY_CUDA(cudaEventRecord(done, stream()));
+  }
+};
+
 struct PairState {
   DevWF *R = nullptr, *S = nullptr;
   std::vector<int> N_R, N_S, N_RS_R, N_RS_S;
@@ -249,6 +293,7 @@ struct PairState {
   DevBuf<double2> b_val;
   DevBuf<double2> pair_phase;  // [nk][npairs]
   DevBuf<float2> b_val32;      // [nk][entries]: b_val times the column's pair phase, FP32
+  PinnedStage aug_stage;       // host staging of the lists above
   // aug_recip: set by overlap_setup_recip (the overlaps then follow that method). The
   // augmentation coefficients of R's bands on its N_R sites and of S's bands on its N_S
   // sites, [nk][nband][Wpad] in the sorted plane-wave order (empty when the list is);
@@ -2360,26 +2405,31 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
       ph[(size_t)k * npairs + p] = make_double2(std::cos(a), std::sin(a));
     }
   }
+  // FP32 entries with the pair phase of their column folded in, per k-point (on the device)
+  const size_t ne = std::max<size_t>(1, b_val.size());
+  std::vector<int> e_pair(ne, -1);
+  for (size_t c = 0; c + 1 < b_ptr.size(); c++)
+    for (int e = b_ptr[c]; e < b_ptr[c + 1]; e++) e_pair[e] = b_pair[c];
+  // the lists go up through pinned staging: the host does not wait for the projections queued
+  // before them
+  ps.aug_stage.begin(16 * 8 + sizeof(int) * (a_src.size() + b_ptr.size() + b_col.size() + b_pair.size() + ne) +
+                     sizeof(double2) * (b_val.size() + ph.size()));
   ps.a_src.alloc(std::max(1, ps.Kc));
-  ps.a_src.upload(a_src.data(), a_src.size());
+  ps.aug_stage.upload(ps.a_src, a_src);
   ps.b_ptr.alloc(b_ptr.size());
-  ps.b_ptr.upload(b_ptr.data(), b_ptr.size());
+  ps.aug_stage.upload(ps.b_ptr, b_ptr);
   ps.b_col.alloc(std::max<size_t>(1, b_col.size()));
-  ps.b_col.upload(b_col.data(), b_col.size());
+  ps.aug_stage.upload(ps.b_col, b_col);
   ps.b_val.alloc(std::max<size_t>(1, b_val.size()));
-  ps.b_val.upload(b_val.data(), b_val.size());
+  ps.aug_stage.upload(ps.b_val, b_val);
   ps.b_pair.alloc(std::max<size_t>(1, b_pair.size()));
-  ps.b_pair.upload(b_pair.data(), b_pair.size());
+  ps.aug_stage.upload(ps.b_pair, b_pair);
   ps.pair_phase.alloc(ph.size());
-  ps.pair_phase.upload(ph.data(), ph.size());
+  ps.aug_stage.upload(ps.pair_phase, ph);
   {
-    // FP32 entries with the pair phase of their column folded in, per k-point (on the device)
-    const size_t ne = std::max<size_t>(1, b_val.size());
-    std::vector<int> e_pair(ne, -1);
-    for (size_t c = 0; c + 1 < b_ptr.size(); c++)
-      for (int e = b_ptr[c]; e < b_ptr[c + 1]; e++) e_pair[e] = b_pair[c];
     DevBuf<int> e_pair_d(ne);
-    e_pair_d.upload(e_pair.data(), ne);
+    ps.aug_stage.upload(e_pair_d, e_pair);
+    ps.aug_stage.end();
     ps.b_val32.alloc((size_t)S.nk * ne);
     launch_aug_val32(ps.b_val.p, e_pair_d.p, (int)b_val.size(), (int)ne, ps.pair_phase.p, std::max(1, npairs), S.nk,
                      ps.b_val32.p);
