@@ -229,7 +229,9 @@ struct AugKey {
 
 // Pinned host staging for uploads issued behind long device work: a copy from pinned memory
 // returns at once, where one from pageable memory can wait for the stream's earlier launches.
-// begin() waits for the previous round's copies before the buffer is rewritten.
+// One per host thread (aug_stage), kept for the thread's life: pinning and unpinning host
+// memory is slow and can wait for the device. begin() waits for the previous round's copies
+// before the buffer is rewritten.
 struct PinnedStage {
   void *h = nullptr;
   size_t cap = 0, used = 0;
@@ -271,6 +273,11 @@ struct PinnedStage {
   }
 };
 
+static PinnedStage &aug_stage() {
+  static thread_local PinnedStage s;
+  return s;
+}
+
 struct PairState {
   DevWF *R = nullptr, *S = nullptr;
   std::vector<int> N_R, N_S, N_RS_R, N_RS_S;
@@ -293,7 +300,6 @@ struct PairState {
   DevBuf<double2> b_val;
   DevBuf<double2> pair_phase;  // [nk][npairs]
   DevBuf<float2> b_val32;      // [nk][entries]: b_val times the column's pair phase, FP32
-  PinnedStage aug_stage;       // host staging of the lists above
   // aug_recip: set by overlap_setup_recip (the overlaps then follow that method). The
   // augmentation coefficients of R's bands on its N_R sites and of S's bands on its N_S
   // sites, [nk][nband][Wpad] in the sorted plane-wave order (empty when the list is);
@@ -2412,24 +2418,24 @@ static void ensure_aug(PairState &ps, const std::vector<int> lists[6], int flip)
     for (int e = b_ptr[c]; e < b_ptr[c + 1]; e++) e_pair[e] = b_pair[c];
   // the lists go up through pinned staging: the host does not wait for the projections queued
   // before them
-  ps.aug_stage.begin(16 * 8 + sizeof(int) * (a_src.size() + b_ptr.size() + b_col.size() + b_pair.size() + ne) +
+  aug_stage().begin(16 * 8 + sizeof(int) * (a_src.size() + b_ptr.size() + b_col.size() + b_pair.size() + ne) +
                      sizeof(double2) * (b_val.size() + ph.size()));
   ps.a_src.alloc(std::max(1, ps.Kc));
-  ps.aug_stage.upload(ps.a_src, a_src);
+  aug_stage().upload(ps.a_src, a_src);
   ps.b_ptr.alloc(b_ptr.size());
-  ps.aug_stage.upload(ps.b_ptr, b_ptr);
+  aug_stage().upload(ps.b_ptr, b_ptr);
   ps.b_col.alloc(std::max<size_t>(1, b_col.size()));
-  ps.aug_stage.upload(ps.b_col, b_col);
+  aug_stage().upload(ps.b_col, b_col);
   ps.b_val.alloc(std::max<size_t>(1, b_val.size()));
-  ps.aug_stage.upload(ps.b_val, b_val);
+  aug_stage().upload(ps.b_val, b_val);
   ps.b_pair.alloc(std::max<size_t>(1, b_pair.size()));
-  ps.aug_stage.upload(ps.b_pair, b_pair);
+  aug_stage().upload(ps.b_pair, b_pair);
   ps.pair_phase.alloc(ph.size());
-  ps.aug_stage.upload(ps.pair_phase, ph);
+  aug_stage().upload(ps.pair_phase, ph);
   {
     DevBuf<int> e_pair_d(ne);
-    ps.aug_stage.upload(e_pair_d, e_pair);
-    ps.aug_stage.end();
+    aug_stage().upload(e_pair_d, e_pair);
+    aug_stage().end();
     ps.b_val32.alloc((size_t)S.nk * ne);
     launch_aug_val32(ps.b_val.p, e_pair_d.p, (int)b_val.size(), (int)ne, ps.pair_phase.p, std::max(1, npairs), S.nk,
                      ps.b_val32.p);

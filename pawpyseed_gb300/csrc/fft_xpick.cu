@@ -72,11 +72,12 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   DirectFn dfn = find_direct(g.N1, g.N3, stile, &bpc);
   const size_t dsmem = xpick_direct_smem(g, bpc);
   allow_smem((const void *)dfn, dsmem);
-  // candidates: 1, 2, 4 band groups per plane of the pipelined kernel; 0 the direct kernel; -1
-  // the tensor-core form (Gamma point, split rows). PAWPY_GPU_XPICK_TC=1 uses the tensor-core
-  // form wherever it applies, 0 never.
+  // candidates: 1, 2, 4 band groups per plane of the pipelined kernel; 0 the direct kernel. The
+  // tensor-core form (Gamma point, split rows) runs only where PAWPY_GPU_XPICK_TC=1 asks for it:
+  // slower than the register transform at the measured shapes, and a persistent kernel holding
+  // every SM's TMEM and shared memory, which stalls concurrent requests' launches.
   const char *tc_env = getenv("PAWPY_GPU_XPICK_TC");
-  const bool tc = stile && xpick_tc_supported(g) && !(tc_env && tc_env[0] == '0');
+  const bool tc = stile && xpick_tc_supported(g) && tc_env && tc_env[0] == '1';
   auto run = [&](int mult) {
     if (mult < 0) {
       launch_xpick_tc(H, g, pl, X, nb, lo_words);
@@ -96,13 +97,12 @@ void launch_fft_x_pick_fast(const float2 *H, const PlaneGeom &g, const PickList 
   // tuned per form and per density of the pick (picked points per grid point, up to 3): a
   // pass dominated by its transform and one dominated by its pick tune apart
   const int density = (int)std::min<long long>(3, pl.npts / std::max(1, g.N1 * g.N2 * g.N3));
-  if (tc && tc_env && tc_env[0] == '1') {
+  if (tc) {
     run(-1);
     note_work("fft_x_pick", 8.0 * ((double)g.n1 * g.N2 * g.N3 + (double)pl.npts) * nb);
     return;
   }
   std::vector<int> cands = {0, 1, 2, 4};
-  if (tc) cands.push_back(-1);
   int mult = tune(std::make_tuple((lo_words ? 3 : 1) + (gamma ? 4 : 0) + 8 * density, g.N1, g.N2, g.N3), cands, run);
   run(mult);
   // algorithmic bytes: the occupied planes of H read, 8 bytes per picked value written
