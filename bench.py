@@ -677,6 +677,31 @@ def run_cpu_report(args):
                               sample=smp.describe())), flush=True)
 
 
+def copy_rates(nbytes):
+    """Host-to-device copy rates of nbytes (cudaMemcpyAsync through torch, CUDA events, best of
+    three): from pinned and from pageable host memory."""
+    import torch
+
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for kind, pin in (("pinned_copy_gb_s", True), ("pageable_copy_gb_s", False)):
+        host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=pin)
+        host.fill_(1)
+        best = float("inf")
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record()
+            dev.copy_(host, non_blocking=pin)
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        out[kind] = nbytes / best / 1e6
+        del host
+    del dev
+    return out
+
+
 def _time_reader(path, nwk, reps):
     from pawpyseed_gb300 import _lib
 
@@ -724,6 +749,25 @@ def run_ingest_report(args):
             t0 = time.perf_counter()
             vaspio.read_wavecar_numpy(path)
             numpy_ms = (time.perf_counter() - t0) * 1e3
+            # the device's in-place read of the host band arrays (the end-to-end step's upload):
+            # device time of its launches against plain host-to-device copies of the same bytes
+            p = L.pawpy_gpu_read_wavefunctions(path.encode(), np.full(nwk, 1.0 / nwk))
+            _lib.check()
+            L.pawpy_gpu_upload(p)
+            L.pawpy_gpu_synchronize()
+            L.pawpy_gpu_release(p)
+            _lib.kernel_stats(reset=True)
+            L.pawpy_gpu_profile(1)
+            L.pawpy_gpu_upload(p)
+            L.pawpy_gpu_synchronize()
+            L.pawpy_gpu_profile(0)
+            st = _lib.kernel_stats(reset=True)
+            L.pawpy_gpu_release(p)
+            L.pawpy_gpu_free_pswf(p)
+            coef_bytes = sum(int(c.nbytes) for c in data["coeffs"])
+            read_ms = st.get("load_host", (float("nan"), 0))[0]
+            link = dict(in_place_read_gb_s=coef_bytes / read_ms / 1e6, in_place_read_ms=read_ms)
+            link.update(copy_rates(coef_bytes))
         lat = np.ascontiguousarray(np.asarray(data["lattice"], dtype=np.float64).reshape(-1))
         ks = [np.ascontiguousarray(k, dtype=np.float64) for k in np.asarray(data["kpts"]).reshape(-1, 3)]
         L.pawpy_gpu_gvectors(lat, ks[0], float(data["encut"]), None, 0)
@@ -741,7 +785,7 @@ def run_ingest_report(args):
                               reader_ms=dev_ms, reader_gb_s=size / dev_ms / 1e6,
                               reader_no_device_ms=host_ms, numpy_reader_ms=numpy_ms,
                               spheres_device_ms=sph_dev_ms, spheres_numpy_ms=sph_np_ms,
-                              host_threads=threads_used())), flush=True)
+                              host_link=link, host_threads=threads_used())), flush=True)
 
 
 def main():
