@@ -41,7 +41,7 @@ def test_reference_extension_links_against_the_library():
     needed = subprocess.run(["readelf", "-d", EXT], capture_output=True, text=True, check=True).stdout
     assert "[libpawpy_gpu.so]" in needed
     names = _library_entry_points()
-    # the hot path of SURVEY's boundary and the rows built after it
+    # the band-projection entry points and those of the aug_recip and real-space methods
     for n in ("pseudoprojection", "get_projector_list", "setup_projections", "onto_projector", "overlap_setup_real",
               "compensation_terms", "fft3d", "overlap_setup_recip", "compensation_terms_recip", "realspace_state",
               "ae_chg_density", "project_realspace_state"):

@@ -183,7 +183,7 @@ def test_potcar_parser_agrees_with_reference_parser():
     import sys
     import types
 
-    src = "/root/reference/pawpyseed/core/wavefunction.py"
+    src = os.path.join(os.environ.get("PAWPY_REFERENCE", "/root/reference"), "pawpyseed/core/wavefunction.py")
     if not os.path.exists(src):
         pytest.skip("reference sources not present")
     from pawpyseed_gb300 import synth, vaspio
