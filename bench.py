@@ -319,6 +319,9 @@ def peaks():
 # pass-A and pass-B launches of one k-point, divided by its band count), per FFT grid
 FFT_TRAFFIC = {
     (60, 60, 60): (47.9e6 + 195.0e6 + 261.2e6 + 99.1e6) / 256.0,
+    # the 216-atom defect's step: k_planes_pipe 81.5 MB read + 375.5 MB written, k_xpick_direct
+    # 456.6 MB read + 1,385 MB written per 128 bands (the picked values of every sphere)
+    (90, 90, 90): (81.5e6 + 375.5e6 + 456.6e6 + 1385.0e6) / 128.0,
 }
 
 
