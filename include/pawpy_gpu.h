@@ -365,6 +365,17 @@ int pawpy_gpu_band_character(double *v, double *c, pswf_t *wf_R, pswf_t *wf_S, i
                              int *N_R, int *N_S, int *N_RS_R, int *N_RS_S, const double *w_v,
                              const double *w_c, int nch, int flip_spin);
 
+/* Noncollinear all-electron real-space wavefunction (ncl_realspace_state, density.c:328-408):
+ * x receives the up then the down spinor component, 2 N1 N2 N3 complex values, each the
+ * collinear realspace_state of its half with its own projections (up_projections,
+ * down_projections). Replaces ncl_realspace_state (pawpyc_extern.pxd:257). */
+void ncl_realspace_state(pawpy_c128 *x, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg, int *labels,
+                         double *coords);
+/* Noncollinear all-electron charge density (ncl_ae_chg_density, density.c:181-204): P +=
+ * sum over occupied bands of (|psi_up|^2 + |psi_down|^2) weight occupation. Replaces
+ * ncl_ae_chg_density (pawpyc_extern.pxd:260). The collinear real-space functions report
+ * status 5 for a noncollinear wavefunction, as these do for a collinear one. */
+void ncl_ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coords);
 /* project_realspace_state for every band of wf at once: out[bS*(NB_R*NK) +
  * bR*NK + k], one contraction per k-point. No counterpart in the reference.
  * Returns 0, or the status. */

@@ -77,6 +77,8 @@ def _declare(L):
     L.remove_phase.argtypes = [_zp, C.c_int, _wfp, _ip]
     L.ae_state_density.argtypes = [_dp, C.c_int, C.c_int, _wfp, _ip, _ip, _dp]
     L.ae_chg_density.argtypes = [_dp, _wfp, _ip, _ip, _dp]
+    L.ncl_realspace_state.argtypes = [_zp, C.c_int, C.c_int, _wfp, _ip, _ip, _dp]
+    L.ncl_ae_chg_density.argtypes = [_dp, _wfp, _ip, _ip, _dp]
     L.project_realspace_state.argtypes = [_zp, C.c_int, _wfp, _wfp, _ip, _ip, _dp, _ip, _dp]
     L.pawpy_gpu_project_realspace_all.restype = C.c_int
     L.pawpy_gpu_project_realspace_all.argtypes = [_zp, _wfp, _wfp, _ip, _ip, _dp, _ip, _dp]

@@ -2002,7 +2002,6 @@ static void do_overlap_setup_recip(pswf_t *wf_R, pswf_t *wf_S, const int *labels
 // The real-space sphere tables of d's sites on grid N (built once per grid and site list).
 static AeTables &ae_tables(DevWF &d, const int *N, const int *labels, const double *coords) {
   PAWPY_REQUIRE(d.tables_ready, "real-space wavefunctions need setup_projections first");
-  PAWPY_REQUIRE(!d.ncl, "real-space wavefunctions of noncollinear wavefunctions are not part of this library");
   const int ns = (int)d.labels.size();
   std::vector<int> lab(labels, labels + ns);
   std::vector<double> crd(coords, coords + 3 * (size_t)ns);
@@ -2830,6 +2829,8 @@ static void realspace_overlaps(pswf_t *wf_S, pswf_t *wf_R, const int *fftg, cons
                                const int *labels_R, const double *coords_R, int s0, int ns, pawpy_c128 *out) {
   DevWF &S = mirror(wf_S);
   DevWF &R = mirror(wf_R);
+  if (S.ncl || R.ncl)
+    throw Error(ERR_UNSUPPORTED, "real-space projections of noncollinear wavefunctions are not part of this library");
   PAWPY_REQUIRE(S.nk == R.nk, "basis and defect differ in k-points");
   PAWPY_REQUIRE(s0 >= 0 && ns >= 1 && s0 + ns <= S.nband, "band index out of range");
   AeTables &tS = ae_tables(S, fftg, labels, coords);
@@ -2863,6 +2864,7 @@ void realspace_state(pawpy_c128 *x, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, in
   HostPhase hp_api("realspace_state");
   PAWPY_REQUIRE(x && wf && fftg && labels && coords, "realspace_state: NULL argument");
   DevWF &d = mirror(wf);
+  if (d.ncl) throw Error(ERR_UNSUPPORTED, "realspace_state: a noncollinear wavefunction (use the ncl_ functions)");
   PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < d.nband && KPOINT_NUM >= 0 && KPOINT_NUM < d.nk,
                 "realspace_state: band or k-point index out of range");
   AeTables &t = ae_tables(d, fftg, labels, coords);
@@ -2896,6 +2898,7 @@ void ae_state_density(double *P, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *
   HostPhase hp_api("ae_state_density");
   PAWPY_REQUIRE(P && wf && fftg && labels && coords, "ae_state_density: NULL argument");
   DevWF &d = mirror(wf);
+  if (d.ncl) throw Error(ERR_UNSUPPORTED, "ae_state_density: a noncollinear wavefunction (use the ncl_ functions)");
   PAWPY_REQUIRE(BAND_NUM >= 0 && BAND_NUM < d.nband && KPOINT_NUM >= 0 && KPOINT_NUM < d.nk,
                 "ae_state_density: band or k-point index out of range");
   AeTables &t = ae_tables(d, fftg, labels, coords);
@@ -2917,6 +2920,7 @@ void ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coord
   HostPhase hp_api("ae_chg_density");
   PAWPY_REQUIRE(P && wf && fftg && labels && coords, "ae_chg_density: NULL argument");
   DevWF &d = mirror(wf);
+  if (d.ncl) throw Error(ERR_UNSUPPORTED, "ae_chg_density: a noncollinear wavefunction (use ncl_ae_chg_density)");
   AeTables &t = ae_tables(d, fftg, labels, coords);
   const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
   const int bb = ae_batch(t);
@@ -2936,6 +2940,69 @@ void ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coord
       }
     }
     // runs of consecutive occupied bands in batches
+    size_t i = 0;
+    while (i < occ.size()) {
+      size_t j = i + 1;
+      while (j < occ.size() && occ[j] == occ[j - 1] + 1 && (int)(j - i) < bb) j++;
+      const int nb = (int)(j - i);
+      ae_grids(d, t, k, occ[i], nb, g.p);
+      w.upload(wk.data() + i, nb);
+      launch_density(g.p, w.p, nb, n3d, rho.p);
+      i = j;
+    }
+  }
+  rho.download(P, n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+// Noncollinear: the spinor halves of band b are device bands 2b and 2b + 1, each transformed and
+// completed with its own projections (up_projections, down_projections) as a collinear band.
+void ncl_realspace_state(pawpy_c128 *x, int BAND_NUM, int KPOINT_NUM, pswf_t *wf, int *fftg, int *labels,
+                         double *coords) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("ncl_realspace_state");
+  PAWPY_REQUIRE(x && wf && fftg && labels && coords, "ncl_realspace_state: NULL argument");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(d.ncl, "ncl_realspace_state: a collinear wavefunction (use realspace_state)");
+  PAWPY_REQUIRE(BAND_NUM >= 0 && 2 * BAND_NUM < d.nband && KPOINT_NUM >= 0 && KPOINT_NUM < d.nk,
+                "ncl_realspace_state: band or k-point index out of range");
+  AeTables &t = ae_tables(d, fftg, labels, coords);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  DevBuf<float2> g(2 * n3d);
+  ae_grids(d, t, KPOINT_NUM, 2 * BAND_NUM, 2, g.p);
+  DevBuf<double2> o(2 * n3d);
+  launch_scale_to_c128(g.p, 2 * n3d, 1.0, o.p);
+  o.download(reinterpret_cast<double2 *>(x), 2 * n3d);
+  sync();
+  PAWPY_API_END()
+}
+
+// sum over occupied bands of (|psi_up|^2 + |psi_down|^2) weight occupation (density.c:181-204)
+void ncl_ae_chg_density(double *P, pswf_t *wf, int *fftg, int *labels, double *coords) {
+  PAWPY_API_BEGIN
+  HostPhase hp_api("ncl_ae_chg_density");
+  PAWPY_REQUIRE(P && wf && fftg && labels && coords, "ncl_ae_chg_density: NULL argument");
+  DevWF &d = mirror(wf);
+  PAWPY_REQUIRE(d.ncl, "ncl_ae_chg_density: a collinear wavefunction (use ae_chg_density)");
+  AeTables &t = ae_tables(d, fftg, labels, coords);
+  const long long n3d = (long long)fftg[0] * fftg[1] * fftg[2];
+  const int bb = std::max(2, ae_batch(t) / 2 * 2);
+  DevBuf<float2> g((size_t)std::min(bb, d.nband) * n3d);
+  DevBuf<double> rho(n3d), w((size_t)d.nband);
+  rho.upload(P, n3d);
+  for (int k = 0; k < d.nk; k++) {
+    // both halves of every occupied band, weight x occupation (no spin factor)
+    std::vector<int> occ;
+    std::vector<double> wk;
+    for (int b = 0; b < d.nband / 2; b++) {
+      const band_t *bd = wf->kpts[k]->bands[b];
+      if (bd->occ > 0)
+        for (int h = 0; h < 2; h++) {
+          occ.push_back(2 * b + h);
+          wk.push_back(wf->kpts[k]->weight * bd->occ);
+        }
+    }
     size_t i = 0;
     while (i < occ.size()) {
       size_t j = i + 1;

@@ -360,6 +360,53 @@ class NCLWavefunction(Wavefunction):
 
     _NCL = True
 
+    def get_state_realspace(self, b, k, s, dim=None, remove_phase=False):
+        """All-electron spinor components of band b, k-point k, spin s on the grid dim (default the
+        wavefunction's own): (up, down), complex128 [N1, N2, N3] each (ncl_realspace_state,
+        density.c:328-408; pawpyc.pyx:563-580)."""
+        self.check_c_projectors()
+        self._check_bks(b, k, s)
+        g = self._grid(dim, False)
+        n = int(np.prod(g))
+        res = np.zeros(2 * n, dtype=np.complex128)
+        L = _lib.lib()
+        L.ncl_realspace_state(res, int(b), int(k + s * self.nwk), self._ptr, g, self.nums, self.coords)
+        _lib.check()
+        up, down = res[:n].copy(), res[n:].copy()
+        if remove_phase:
+            for half in (up, down):
+                L.remove_phase(half, int(k + s * self.nwk), self._ptr, g)
+                _lib.check()
+        return up.reshape(tuple(g)), down.reshape(tuple(g))
+
+    def get_state_realspace_density(self, b, k, s, dim=None):
+        """|psi_up|^2 + |psi_down|^2 of one band on the grid dim (default twice the wavefunction's)."""
+        up, down = self.get_state_realspace(b, k, s, self._grid(dim, True))
+        return np.abs(up) ** 2 + np.abs(down) ** 2
+
+    def get_realspace_density(self, dim=None, bands=None):
+        """All-electron charge density of the occupied bands on the grid dim (default twice the
+        wavefunction's grid): ncl_ae_chg_density (density.c:181-204; pawpyc.pyx:582-588)."""
+        if bands is not None:
+            raise ValueError("band-resolved densities are not defined for noncollinear wavefunctions")
+        self.check_c_projectors()
+        g = self._grid(dim, True)
+        res = np.zeros(int(np.prod(g)), dtype=np.float64)
+        _lib.lib().ncl_ae_chg_density(res, self._ptr, g, self.nums, self.coords)
+        _lib.check()
+        return res.reshape(tuple(g))
+
+    def write_state_realspace(self, b, k, s, fileprefix="", dim=None, scale=1, remove_phase=False):
+        """Writes the real and imaginary parts of both spinor components to
+        <prefix>B<b>K<k>S<s>_UP_REAL.vasp, _UP_IMAG, _DOWN_REAL, _DOWN_IMAG (noncollinear.py:98-147);
+        returns (up, down)."""
+        up, down = self.get_state_realspace(b, k, s, dim, remove_phase)
+        base = "%sB%dK%dS%d" % (fileprefix, b, k, s)
+        for tag, v in (("UP", up), ("DOWN", down)):
+            self._write_volumetric("%s_%s_REAL.vasp" % (base, tag), np.real(v), v.shape, scale)
+            self._write_volumetric("%s_%s_IMAG.vasp" % (base, tag), np.imag(v), v.shape, scale)
+        return up, down
+
     def spinor_projections(self, band, k):
         """(<p|psi_up>, <p|psi_down>) of one band at k-point index k (spin-major), complex128
         over every site's lm channels in site order."""

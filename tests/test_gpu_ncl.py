@@ -111,3 +111,43 @@ def test_mixed_collinear_noncollinear_overlaps_are_refused():
     _lib.lib().pseudoprojection(res, b.wf_ptr, a.wf_ptr, 0, 0)
     with pytest.raises(_lib.PAWpyGPUError, match="noncollinear"):
         _lib.check()
+
+
+def test_ncl_realspace_state_and_density_match_oracle_on_each_half():
+    """ncl_realspace_state (density.c:328-408): the up and down components are the collinear
+    real-space states of the two halves with their own projections; ncl_ae_chg_density
+    (density.c:181-204) sums |up|^2 + |down|^2 x weight x occupation (no spin factor), so it is
+    half the sum of the two halves' collinear densities (whose factor is 2 / nspin = 2).
+    Tolerance 1e-5 of the largest magnitude, as the collinear real-space test."""
+    import oracle as orc
+
+    from pawpyseed_gb300.wavefunction import NCLWavefunction
+
+    bs, cr, w, data = ncl_case()
+    wf = NCLWavefunction.from_arrays(bs, cr, w["dim"], data)
+    wf.check_c_projectors()
+    N = np.asarray(w["dim"], dtype=np.int32)
+    halves = []
+    for h in (0, 1):
+        ow = orc.OracleWavefunction(data=half(data, h), struct=bs, cr=cr, dim=w["dim"])
+        ow.setup_projectors()
+        halves.append(ow)
+    for b, k in ((0, 0), (3, 1)):
+        up, down = wf.get_state_realspace(b, k, 0, dim=N)
+        for mine, ow in ((up, halves[0]), (down, halves[1])):
+            truth = ow.realspace_state(b, k, N)
+            assert np.abs(mine - truth).max() <= 1e-5 * np.abs(truth).max()
+    rho = wf.get_realspace_density(dim=N)
+    rtruth = 0.5 * (halves[0].ae_chg_density(N) + halves[1].ae_chg_density(N))
+    assert np.abs(rho - rtruth).max() <= 1e-5 * np.abs(rtruth).max()
+
+
+def test_collinear_realspace_functions_refuse_noncollinear_wavefunctions():
+    from pawpyseed_gb300 import _lib
+    from pawpyseed_gb300.wavefunction import NCLWavefunction, Wavefunction
+
+    bs, cr, w, data = ncl_case()
+    wf = NCLWavefunction.from_arrays(bs, cr, w["dim"], data)
+    wf.check_c_projectors()
+    with pytest.raises(_lib.PAWpyGPUError):
+        Wavefunction.get_state_realspace(wf, 0, 0, 0)
