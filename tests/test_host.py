@@ -311,3 +311,37 @@ def test_defect_band_analysis_rejects_out_of_range_bands(bad):
     pr.band_character = no_device
     with pytest.raises(ValueError, match="Band index out of range"):
         pr.defect_band_analysis(band_list=bad)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_reader_spheres_without_a_device_match_reference_enumeration(seed, tmp_path):
+    """Without a CUDA device the reader enumerates the plane-wave spheres on the host threads with
+    the reference's expression (gsphere_keep, the test the device path applies to the points it
+    leaves undecided): bit-identical lists for triclinic cells, including k-points whose sphere
+    has a plane wave exactly on ENCUT."""
+    from test_gpu_gsphere import _etot, _rec, reference_gvectors
+
+    from pawpyseed_gb300 import _lib, vaspio
+
+    rng = np.random.default_rng(500 + seed)
+    lat = np.diag(rng.uniform(3.0, 5.0, 3)) + rng.uniform(-1.0, 1.0, (3, 3)) * (1 - np.eye(3))
+    kpts = np.array([rng.uniform(-0.5, 0.5, 3), np.zeros(3)])
+    encut = float(rng.uniform(120.0, 220.0))
+    if seed % 2:
+        # ENCUT exactly the energy of a plane wave of the second k-point (on the cutoff)
+        encut = _etot(_rec(lat), [0.0, 0.0, 0.0], (2, -1, 1))
+    gs = [reference_gvectors(lat, k, encut) for k in kpts]
+    coeffs = [np.ones((2, g.shape[0]), np.complex64) for g in gs]
+    path = str(tmp_path / "WAVECAR")
+    vaspio.write_wavecar(path, lat, encut, kpts, coeffs, np.zeros((2, 2)), np.zeros((2, 2)))
+    L = _lib.lib()
+    p = L.pawpy_gpu_read_wavefunctions(path.encode(), np.full(2, 0.5))
+    _lib.check()
+    try:
+        w = p.contents
+        for k in range(2):
+            kp = w.kpts[k].contents
+            g = np.ctypeslib.as_array(kp.Gs, shape=(3 * kp.num_waves,)).reshape(-1, 3)
+            assert np.array_equal(g, gs[k])
+    finally:
+        L.pawpy_gpu_free_pswf(p)
