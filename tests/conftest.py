@@ -68,7 +68,7 @@ def workload_dirs(tmp_path_factory):
 
 @pytest.fixture(scope="session")
 def realspace_dirs(tmp_path_factory):
-    """The 64-atom workload reduced to 4 bands and 2 k-points (the real-space golden fixture's)."""
+    """The 8-atom workload reduced to 4 bands and 2 k-points (the real-space golden fixture's)."""
     from pawpyseed_gb300 import synth
 
     return synth.write_workload(str(tmp_path_factory.mktemp("realspace")), 0, nband=4, nk=2)

@@ -22,11 +22,15 @@ Fixtures:
   band->CAs of band 0 of each side that has them, per k-point, first 4096
   plane waves in file order (``recip_CA_<side>_k<k>``).
 * ``realspace_cfg0.npz`` -- the real-space functions of density.c on the
-  64-atom workload reduced to 4 bands and 2 k-points, on the defect's grid:
+  8-atom workload reduced to 4 bands and 2 k-points, on the defect's grid:
   ``realspace_state`` of band 1 at k-point 1 (``state_b1_k1``),
   ``ae_chg_density`` of the defect (``rho``), and
   ``project_realspace_state`` of every defect band onto the basis (``proj``,
   [band][basis band * nk + k]).
+* ``realspace_ncl_cfg0.npz`` -- the noncollinear real-space functions of
+  density.c (``ncl_realspace_state``, up then down component, of band 3 at
+  k-point 1; ``ncl_ae_chg_density``) on a spinor
+  wavefunction of the 8-atom cell (4 bands, 2 k-points).
 
 The reference tree is read from $PAWPY_REFERENCE (default /root/reference).
 """
@@ -185,12 +189,58 @@ def realspace_fixture():
         shutil.rmtree(tmp)
 
 
+def ncl_realspace_inputs():
+    """The noncollinear case of the real-space fixture: the 8-atom cell, 4 spinor bands, 2
+    k-points, species A only, coefficients seed 77 (tests/test_oracle.py rebuilds the same)."""
+    w = synth.small_workload(0, nband=4, nk=2)
+    bs, _ = synth.structures(0)
+    data = synth.wavefunction_data(bs, w, 77, ncl=True)
+    return bs, w, data
+
+
+def ncl_realspace_fixture():
+    import ref_harness as rh
+
+    lib = rh.load_ref()
+    zp = np.ctypeslib.ndpointer(dtype=np.complex128, flags="C_CONTIGUOUS")
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+    wfp = C.POINTER(rh.S.pswf_t)
+    lib.ncl_realspace_state.argtypes = [zp, C.c_int, C.c_int, wfp, ip, ip, dp]
+    lib.ncl_ae_chg_density.argtypes = [dp, wfp, ip, ip, dp]
+    tmp = tempfile.mkdtemp()
+    try:
+        bs, w, data = ncl_realspace_inputs()
+        path = os.path.join(tmp, "ncl")
+        synth.write_structure_dir(path, bs, data, w["dim"], symbols=["A"])
+        d = rh.RefWavefunction(lib, path)
+        assert d.ptr.contents.is_ncl == 1
+        d.setup_projectors()
+        fftg = np.ascontiguousarray(d.dim, dtype=np.int32)
+        n = int(np.prod(fftg))
+        out = dict(fp=fingerprint(path), fftg=fftg)
+        x = np.zeros(2 * n, np.complex128)
+        lib.ncl_realspace_state(x, 3, 1, d.ptr, fftg, d.nums, d.coords)
+        out["state_b3_k1"] = x.reshape((2,) + tuple(fftg))
+        rho = np.zeros(n)
+        lib.ncl_ae_chg_density(rho, d.ptr, fftg, d.nums, d.coords)
+        out["rho"] = rho.reshape(tuple(fftg))
+        np.savez_compressed(os.path.join(HERE, "realspace_ncl_cfg0.npz"), **out)
+        print("realspace_ncl_cfg0 written: grid", tuple(fftg), "sum rho dV =",
+              rho.sum() * abs(np.linalg.det(d.struct.lattice)) / n)
+        d.free()
+    finally:
+        shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["fft"] + list(CASES) + ["realspace"]
+    which = sys.argv[1:] or ["fft"] + list(CASES) + ["realspace", "realspace_ncl"]
     for w in which:
         if w == "fft":
             fft_fixture()
         elif w == "realspace":
             realspace_fixture()
+        elif w == "realspace_ncl":
+            ncl_realspace_fixture()
         else:
             case_fixture(w, *CASES[w])

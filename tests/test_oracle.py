@@ -9,7 +9,9 @@ warning is raised and the comparisons run at tolerances that allow for it.
 import numpy as np
 import pytest
 
-from conftest import CASES, same_golden_inputs
+import warnings
+
+from conftest import CASES, GoldenInputsDiffer, fingerprint, same_golden_inputs
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -178,3 +180,41 @@ def test_oracle_realspace_matches_reference(realspace_dirs, golden):
         R = np.array([b.realspace_state(bb, k, N).ravel() for bb in range(b.nband)])
         proj[:, k::nk] = S @ R.conj().T * vol / n3
     assert np.abs(proj - g["proj"]).max() <= tol
+
+
+def test_oracle_ncl_realspace_matches_reference(tmp_path, golden):
+    """ncl_realspace_state and ncl_ae_chg_density (density.c:181-204, 328-408) of the reference on
+    a spinor wavefunction against the oracle's collinear real-space functions on each spinor half
+    (each with its own projections, as onto_projector_ncl gives them, projector.c:359-392): the
+    up and down components are the halves' states, and the density, which carries no spin
+    factor, is half the sum of the halves' collinear densities (factor 2 / nspin = 2). This is the
+    restatement the noncollinear device functions are checked against."""
+    import oracle as orc
+
+    from pawpyseed_gb300 import synth, vaspio
+
+    g = golden("realspace_ncl_cfg0")
+    w = synth.small_workload(0, nband=4, nk=2)
+    bs, _ = synth.structures(0)
+    data = synth.wavefunction_data(bs, w, 77, ncl=True)
+    synth.write_structure_dir(str(tmp_path), bs, data, w["dim"], symbols=["A"])
+    same = fingerprint(str(tmp_path)) == str(g["fp"])
+    if not same:
+        warnings.warn(GoldenInputsDiffer("realspace_ncl_cfg0: regenerated inputs differ in bytes from the "
+                                         "golden fixture's; comparing at the FP64-truth tolerance instead"))
+    tol = 1e-12 if same else 1e-5
+    cr = vaspio.CoreRegion(synth.potcar_text(["A"]))
+    N = g["fftg"]
+    halves = []
+    for h in (0, 1):
+        half = dict(data, ncl=False)
+        half["coeffs"] = [np.ascontiguousarray(c[:, h * gs.shape[0]:(h + 1) * gs.shape[0]])
+                          for c, gs in zip(data["coeffs"], data["gs"])]
+        ow = orc.OracleWavefunction(data=half, struct=bs, cr=cr, dim=w["dim"])
+        ow.setup_projectors()
+        halves.append(ow)
+    for h in (0, 1):
+        x = halves[h].realspace_state(3, 1, N)
+        assert np.abs(x - g["state_b3_k1"][h]).max() <= tol
+    rho = 0.5 * (halves[0].ae_chg_density(N) + halves[1].ae_chg_density(N))
+    assert np.abs(rho - g["rho"]).max() <= tol
