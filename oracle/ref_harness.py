@@ -130,11 +130,12 @@ class RefWavefunction:
         self.grid_encut = grid_encut
 
     def projections(self, band, kidx, which="projections"):
-        """Per-site <p|psi> (or wave_projections) of one band as a list of complex arrays."""
+        """Per-site <p|psi> (projections, or up_projections / down_projections of a spinor band),
+        or the wave_projections, of one band as a list of complex arrays."""
         kp = self.ptr.contents.kpts[kidx].contents
         bd = kp.bands[band].contents
         arr = getattr(bd, which)
-        n = len(self.struct) if which == "projections" else self.ptr.contents.wp_num
+        n = self.ptr.contents.wp_num if which == "wave_projections" else len(self.struct)
         out = []
         for s in range(n):
             p = arr[s]

@@ -29,8 +29,9 @@ Fixtures:
   [band][basis band * nk + k]).
 * ``realspace_ncl_cfg0.npz`` -- the noncollinear real-space functions of
   density.c (``ncl_realspace_state``, up then down component, of band 3 at
-  k-point 1; ``ncl_ae_chg_density``) on a spinor
-  wavefunction of the 8-atom cell (4 bands, 2 k-points).
+  k-point 1; ``ncl_ae_chg_density``) and the spinor projections of
+  ``onto_projector_ncl`` (``P_up``, ``P_down``: [k][band][sites x channels]) on
+  a spinor wavefunction of the 8-atom cell (4 bands, 2 k-points).
 
 The reference tree is read from $PAWPY_REFERENCE (default /root/reference).
 """
@@ -219,6 +220,10 @@ def ncl_realspace_fixture():
         fftg = np.ascontiguousarray(d.dim, dtype=np.int32)
         n = int(np.prod(fftg))
         out = dict(fp=fingerprint(path), fftg=fftg)
+        nk = d.nwk * d.nspin
+        for side in ("up", "down"):
+            out["P_" + side] = np.array([[np.concatenate(d.projections(b, k, side + "_projections"))
+                                          for b in range(d.nband)] for k in range(nk)])
         x = np.zeros(2 * n, np.complex128)
         lib.ncl_realspace_state(x, 3, 1, d.ptr, fftg, d.nums, d.coords)
         out["state_b3_k1"] = x.reshape((2,) + tuple(fftg))

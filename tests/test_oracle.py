@@ -182,11 +182,12 @@ def test_oracle_realspace_matches_reference(realspace_dirs, golden):
     assert np.abs(proj - g["proj"]).max() <= tol
 
 
-def test_oracle_ncl_realspace_matches_reference(tmp_path, golden):
-    """ncl_realspace_state and ncl_ae_chg_density (density.c:181-204, 328-408) of the reference on
-    a spinor wavefunction against the oracle's collinear real-space functions on each spinor half
-    (each with its own projections, as onto_projector_ncl gives them, projector.c:359-392): the
-    up and down components are the halves' states, and the density, which carries no spin
+def test_oracle_ncl_matches_reference(tmp_path, golden):
+    """The spinor projections (onto_projector_ncl, projector.c:359-392), ncl_realspace_state and
+    ncl_ae_chg_density (density.c:181-204, 328-408) of the reference on a spinor wavefunction
+    against the oracle's collinear functions on each spinor half: up_projections and
+    down_projections are the halves' projections, the up and down components of the state are
+    the halves' states (each with its own projections), and the density, which carries no spin
     factor, is half the sum of the halves' collinear densities (factor 2 / nspin = 2). This is the
     restatement the noncollinear device functions are checked against."""
     import oracle as orc
@@ -213,7 +214,9 @@ def test_oracle_ncl_realspace_matches_reference(tmp_path, golden):
         ow = orc.OracleWavefunction(data=half, struct=bs, cr=cr, dim=w["dim"])
         ow.setup_projectors()
         halves.append(ow)
-    for h in (0, 1):
+    for h, side in ((0, "P_up"), (1, "P_down")):
+        for k in range(halves[h].nk):
+            assert np.abs(halves[h].P[k] - g[side][k]).max() <= (1e-13 if same else 1e-6)
         x = halves[h].realspace_state(3, 1, N)
         assert np.abs(x - g["state_b3_k1"][h]).max() <= tol
     rho = 0.5 * (halves[0].ae_chg_density(N) + halves[1].ae_chg_density(N))
