@@ -20,7 +20,11 @@ static const double kC = 0.262465831;
 
 void spline_coeffs(const double *x, const double *y, int n, double *b, double *c, double *d) {
   // Tridiagonal sweep for the second derivatives M_i (kept in c), then the
-  // polynomial coefficients of each interval.
+  // polynomial coefficients of each interval. The start slope is the first
+  // secant (clamped end; b[0] is then exactly 0); a secant above 0.99e30 selects
+  // the natural end instead. That test is kept only so that the sweep follows the
+  // reference's (utils.c:699-749) operation for operation; the radial functions
+  // of a POTCAR never take it.
   double s0 = (y[1] - y[0]) / (x[1] - x[0]);
   if (s0 > 0.99e30) {
     c[0] = 0;
