@@ -345,3 +345,35 @@ def test_reader_spheres_without_a_device_match_reference_enumeration(seed, tmp_p
             assert np.array_equal(g, gs[k])
     finally:
         L.pawpy_gpu_free_pswf(p)
+
+
+def test_entry_points_record_argument_errors_instead_of_exiting():
+    """The reference's C prints and exits on bad input (utils.c:1100-1118); the library records a
+    status and returns. Arguments that are rejected before any device work: the no-allocation
+    overlap's output limit and K rule (fake device pointers are never touched), and the
+    plane-wave sphere entry point in a process without a device."""
+    import ctypes as C
+
+    from pawpyseed_gb300 import _lib
+
+    L = _lib.lib()
+    L.pawpy_gpu_overlap_noalloc.restype = C.c_int
+    L.pawpy_gpu_overlap_noalloc.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
+                                            C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    fake = C.c_void_p(256)
+    assert L.pawpy_gpu_overlap_noalloc(fake, 16, fake, 16, 4096, 4096, 16, fake, None) < 0
+    with pytest.raises(_lib.PAWpyGPUError, match="scratch limit"):
+        _lib.check()
+    assert L.pawpy_gpu_overlap_noalloc(fake, 32, fake, 32, 8, 8, 24, fake, None) < 0
+    with pytest.raises(_lib.PAWpyGPUError, match="multiple of 16"):
+        _lib.check()
+    assert L.pawpy_gpu_overlap_noalloc(None, 16, fake, 16, 8, 8, 16, fake, None) < 0
+    with pytest.raises(_lib.PAWpyGPUError, match="NULL"):
+        _lib.check()
+    assert L.pawpy_gpu_last_error() == 0
+    lat = np.eye(3) * 5.0
+    n = L.pawpy_gpu_gvectors(np.ascontiguousarray(lat.reshape(-1)), np.zeros(3), 200.0, None, 0)
+    if n >= 0:
+        pytest.skip("a CUDA device is present: the sphere entry point runs")
+    with pytest.raises(_lib.PAWpyGPUError, match="no CUDA device"):
+        _lib.check()
