@@ -247,7 +247,7 @@ static void osbt_setup(osbt *d, double encut, double enbuf, int lmax, int n,
   d->N = N;
   d->lmax = lmax;
   d->ks = malloc(sizeof(double) * N);
-  d->rs = malloc(sizeof(double) * N);
+  d->rs = calloc((size_t)N, sizeof(double));
   d->M = calloc((size_t)(lmax + 1) * N, sizeof(double complex));
   double drho = log(r[1] / r[0]);
   double dt = 2 * O_PI / N / drho;
@@ -514,7 +514,7 @@ int oracle_site_table(const double *L, const int *fftg, const double *coord, dou
         paths[3 * n + 1] = tc[1];
         paths[3 * n + 2] = tc[2];
         double gp[3] = {(double)ii / fftg[0], (double)jj / fftg[1], (double)kk / fftg[2]};
-        double t[3], r;
+        double t[3] = {0, 0, 0}, r = 0;
         min_image(gp, coord, L, t, &r);
         int p = 0;
         for (int q = 0; q < nproj; q++) {

@@ -1,8 +1,9 @@
 /* TEST INFRASTRUCTURE -- the oracle (checker) for the band-projection path.
  *
  * A CPU restatement, in plain C with OpenMP, of the reference pawpyseed
- * algorithm (pawpyseed/core/*.c). Only the tests, the smoke check and the CPU
- * baseline leg of bench.py use it; the product library never links it.
+ * algorithm (the C sources of pawpyseed/core). Only the tests, the smoke
+ * check and the CPU baseline leg of bench.py use it; the product library
+ * never links it.
  * Every function cites the reference lines it follows. All arithmetic is
  * double precision; pseudo overlaps can also be accumulated in single
  * precision to mimic the reference's cblas_cdotc_sub. */
